@@ -1,0 +1,176 @@
+/*
+ * qtnh_cuda.h — C ABI of the GB300 (sm_103a) tensor-contraction engine.
+ *
+ * This is the boundary between host code written against qtnh's C++ API and the
+ * CUDA kernels. Every entry point takes plain pointers and sizes, returns an
+ * int status (QTNH_OK == 0) and records a message readable with qtnh_last_error().
+ *
+ * Element type: complex<double> (the reference's `tel`, include/core/typedefs.hpp:21),
+ * stored as interleaved (re, im) doubles, 16 bytes per element. Tensors are dense
+ * row-major arrays over dis_dims ++ loc_dims (last index fastest,
+ * src/core/utils.cpp:27-46). The reference spreads the leading dis_dims over MPI
+ * ranks; here all slabs are resident in one HBM array in rank order, which is the
+ * same global row-major order, so rescatter and rebcast are metadata-only and
+ * distributed swaps/permutes are on-device transposes.
+ *
+ * Data pointers are device pointers unless named *_host. `stream` is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream). Calls are asynchronous with
+ * respect to the host unless stated otherwise.
+ *
+ * Axis indices are uint16_t like the reference's tidx_tup_st
+ * (include/core/typedefs.hpp:16); QTNH_X (0xFFFF) is the reference's wildcard X
+ * (include/core/typedefs.hpp:55).
+ */
+#ifndef QTNH_CUDA_H
+#define QTNH_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QTNH_ABI_VERSION 1
+#define QTNH_X 0xFFFFu
+#define QTNH_MAX_RANK 64
+
+/* Status codes. The C++ facade maps them back to the reference's exception types. */
+enum {
+  QTNH_OK = 0,
+  QTNH_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument (contract.cpp:210,213; dense.cpp:80,89) */
+  QTNH_ERR_RUNTIME = 2,          /* std::runtime_error (dense.cpp:179; utils.cpp:10)            */
+  QTNH_ERR_OUT_OF_RANGE = 3,     /* std::out_of_range (indexing.cpp:96,118; .at())               */
+  QTNH_ERR_CUDA = 4,             /* CUDA runtime error                                           */
+  QTNH_ERR_NO_MEMORY = 5,        /* device allocation failed                                     */
+  QTNH_ERR_UNSUPPORTED = 6,      /* shape outside what a specialised kernel handles              */
+  QTNH_ERR_CAPACITY = 7          /* output buffer too small (query protocol)                     */
+};
+
+/* Tensor kinds (include/core/typedefs.hpp:36-46, restricted to constructible classes). */
+enum {
+  QTNH_KIND_DENSE = 0, /* DenseTensor  (include/tensor/dense.hpp:75)               */
+  QTNH_KIND_SYMM = 1,  /* SymmTensor   (include/tensor/symm.hpp:93)                */
+  QTNH_KIND_SWAP = 2,  /* SwapTensor   (include/tensor/symm.hpp:230), implicit      */
+  QTNH_KIND_IDEN = 3,  /* IdenTensor   (include/tensor/diag.hpp:204), implicit      */
+  QTNH_KIND_DIAG = 4   /* DiagTensor   (include/tensor/diag.hpp:65), diagonal only  */
+};
+
+/* A tensor as the engine sees it. `data` is a device pointer:
+ *   DENSE/SYMM: all prod(dims) elements;
+ *   DIAG:       prod(input dims) diagonal elements, row-major over the input indices
+ *               (dis inputs then local inputs, include/tensor/symm.hpp:22-45);
+ *   SWAP/IDEN:  NULL (elements are implicit). */
+typedef struct qtnh_tensor_desc {
+  int32_t kind;
+  int32_t ndis;
+  int32_t nloc;
+  int32_t n_dis_in;      /* symmetric family: number of distributed input indices */
+  const uint64_t* dims;  /* ndis + nloc entries, host memory                     */
+  const void* data;
+} qtnh_tensor_desc;
+
+/* ---- library, device and memory --------------------------------------------------- */
+
+/* Message of the last failed call on this host thread (never NULL). */
+const char* qtnh_last_error(void);
+int qtnh_abi_version(void);
+int qtnh_device_count(int* count);
+int qtnh_set_device(int device);
+int qtnh_malloc(void** ptr, size_t bytes);                    /* stream-ordered pool */
+int qtnh_free(void* ptr);
+int qtnh_memcpy_h2d(void* dst, const void* src_host, size_t bytes, void* stream);
+int qtnh_memcpy_d2h(void* dst_host, const void* src, size_t bytes, void* stream);
+int qtnh_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream);
+int qtnh_memset(void* dst, int value, size_t bytes, void* stream);
+int qtnh_stream_synchronize(void* stream);
+/* Number of kernels this library has launched since load (all entry points). */
+uint64_t qtnh_kernel_launch_count(void);
+
+/* ---- data movement: TIDense kernels ------------------------------------------------ */
+
+/* Tensor::permute / TIDense::_permute_internal (src/tensor/dense.cpp:152-169, 354-488):
+ * old axis i moves to new position ptup[i]; out has dims new[ptup[i]] = dims[i].
+ * Bit-exact. `in` and `out` must not overlap. */
+int qtnh_permute(const void* in, void* out, int32_t rank, const uint64_t* dims, const uint16_t* ptup,
+                 void* stream);
+
+/* Tensor::swap / TIDense::_swap_internal (src/tensor/dense.cpp:171-274): exchange two
+ * axes of equal dimension (local, mixed and distributed cases alike). Unequal
+ * dimensions fail with QTNH_ERR_RUNTIME like dense.cpp:178-180. Bit-exact. */
+int qtnh_swap(const void* in, void* out, int32_t rank, const uint64_t* dims, int32_t idx1, int32_t idx2,
+              void* stream);
+
+/* ---- contraction metadata: Tensor::contract (src/tensor/contract.cpp:204-289) ------ */
+
+/* Validates the wires and chooses the dimension replacements exactly as the reference:
+ * default order [t1 open dis, t2 open dis, t1 open loc, t2 open loc] (contract.cpp:220-248)
+ * or, for a symmetric second operand with all inputs wired, the in-place rule
+ * (contract.cpp:250-289). With use_default == 0 the caller's repls are kept.
+ * repls1/repls2 are in/out (rank1 / rank2 entries, QTNH_X for closed indices).
+ * out_dims must hold rank1 + rank2 entries; out_str receives the stretch factor of the
+ * result's broadcaster (product of contracted distributed dimensions, contract.cpp:196-200).
+ * Host-only: needs no GPU. */
+int qtnh_contract_plan(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, int32_t nwires,
+                       const uint16_t* wires, int32_t use_default, uint16_t* repls1, uint16_t* repls2,
+                       int32_t* out_ndis, int32_t* out_nloc, uint64_t* out_dims, uint64_t* out_str);
+
+/* ---- contraction ------------------------------------------------------------------- */
+
+/* Tensor::contract (contract.cpp:204-313 with _contract_dense, 12-201): plans as
+ * qtnh_contract_plan, then computes C[out] = sum over wired index pairs of t1 * t2 with
+ * the result index order given by the replacements. Dispatches to specialised kernels:
+ * symmetric gates applied in place (register-blocked group kernel), diagonal tensors
+ * (streaming phase multiply), swap/identity tensors (transpose, bit-exact), and
+ * everything else to the permute-fused complex GEMM. `out` receives prod(out_dims)
+ * elements (out_capacity is in elements); with out == NULL only the metadata is filled
+ * and QTNH_ERR_CAPACITY is returned. `out` may alias t1->data when the result has the
+ * same size as t1 (the caller gives up t1, as Tensor::contract consumes tp1). */
+int qtnh_contract(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, int32_t nwires, const uint16_t* wires,
+                  int32_t use_default, uint16_t* repls1, uint16_t* repls2, int32_t* out_ndis, int32_t* out_nloc,
+                  uint64_t* out_dims, uint64_t* out_str, void* out, uint64_t out_capacity, void* stream);
+
+/* General dense contraction with explicit output positions (the global form of
+ * _contract_dense): C[...] = sum_wired A * B, where open axis i of A goes to output
+ * position out_pos_a[i] and open axis j of B to out_pos_b[j] (QTNH_X for wired axes).
+ * Permute-fused FP64 complex GEMM. `c` must not overlap `a` or `b`. */
+int qtnh_contract_dense(const void* a, int32_t rank_a, const uint64_t* dims_a, const void* b, int32_t rank_b,
+                        const uint64_t* dims_b, int32_t nwires, const uint16_t* wires, const uint16_t* out_pos_a,
+                        const uint16_t* out_pos_b, void* c, void* stream);
+
+/* ---- symmetric gates and diagonals (the in-place rule, contract.cpp:250-289) -------- */
+
+/* psi'[.., o_j at targets[j], ..] = sum_in G[in, o] psi[.., in_j at targets[j], ..] where
+ * G = gate elements in SymmTensor layout [in_0..in_{k-1}, out_0..out_{k-1}] row-major
+ * (include/tensor/symm.hpp:22-45). All target dims must be equal to the gate's.
+ * In place (state is read and overwritten). Device pointer `gate`. */
+int qtnh_apply_gate(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
+                    const void* gate, void* stream);
+
+/* Several gates applied in list order (each as qtnh_apply_gate), fused into as few
+ * passes over the state as the target sets allow. gate_k[g] targets per gate,
+ * targets: concatenated target lists, gates: device pointers (one per gate). */
+int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32_t ngates, const int32_t* gate_k,
+                          const uint16_t* targets, const void* const* gates, void* stream);
+
+/* DiagTensor contraction in place: psi[x] *= d[x restricted to targets] with d the
+ * diagonal (row-major over the target dims). Device pointer `diag`. */
+int qtnh_apply_diag(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
+                    const void* diag, void* stream);
+
+/* A layer of single-index diagonals in one streaming pass:
+ * psi[x] *= prod_f d_f[x_{axes[f]}], d_f = factors + offset_f (each dims[axes[f]] long,
+ * concatenated in f order). Device pointer `factors`. */
+int qtnh_apply_diag_layer(void* state, int32_t rank, const uint64_t* dims, int32_t nfactors, const uint16_t* axes,
+                          const void* factors, void* stream);
+
+/* ---- reductions (FP64) ------------------------------------------------------------- */
+
+/* sum |x|^2 over n elements, computed in FP64 on the device; result to host. Synchronous. */
+int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QTNH_CUDA_H */

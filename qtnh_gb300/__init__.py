@@ -1,0 +1,233 @@
+"""Python binding of the GB300 tensor-contraction engine (``libqtnh_cuda.so``).
+
+The engine's boundary is the C ABI in ``include/qtnh_cuda.h``; this module binds
+it with ctypes so tests and benchmarks can drive the same entry points a C or C++
+caller uses. PyTorch only supplies device memory and streams: tensors passed in
+are ``torch.complex128`` CUDA tensors (global row-major order over
+``dis_dims + loc_dims``) and results come back the same way.
+
+There is no CPU fallback: every call goes through the CUDA library, and loading
+fails loudly when it has not been built (``python -m qtnh_gb300.build``).
+"""
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "lib", "libqtnh_cuda.so")
+HEADER = os.path.join(ROOT, "include", "qtnh_cuda.h")
+
+X = 0xFFFF
+DENSE, SYMM, SWAP, IDEN, DIAG = 0, 1, 2, 3, 4
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "RUNTIME", 3: "OUT_OF_RANGE", 4: "CUDA", 5: "NO_MEMORY",
+          6: "UNSUPPORTED", 7: "CAPACITY"}
+
+
+class QtnhError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class InvalidArgument(QtnhError, ValueError):
+    pass
+
+
+class OutOfRange(QtnhError, IndexError):
+    pass
+
+
+_EXC = {1: InvalidArgument, 3: OutOfRange}
+
+
+class TensorDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("ndis", ctypes.c_int32), ("nloc", ctypes.c_int32),
+                ("n_dis_in", ctypes.c_int32), ("dims", ctypes.POINTER(ctypes.c_uint64)), ("data", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """Load ``libqtnh_cuda.so`` (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libqtnh_cuda.so is not built; run `python -m qtnh_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        L.qtnh_last_error.restype = ctypes.c_char_p
+        L.qtnh_kernel_launch_count.restype = ctypes.c_uint64
+        _lib = L
+    return _lib
+
+
+def declared_functions():
+    """Names of the entry points declared in include/qtnh_cuda.h."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(qtnh_\w+)\s*\(", src)))
+
+
+def check(rc):
+    if rc != 0:
+        msg = lib().qtnh_last_error().decode()
+        raise _EXC.get(rc, QtnhError)(rc, msg)
+
+
+def launches():
+    """Kernels launched by the library since it was loaded."""
+    return int(lib().qtnh_kernel_launch_count())
+
+
+def _u64(vals):
+    vals = [int(v) for v in vals]
+    return (ctypes.c_uint64 * max(1, len(vals)))(*vals)
+
+
+def _u16(vals):
+    vals = [int(v) for v in vals]
+    return (ctypes.c_uint16 * max(1, len(vals)))(*vals)
+
+
+def _stream(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _check_c128(t):
+    import torch
+    if t.dtype != torch.complex128 or not t.is_cuda or not t.is_contiguous():
+        raise TypeError("expected a contiguous complex128 CUDA tensor")
+
+
+class Tensor:
+    """A tensor as the engine sees it: kind, dis/loc dims, input count, device data."""
+
+    def __init__(self, kind, dis, loc, data=None, n_dis_in=0):
+        self.kind = kind
+        self.dis = [int(d) for d in dis]
+        self.loc = [int(d) for d in loc]
+        self.n_dis_in = int(n_dis_in)
+        self.data = data
+        if data is not None:
+            _check_c128(data)
+
+    @property
+    def dims(self):
+        return self.dis + self.loc
+
+    def desc(self):
+        self._dims = _u64(self.dims)
+        return TensorDesc(self.kind, len(self.dis), len(self.loc), self.n_dis_in,
+                          ctypes.cast(self._dims, ctypes.POINTER(ctypes.c_uint64)),
+                          ctypes.c_void_p(self.data.data_ptr() if self.data is not None else 0))
+
+
+def contract_plan(t1, t2, wires, repls=None):
+    """Tensor::contract metadata (host only). Returns (dis, loc, repls1, repls2, str)."""
+    r1, r2 = len(t1.dims), len(t2.dims)
+    w = _u16([x for p in wires for x in p])
+    rep1 = (ctypes.c_uint16 * max(1, r1))(*(repls[0] if repls else [X] * r1))
+    rep2 = (ctypes.c_uint16 * max(1, r2))(*(repls[1] if repls else [X] * r2))
+    ndis, nloc, st = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint64()
+    out_dims = (ctypes.c_uint64 * max(1, r1 + r2))()
+    d1, d2 = t1.desc(), t2.desc()
+    check(lib().qtnh_contract_plan(ctypes.byref(d1), ctypes.byref(d2), ctypes.c_int32(len(wires)), w,
+                                   ctypes.c_int32(0 if repls else 1), rep1, rep2, ctypes.byref(ndis),
+                                   ctypes.byref(nloc), out_dims, ctypes.byref(st)))
+    dims = [int(out_dims[i]) for i in range(ndis.value + nloc.value)]
+    return (dims[:ndis.value], dims[ndis.value:], [rep1[i] for i in range(r1)], [rep2[i] for i in range(r2)],
+            int(st.value))
+
+
+def contract(t1, t2, wires, repls=None, out=None, stream=None):
+    """Tensor::contract on the device. Returns (Tensor result, repls1, repls2, str)."""
+    import torch
+    dis, loc, rep1, rep2, st = contract_plan(t1, t2, wires, repls)
+    n = 1
+    for d in dis + loc:
+        n *= d
+    if out is None:
+        out = torch.empty(n, dtype=torch.complex128, device="cuda")
+    r1, r2 = len(t1.dims), len(t2.dims)
+    w = _u16([x for p in wires for x in p])
+    a1 = (ctypes.c_uint16 * max(1, r1))(*rep1)
+    a2 = (ctypes.c_uint16 * max(1, r2))(*rep2)
+    ndis, nloc, stv = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint64()
+    out_dims = (ctypes.c_uint64 * max(1, r1 + r2))()
+    d1, d2 = t1.desc(), t2.desc()
+    check(lib().qtnh_contract(ctypes.byref(d1), ctypes.byref(d2), ctypes.c_int32(len(wires)), w, ctypes.c_int32(0),
+                              a1, a2, ctypes.byref(ndis), ctypes.byref(nloc), out_dims, ctypes.byref(stv), _ptr(out),
+                              ctypes.c_uint64(out.numel()), _stream(stream)))
+    return Tensor(DENSE, dis, loc, out.reshape(-1)), rep1, rep2, st
+
+
+def permute(x, dims, ptup, out=None, stream=None):
+    import torch
+    _check_c128(x)
+    new = [0] * len(dims)
+    for i, p in enumerate(ptup):
+        new[p] = dims[i]
+    if out is None:
+        out = torch.empty(x.numel(), dtype=torch.complex128, device=x.device)
+    check(lib().qtnh_permute(_ptr(x), _ptr(out), ctypes.c_int32(len(dims)), _u64(dims), _u16(ptup), _stream(stream)))
+    return out
+
+
+def swap(x, dims, i1, i2, out=None, stream=None):
+    import torch
+    _check_c128(x)
+    if out is None:
+        out = torch.empty(x.numel(), dtype=torch.complex128, device=x.device)
+    check(lib().qtnh_swap(_ptr(x), _ptr(out), ctypes.c_int32(len(dims)), _u64(dims), ctypes.c_int32(i1),
+                          ctypes.c_int32(i2), _stream(stream)))
+    return out
+
+
+def apply_gate(state, dims, targets, gate, stream=None):
+    _check_c128(state)
+    _check_c128(gate)
+    check(lib().qtnh_apply_gate(_ptr(state), ctypes.c_int32(len(dims)), _u64(dims), ctypes.c_int32(len(targets)),
+                                _u16(targets), _ptr(gate), _stream(stream)))
+    return state
+
+
+def apply_gate_layer(state, dims, gates, stream=None):
+    """gates: list of (targets, device gate tensor)."""
+    _check_c128(state)
+    ks = (ctypes.c_int32 * max(1, len(gates)))(*[len(t) for t, _ in gates])
+    tg = _u16([x for t, _ in gates for x in t])
+    ptrs = (ctypes.c_void_p * max(1, len(gates)))(*[g.data_ptr() for _, g in gates])
+    check(lib().qtnh_apply_gate_layer(_ptr(state), ctypes.c_int32(len(dims)), _u64(dims), ctypes.c_int32(len(gates)),
+                                      ks, tg, ptrs, _stream(stream)))
+    return state
+
+
+def apply_diag(state, dims, targets, diag, stream=None):
+    _check_c128(state)
+    _check_c128(diag)
+    check(lib().qtnh_apply_diag(_ptr(state), ctypes.c_int32(len(dims)), _u64(dims), ctypes.c_int32(len(targets)),
+                                _u16(targets), _ptr(diag), _stream(stream)))
+    return state
+
+
+def apply_diag_layer(state, dims, axes, factors, stream=None):
+    """factors: concatenated per-axis diagonals (device complex128)."""
+    _check_c128(state)
+    _check_c128(factors)
+    check(lib().qtnh_apply_diag_layer(_ptr(state), ctypes.c_int32(len(dims)), _u64(dims), ctypes.c_int32(len(axes)),
+                                      _u16(axes), _ptr(factors), _stream(stream)))
+    return state
+
+
+def norm2(x, stream=None):
+    _check_c128(x)
+    r = ctypes.c_double()
+    check(lib().qtnh_norm2(_ptr(x), ctypes.c_uint64(x.numel()), ctypes.byref(r), _stream(stream)))
+    return r.value

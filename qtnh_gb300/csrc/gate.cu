@@ -1,0 +1,305 @@
+// Symmetric-gate and diagonal contractions applied in place.
+//
+// When the second operand of Tensor::contract is a SymmTensor whose inputs are all wired
+// (src/tensor/contract.cpp:250-289), the result keeps the state's index order and each
+// gate output replaces the state index wired to the matching input. The reference still
+// runs the generic permute -> triple loop -> permute path (contract.cpp:12-201) through
+// per-element iterator objects. Here it is a register-blocked kernel: each thread owns
+// one group of D = prod(target dims) amplitudes (all other indices fixed), loads them
+// with 128-bit loads, applies the D x D gate from shared memory and stores them back.
+// Consecutive threads own consecutive groups, so loads and stores are coalesced unless a
+// target is the innermost index, in which case every thread touches D contiguous
+// elements.
+//
+// DiagTensor contraction (the reference stubs DiagTensor: src/tensor/diag.cpp:65-117)
+// is defined as contraction with D[in, out] = d[in] * delta(in, out); with the in-place
+// rule that is an elementwise multiply psi[x] *= d[x restricted to the targets], a
+// streaming kernel. A layer of single-index diagonals (one per qubit) is folded into two
+// phase tables (trailing indices, leading indices) so the whole layer is one pass.
+
+#include <algorithm>
+#include <memory>
+#include <numeric>
+
+#include "cuda_common.cuh"
+
+namespace qtnh_impl {
+
+namespace {
+
+constexpr int GATE_MAX_D = 16;
+
+struct GateParams {
+  RestDesc other;              // indices that are not gate targets, merged, with state strides in s_in
+  int64_t off[GATE_MAX_D];     // offsets of the D amplitudes of a group (row-major over targets)
+};
+
+template <int D>
+__global__ void __launch_bounds__(256) gate_kernel(c128* __restrict__ psi, const c128* __restrict__ gate,
+                                                   const __grid_constant__ GateParams p) {
+  __shared__ c128 g[D * D];
+  for (int t = threadIdx.x; t < D * D; t += blockDim.x) g[t] = gate[t];
+  __syncthreads();
+  for (uint64_t grp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; grp < p.other.total;
+       grp += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t base, unused;
+    decode(grp, p.other, base, unused);
+    c128 x[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) x[i] = psi[base + p.off[i]];
+#pragma unroll
+    for (int o = 0; o < D; ++o) {
+      c128 acc = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int i = 0; i < D; ++i) acc = cfma(g[i * D + o], x[i], acc);  // SymmTensor layout [in, out]
+      psi[base + p.off[o]] = acc;
+    }
+  }
+}
+
+struct DiagParams {
+  uint64_t n;
+  int k;
+  uint64_t dim[8], stride[8], mult[8];
+  uint32_t dim_log2[8], stride_log2[8];
+};
+
+__device__ __forceinline__ uint64_t digit(uint64_t e, uint64_t stride, uint32_t stride_log2, uint64_t dim, uint32_t dim_log2) {
+  uint64_t q = (stride_log2 != 0xFFFFFFFFu) ? (e >> stride_log2) : (e / stride);
+  return (dim_log2 != 0xFFFFFFFFu) ? (q & (dim - 1)) : (q % dim);
+}
+
+__global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const c128* __restrict__ d,
+                                                   const __grid_constant__ DiagParams p) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.n; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t idx = 0;
+    for (int j = 0; j < p.k; ++j) idx += digit(e, p.stride[j], p.stride_log2[j], p.dim[j], p.dim_log2[j]) * p.mult[j];
+    psi[e] = cmul(psi[e], __ldg(d + idx));
+  }
+}
+
+// ---- diagonal layer ----------------------------------------------------------------
+
+constexpr int LAYER_MAX_FACTORS = 64;
+
+struct LayerTableParams {
+  uint64_t size;          // table entries
+  uint64_t elem_stride;   // state elements per table step along the table's axes (unused by the kernel)
+  int nf;                 // factors that fall into this table
+  uint64_t f_stride[LAYER_MAX_FACTORS];  // stride of the factor's axis inside the table index
+  uint64_t f_dim[LAYER_MAX_FACTORS];
+  uint64_t f_off[LAYER_MAX_FACTORS];     // offset of the factor's entries in `factors`
+};
+
+__global__ void layer_table_kernel(const c128* __restrict__ factors, c128* __restrict__ table,
+                                   const __grid_constant__ LayerTableParams p) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p.size; j += (uint64_t)gridDim.x * blockDim.x) {
+    c128 v = make_double2(1.0, 0.0);
+    for (int f = 0; f < p.nf; ++f) {
+      uint64_t dgt = (j / p.f_stride[f]) % p.f_dim[f];
+      v = cmul(v, factors[p.f_off[f] + dgt]);
+    }
+    table[j] = v;
+  }
+}
+
+// psi[e] *= hi[e / lo_size] * lo[e % lo_size]; lo_size is a power of two or general.
+__global__ void __launch_bounds__(256) layer_apply_kernel(c128* __restrict__ psi, const c128* __restrict__ hi,
+                                                          const c128* __restrict__ lo, uint64_t n, uint64_t lo_size,
+                                                          uint32_t lo_log2) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t h, l;
+    if (lo_log2 != 0xFFFFFFFFu) h = e >> lo_log2, l = e & (lo_size - 1);
+    else h = e / lo_size, l = e % lo_size;
+    c128 ph = cmul(__ldg(hi + h), __ldg(lo + l));
+    psi[e] = cmul(psi[e], ph);
+  }
+}
+
+// Merge the non-target axes into runs and describe them (state strides in s_in).
+void other_axes(const dims_t& dims, const std::vector<uint16_t>& targets, RestDesc& out) {
+  dims_t st = row_strides(dims);
+  std::vector<char> is_t(dims.size(), 0);
+  for (auto t : targets) is_t[t] = 1;
+  dims_t md, ms;
+  for (size_t i = 0; i < dims.size(); ++i) {
+    if (is_t[i] || dims[i] == 1) continue;
+    if (!md.empty() && i > 0 && !is_t[i - 1] && ms.back() == dims[i] * st[i]) {
+      md.back() *= dims[i];
+      ms.back() = st[i];
+    } else {
+      md.push_back(dims[i]);
+      ms.push_back(st[i]);
+    }
+  }
+  if ((int)md.size() > KMAX) throw Error(QTNH_ERR_UNSUPPORTED, "too many axes");
+  out.n = (int)md.size();
+  out.total = product(md);
+  for (size_t i = 0; i < md.size(); ++i) fill_axis(out.ax[i], md[i], ms[i], 0);
+}
+
+void check_targets(const dims_t& dims, const std::vector<uint16_t>& targets) {
+  std::vector<char> seen(dims.size(), 0);
+  for (auto t : targets) {
+    if (t >= dims.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "target index out of range");
+    if (seen[t]++) throw Error(QTNH_ERR_INVALID_ARGUMENT, "target index repeated");
+  }
+}
+
+}  // namespace
+
+void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* gate,
+                       void* stream) {
+  check_targets(dims, targets);
+  uint64_t D = 1;
+  for (auto t : targets) D *= dims[t];
+  if (product(dims) == 0) return;
+  GateParams p;
+  other_axes(dims, targets, p.other);
+  dims_t st = row_strides(dims);
+  for (uint64_t c = 0; c < D && D <= GATE_MAX_D; ++c) {
+    uint64_t rem = c, off = 0;
+    for (int j = (int)targets.size() - 1; j >= 0; --j) {
+      uint64_t d = rem % dims[targets[j]];
+      rem /= dims[targets[j]];
+      off += d * st[targets[j]];
+    }
+    p.off[c] = (int64_t)off;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  c128* psi = static_cast<c128*>(state);
+  const c128* g = static_cast<const c128*>(gate);
+  int grid = grid_for((p.other.total + 255) / 256, 8);
+  switch (D) {
+    case 1: gate_kernel<1><<<grid, 256, 0, s>>>(psi, g, p); break;
+    case 2: gate_kernel<2><<<grid, 256, 0, s>>>(psi, g, p); break;
+    case 3: gate_kernel<3><<<grid, 256, 0, s>>>(psi, g, p); break;
+    case 4: gate_kernel<4><<<grid, 256, 0, s>>>(psi, g, p); break;
+    case 8: gate_kernel<8><<<grid, 256, 0, s>>>(psi, g, p); break;
+    case 9: gate_kernel<9><<<grid, 256, 0, s>>>(psi, g, p); break;
+    case 16: gate_kernel<16><<<grid, 256, 0, s>>>(psi, g, p); break;
+    default: throw Error(QTNH_ERR_UNSUPPORTED, "gate size outside the register-blocked kernel");
+  }
+  count_launch();
+  check_cuda(cudaGetLastError(), "gate_kernel launch");
+}
+
+void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* diag,
+                       void* stream) {
+  check_targets(dims, targets);
+  if (targets.size() > 8) throw Error(QTNH_ERR_UNSUPPORTED, "diagonal over more than 8 indices");
+  uint64_t n = product(dims);
+  if (n == 0) return;
+  DiagParams p;
+  p.n = n;
+  p.k = (int)targets.size();
+  dims_t st = row_strides(dims);
+  uint64_t m = 1;
+  for (int j = p.k - 1; j >= 0; --j) {
+    p.dim[j] = dims[targets[j]];
+    p.stride[j] = st[targets[j]];
+    p.dim_log2[j] = log2_or_none(p.dim[j]);
+    p.stride_log2[j] = log2_or_none(p.stride[j]);
+    p.mult[j] = m;
+    m *= p.dim[j];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int grid = grid_for((n + 255) / 256, 8);
+  diag_kernel<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
+  count_launch();
+  check_cuda(cudaGetLastError(), "diag_kernel launch");
+}
+
+void apply_diag_layer_device(void* state, const dims_t& dims, const std::vector<uint16_t>& axes, const void* factors,
+                             void* stream) {
+  check_targets(dims, axes);
+  if (axes.size() > (size_t)LAYER_MAX_FACTORS) throw Error(QTNH_ERR_UNSUPPORTED, "too many diagonal factors");
+  const uint64_t n = product(dims);
+  if (n == 0 || axes.empty()) return;
+  // Split the indices: trailing ones whose extent product is at most 4096 form the
+  // low table, the rest the high table.
+  const int r = (int)dims.size();
+  int split = r;
+  uint64_t lo_size = 1;
+  while (split > 0 && lo_size * dims[split - 1] <= 4096) lo_size *= dims[--split];
+  const uint64_t hi_size = n / lo_size;
+  dims_t st = row_strides(dims);
+  std::vector<uint64_t> foff(axes.size());
+  for (size_t f = 0, o = 0; f < axes.size(); ++f) foff[f] = o, o += dims[axes[f]];
+
+  std::unique_ptr<LayerTableParams> lo(new LayerTableParams()), hi(new LayerTableParams());
+  lo->size = lo_size;
+  hi->size = hi_size;
+  for (size_t f = 0; f < axes.size(); ++f) {
+    int a = axes[f];
+    LayerTableParams& t = (a >= split) ? *lo : *hi;
+    // Stride of axis a inside the table index: the state stride divided by lo_size for
+    // the high table (the high index is e / lo_size).
+    t.f_stride[t.nf] = (a >= split) ? st[a] : st[a] / lo_size;
+    t.f_dim[t.nf] = dims[a];
+    t.f_off[t.nf] = foff[f];
+    ++t.nf;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  c128* tables = static_cast<c128*>(workspace_alloc((lo_size + hi_size) * sizeof(c128), stream));
+  const c128* fac = static_cast<const c128*>(factors);
+  layer_table_kernel<<<grid_for((lo_size + 255) / 256, 4), 256, 0, s>>>(fac, tables, *lo);
+  layer_table_kernel<<<grid_for((hi_size + 255) / 256, 4), 256, 0, s>>>(fac, tables + lo_size, *hi);
+  layer_apply_kernel<<<grid_for((n + 255) / 256, 8), 256, 0, s>>>(static_cast<c128*>(state), tables + lo_size, tables, n,
+                                                                  lo_size, log2_or_none(lo_size));
+  count_launch(3);
+  cudaError_t e = cudaGetLastError();
+  workspace_free(tables, stream);
+  check_cuda(e, "diagonal layer launch");
+}
+
+}  // namespace qtnh_impl
+
+using namespace qtnh_impl;
+
+extern "C" {
+
+int qtnh_apply_gate(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
+                    const void* gate, void* stream) {
+  return guarded([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK || k < 0 || k > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    apply_gate_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(targets, targets + k), gate, stream);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32_t ngates, const int32_t* gate_k,
+                          const uint16_t* targets, const void* const* gates, void* stream) {
+  return guarded([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK || ngates < 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    dims_t d(dims, dims + rank);
+    size_t o = 0;
+    for (int32_t g = 0; g < ngates; ++g) {
+      if (gate_k[g] < 0 || gate_k[g] > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "gate arity out of range");
+      apply_gate_device(state, d, std::vector<uint16_t>(targets + o, targets + o + gate_k[g]), gates[g], stream);
+      o += (size_t)gate_k[g];
+    }
+    return QTNH_OK;
+  });
+}
+
+int qtnh_apply_diag(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
+                    const void* diag, void* stream) {
+  return guarded([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK || k < 0 || k > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    apply_diag_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(targets, targets + k), diag, stream);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_apply_diag_layer(void* state, int32_t rank, const uint64_t* dims, int32_t nfactors, const uint16_t* axes,
+                          const void* factors, void* stream) {
+  return guarded([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK || nfactors < 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    apply_diag_layer_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(axes, axes + nfactors), factors,
+                            stream);
+    return QTNH_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+// Shared declarations of the engine's translation units (not installed).
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "qtnh_cuda.h"
+
+namespace qtnh_impl {
+
+using dims_t = std::vector<uint64_t>;
+
+// Error carrying a QTNH_ERR_* code; entry points translate it into a return value.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+int status_from_current_exception();
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (...) {
+    return status_from_current_exception();
+  }
+}
+
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+inline uint64_t product(const dims_t& d) {
+  uint64_t p = 1;
+  for (auto x : d) p *= x;
+  return p;
+}
+
+inline dims_t row_strides(const dims_t& dims) {
+  dims_t s(dims.size(), 1);
+  for (int i = (int)dims.size() - 2; i >= 0; --i) s[i] = s[i + 1] * dims[i + 1];
+  return s;
+}
+
+// ---- host planning (plan.cpp; no CUDA) ---------------------------------------------
+
+struct Wire {
+  uint16_t first, second;
+};
+
+struct TensorMeta {
+  int32_t kind = QTNH_KIND_DENSE;
+  dims_t dis, loc;
+  int32_t n_dis_in = 0;
+  dims_t tot() const {
+    dims_t t = dis;
+    t.insert(t.end(), loc.begin(), loc.end());
+    return t;
+  }
+  uint64_t n_loc_in() const;  // include/tensor/symm.hpp:26-28 (throws when the range underflows)
+};
+
+TensorMeta meta_from_desc(const qtnh_tensor_desc* d);
+
+struct ContractPlan {
+  std::vector<Wire> wires;       // as given (validated)
+  std::vector<uint16_t> repls1;  // output position of t1 axes (QTNH_X when wired)
+  std::vector<uint16_t> repls2;
+  dims_t out_dims;
+  int32_t out_ndis = 0;
+  uint64_t out_str = 1;
+  bool inplace_rule = false;  // the symmetric in-place rule fired (contract.cpp:262)
+};
+
+// Tensor::contract metadata (contract.cpp:204-289) plus the result layout of
+// _contract_dense (contract.cpp:86-111, 180-200).
+ContractPlan plan_contract(const TensorMeta& t1, const TensorMeta& t2, const std::vector<Wire>& wires,
+                           bool use_default, const std::vector<uint16_t>& repls1_in,
+                           const std::vector<uint16_t>& repls2_in);
+
+// ---- device-side entry points shared across translation units -----------------------
+
+void permute_device(const void* in, void* out, const dims_t& dims, const std::vector<uint16_t>& ptup, void* stream);
+void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* gate,
+                       void* stream);
+void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* diag,
+                       void* stream);
+void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
+                           const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,
+                           const std::vector<uint16_t>& pos_b, void* c, void* stream);
+// Dense materialisation of an implicit kind (swap/iden/diag) into `out` (prod(dims) elements).
+void materialise_device(const TensorMeta& t, const void* data, void* out, void* stream);
+
+// Stream-ordered workspace (cudaMallocAsync pool).
+void* workspace_alloc(size_t bytes, void* stream);
+void workspace_free(void* p, void* stream);
+
+}  // namespace qtnh_impl

@@ -1,0 +1,328 @@
+// Axis permutation of complex128 tensors: Tensor::permute / Tensor::swap on one GPU.
+//
+// The reference moves data with MPI datatypes and MPI_Alltoallv even for a purely local
+// permutation (src/tensor/dense.cpp:354-488) and swaps with per-pair std::swap,
+// MPI_Scatter or MPI_Sendrecv (dense.cpp:171-274). Here all slabs are resident, so every
+// case is one out-of-place transpose of a row-major array in HBM, bound by HBM
+// bandwidth (algorithmic traffic 32 bytes per element: one 16-byte read, one write).
+//
+// Planner: drop size-1 axes, merge input-adjacent axes that stay adjacent, then pick
+//   * a straight copy when the merged permutation is the identity;
+//   * a run copy when the innermost axis stays innermost with >= 32 elements
+//     (each contiguous run of the input is one contiguous run of the output);
+//   * otherwise a tiled transpose: the tile spans the input's trailing axes (>= 32
+//     contiguous elements, coalesced 128-bit loads) and the output's trailing axes
+//     (>= 32 contiguous elements, coalesced 128-bit stores); the tile is staged in
+//     shared memory with one padding slot per row, and the per-element offsets of
+//     the tile come as tables in the kernel parameters (copied to shared memory);
+//   * a gather (coalesced stores, indexed loads) when no tile fits.
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "cuda_common.cuh"
+
+namespace qtnh_impl {
+
+namespace {
+
+constexpr int TILE_MAX = 1024;   // elements per transpose tile
+constexpr int TILE_THREADS = 256;
+
+
+struct TileParams {
+  RestDesc rest;
+  int T;
+  int tile_slots;
+  int64_t rin[TILE_MAX];   // read order: input offset within the tile
+  int64_t wout[TILE_MAX];  // write order: output offset within the tile
+  int32_t rslot[TILE_MAX];
+  int32_t wslot[TILE_MAX];
+};
+
+struct RunParams {
+  RestDesc rest;  // all axes but the innermost
+  uint64_t L;     // run length (innermost axis)
+  uint32_t L_log2;
+};
+
+__global__ void __launch_bounds__(TILE_THREADS) tiled_permute_kernel(const c128* __restrict__ in, c128* __restrict__ out,
+                                                                     const __grid_constant__ TileParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = p.T;
+  c128* tile = reinterpret_cast<c128*>(smem_raw);
+  int64_t* s_rin = reinterpret_cast<int64_t*>(tile + p.tile_slots);
+  int64_t* s_wout = s_rin + T;
+  int32_t* s_rslot = reinterpret_cast<int32_t*>(s_wout + T);
+  int32_t* s_wslot = s_rslot + T;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    s_rin[t] = p.rin[t];
+    s_wout[t] = p.wout[t];
+    s_rslot[t] = p.rslot[t];
+    s_wslot[t] = p.wslot[t];
+  }
+  __syncthreads();
+  for (uint64_t r = blockIdx.x; r < p.rest.total; r += gridDim.x) {
+    uint64_t bin, bout;
+    decode(r, p.rest, bin, bout);
+    for (int t = threadIdx.x; t < T; t += blockDim.x) tile[s_rslot[t]] = __ldg(in + bin + s_rin[t]);
+    __syncthreads();
+    for (int t = threadIdx.x; t < T; t += blockDim.x) out[bout + s_wout[t]] = tile[s_wslot[t]];
+    __syncthreads();
+  }
+}
+
+// Innermost axis fixed: copy runs of L elements. When L is a multiple of 128 every warp
+// copies 128 contiguous elements (4 per lane) of a single run per step.
+__global__ void __launch_bounds__(256) run_copy_kernel(const c128* __restrict__ in, c128* __restrict__ out,
+                                                       const __grid_constant__ RunParams p) {
+  const uint64_t N = p.rest.total * p.L;
+  const int lane = threadIdx.x & 31;
+  if ((p.L & 127) == 0) {
+    const uint64_t nchunks = N >> 7;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c = warp; c < nchunks; c += nwarps) {
+      const uint64_t e0 = c << 7;
+      uint64_t run, t0;
+      if (p.L_log2 != 0xFFFFFFFFu) run = e0 >> p.L_log2, t0 = e0 & (p.L - 1);
+      else run = e0 / p.L, t0 = e0 % p.L;
+      uint64_t bin, bout;
+      decode(run, p.rest, bin, bout);
+      const c128* src = in + bin + t0;
+      c128* dst = out + bout + t0;
+      c128 v0 = __ldg(src + lane), v1 = __ldg(src + lane + 32), v2 = __ldg(src + lane + 64), v3 = __ldg(src + lane + 96);
+      dst[lane] = v0;
+      dst[lane + 32] = v1;
+      dst[lane + 64] = v2;
+      dst[lane + 96] = v3;
+    }
+  } else {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < N; e += (uint64_t)gridDim.x * blockDim.x) {
+      uint64_t run, t;
+      if (p.L_log2 != 0xFFFFFFFFu) run = e >> p.L_log2, t = e & (p.L - 1);
+      else run = e / p.L, t = e % p.L;
+      uint64_t bin, bout;
+      decode(run, p.rest, bin, bout);
+      out[bout + t] = __ldg(in + bin + t);
+    }
+  }
+}
+
+// Fallback: one thread per output element; axes in output order with input strides.
+__global__ void __launch_bounds__(256) gather_permute_kernel(const c128* __restrict__ in, c128* __restrict__ out,
+                                                             const __grid_constant__ RestDesc p) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.total; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t src, unused;
+    decode(e, p, src, unused);
+    out[e] = __ldg(in + src);
+  }
+}
+
+struct Canon {
+  dims_t dims;            // merged input dims
+  std::vector<int> ptup;  // merged axis -> new position
+};
+
+Canon canonicalise(const dims_t& dims, const std::vector<uint16_t>& ptup) {
+  std::vector<int> keep;
+  for (size_t i = 0; i < dims.size(); ++i)
+    if (dims[i] > 1) keep.push_back((int)i);
+  std::vector<int> order(keep.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return ptup[keep[x]] < ptup[keep[y]]; });
+  std::vector<int> kp(keep.size());
+  for (size_t j = 0; j < order.size(); ++j) kp[order[j]] = (int)j;
+  dims_t gd;
+  std::vector<int> gp;
+  for (size_t x = 0; x < keep.size(); ++x) {
+    if (x > 0 && kp[x] == kp[x - 1] + 1) {
+      gd.back() *= dims[keep[x]];
+    } else {
+      gd.push_back(dims[keep[x]]);
+      gp.push_back(kp[x]);
+    }
+  }
+  std::vector<int> go(gd.size());
+  std::iota(go.begin(), go.end(), 0);
+  std::sort(go.begin(), go.end(), [&](int x, int y) { return gp[x] < gp[y]; });
+  Canon c;
+  c.dims = gd;
+  c.ptup.assign(gd.size(), 0);
+  for (size_t j = 0; j < go.size(); ++j) c.ptup[go[j]] = (int)j;
+  return c;
+}
+
+
+}  // namespace
+
+void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std::vector<uint16_t>& ptup, void* stream) {
+  const size_t r0 = dims.size();
+  if (ptup.size() != r0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple size differs from tensor rank");
+  {
+    std::vector<char> seen(r0, 0);
+    for (auto p : ptup) {
+      if (p >= r0 || seen[p]) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple is not a permutation");
+      seen[p] = 1;
+    }
+  }
+  const uint64_t N = product(dims);
+  if (N == 0) return;
+  cudaStream_t s = (cudaStream_t)stream;
+  const c128* in = static_cast<const c128*>(in_v);
+  c128* out = static_cast<c128*>(out_v);
+
+  Canon c = canonicalise(dims, ptup);
+  const int r = (int)c.dims.size();
+  if (r > KMAX) throw Error(QTNH_ERR_UNSUPPORTED, "too many non-trivial axes");
+  if (r <= 1) {
+    check_cuda(cudaMemcpyAsync(out, in, N * sizeof(c128), cudaMemcpyDeviceToDevice, s), "permute copy");
+    return;
+  }
+  dims_t in_stride = row_strides(c.dims);
+  dims_t new_dims(r);
+  for (int i = 0; i < r; ++i) new_dims[c.ptup[i]] = c.dims[i];
+  dims_t ns = row_strides(new_dims);
+  dims_t out_stride(r);
+  std::vector<int> inv(r);
+  for (int i = 0; i < r; ++i) out_stride[i] = ns[c.ptup[i]], inv[c.ptup[i]] = i;
+
+  // Run copy.
+  if (c.ptup[r - 1] == r - 1 && c.dims[r - 1] >= 32) {
+    RunParams p;
+    p.L = c.dims[r - 1];
+    p.L_log2 = log2_or_none(p.L);
+    p.rest.n = r - 1;
+    p.rest.total = N / p.L;
+    for (int i = 0; i < r - 1; ++i) fill_axis(p.rest.ax[i], c.dims[i], in_stride[i], out_stride[i]);
+    int grid = grid_for((N + 1023) / 1024, 16);
+    run_copy_kernel<<<grid, 256, 0, s>>>(in, out, p);
+    count_launch();
+    check_cuda(cudaGetLastError(), "run_copy_kernel launch");
+    return;
+  }
+
+  // Tiled transpose.
+  std::vector<int> A, B;
+  std::vector<char> inA(r, 0), inB(r, 0);
+  uint64_t PA = 1, PB = 1;
+  for (int i = r - 1; i >= 0 && PA < 32; --i) A.push_back(i), PA *= c.dims[i], inA[i] = 1;
+  bool tiled = PA <= (uint64_t)TILE_MAX;
+  if (tiled) {
+    uint64_t run = 1;
+    for (int j = r - 1; j >= 0 && run < 32; --j) {
+      int i = inv[j];
+      if (inA[i]) {
+        run *= c.dims[i];
+        continue;
+      }
+      if (PA * PB * c.dims[i] > (uint64_t)TILE_MAX) break;
+      B.push_back(i), PB *= c.dims[i], inB[i] = 1, run *= c.dims[i];
+    }
+  }
+  if (tiled) {
+    std::sort(A.begin(), A.end());
+    std::sort(B.begin(), B.end());
+    std::unique_ptr<TileParams> pp(new TileParams());  // ~25 KB, passed by value to the launch
+    TileParams& p = *pp;
+    const int T = (int)(PA * PB);
+    p.T = T;
+    p.tile_slots = (int)(PB * (PA + 1));
+    // Row-major multipliers over A and B (input order).
+    auto mults = [&](const std::vector<int>& axes) {
+      std::vector<uint64_t> m(axes.size(), 1);
+      for (int k = (int)axes.size() - 2; k >= 0; --k) m[k] = m[k + 1] * c.dims[axes[k + 1]];
+      return m;
+    };
+    auto mA = mults(A), mB = mults(B);
+    // Read order: t = b * PA + a.
+    for (uint64_t b = 0; b < PB; ++b) {
+      uint64_t offb = 0, rem = b;
+      for (int k = (int)B.size() - 1; k >= 0; --k) {
+        uint64_t d = rem % c.dims[B[k]];
+        rem /= c.dims[B[k]];
+        offb += d * in_stride[B[k]];
+      }
+      for (uint64_t a = 0; a < PA; ++a) {
+        uint64_t offa = 0, ra = a;
+        for (int k = (int)A.size() - 1; k >= 0; --k) {
+          uint64_t d = ra % c.dims[A[k]];
+          ra /= c.dims[A[k]];
+          offa += d * in_stride[A[k]];
+        }
+        int t = (int)(b * PA + a);
+        p.rin[t] = (int64_t)(offa + offb);
+        p.rslot[t] = (int32_t)(b * (PA + 1) + a);
+      }
+    }
+    // Write order: tile axes by output position, row-major.
+    std::vector<int> tax(A);
+    tax.insert(tax.end(), B.begin(), B.end());
+    std::sort(tax.begin(), tax.end(), [&](int x, int y) { return c.ptup[x] < c.ptup[y]; });
+    for (int w = 0; w < T; ++w) {
+      uint64_t rem = (uint64_t)w, off = 0, a = 0, b = 0;
+      for (int k = (int)tax.size() - 1; k >= 0; --k) {
+        int i = tax[k];
+        uint64_t d = rem % c.dims[i];
+        rem /= c.dims[i];
+        off += d * out_stride[i];
+        if (inA[i]) a += d * mA[std::find(A.begin(), A.end(), i) - A.begin()];
+        else b += d * mB[std::find(B.begin(), B.end(), i) - B.begin()];
+      }
+      p.wout[w] = (int64_t)off;
+      p.wslot[w] = (int32_t)(b * (PA + 1) + a);
+    }
+    int nr = 0;
+    for (int i = 0; i < r; ++i)
+      if (!inA[i] && !inB[i]) fill_axis(p.rest.ax[nr++], c.dims[i], in_stride[i], out_stride[i]);
+    p.rest.n = nr;
+    p.rest.total = N / (uint64_t)T;
+    size_t smem = (size_t)p.tile_slots * sizeof(c128) + (size_t)T * (2 * sizeof(int64_t) + 2 * sizeof(int32_t));
+    int grid = grid_for(p.rest.total, 5);
+    tiled_permute_kernel<<<grid, TILE_THREADS, smem, s>>>(in, out, p);
+    count_launch();
+    check_cuda(cudaGetLastError(), "tiled_permute_kernel launch");
+    return;
+  }
+
+  // Gather fallback: axes in output order, input strides.
+  RestDesc g;
+  g.n = r;
+  g.total = N;
+  for (int j = 0; j < r; ++j) fill_axis(g.ax[j], new_dims[j], in_stride[inv[j]], 0);
+  int grid = grid_for((N + 255) / 256, 16);
+  gather_permute_kernel<<<grid, 256, 0, s>>>(in, out, g);
+  count_launch();
+  check_cuda(cudaGetLastError(), "gather_permute_kernel launch");
+}
+
+}  // namespace qtnh_impl
+
+using namespace qtnh_impl;
+
+extern "C" {
+
+int qtnh_permute(const void* in, void* out, int32_t rank, const uint64_t* dims, const uint16_t* ptup, void* stream) {
+  return guarded([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    permute_device(in, out, dims_t(dims, dims + rank), std::vector<uint16_t>(ptup, ptup + rank), stream);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_swap(const void* in, void* out, int32_t rank, const uint64_t* dims, int32_t idx1, int32_t idx2, void* stream) {
+  return guarded([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    if (idx1 < 0 || idx2 < 0 || idx1 >= rank || idx2 >= rank) throw Error(QTNH_ERR_OUT_OF_RANGE, "swap index out of range");
+    if (dims[idx1] != dims[idx2]) throw Error(QTNH_ERR_RUNTIME, "Asymmetric swaps are currently not allowed");
+    std::vector<uint16_t> ptup(rank);
+    std::iota(ptup.begin(), ptup.end(), 0);
+    std::swap(ptup[idx1], ptup[idx2]);
+    permute_device(in, out, dims_t(dims, dims + rank), ptup, stream);
+    return QTNH_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// Library runtime: error reporting, device memory, copies, stream helpers, FP64 norm.
+//
+// Replaces the reference's QTNHEnv/MPI plumbing (src/core/env.cpp:9-29): one process
+// drives one GPU, tensors live in HBM, and every former MPI exchange is a device
+// operation on a caller-supplied stream.
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "cuda_common.cuh"
+
+namespace qtnh_impl {
+
+static thread_local std::string g_last_error = "";
+std::atomic<uint64_t> g_launches{0};
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+int status_from_current_exception() {
+  try {
+    throw;
+  } catch (const Error& e) {
+    set_last_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc& e) {
+    set_last_error("host allocation failed");
+    return QTNH_ERR_NO_MEMORY;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return QTNH_ERR_RUNTIME;
+  } catch (...) {
+    set_last_error("unknown error");
+    return QTNH_ERR_RUNTIME;
+  }
+}
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) throw Error(QTNH_ERR_NO_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    throw Error(QTNH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+void* workspace_alloc(size_t bytes, void* stream) {
+  if (bytes == 0) return nullptr;
+  void* p = nullptr;
+  check_cuda(cudaMallocAsync(&p, bytes, (cudaStream_t)stream), "cudaMallocAsync");
+  return p;
+}
+
+void workspace_free(void* p, void* stream) {
+  if (p) check_cuda(cudaFreeAsync(p, (cudaStream_t)stream), "cudaFreeAsync");
+}
+
+// FP64 sum of |x|^2: grid-stride partial sums, one atomic per block.
+__global__ void norm2_kernel(const double2* __restrict__ x, uint64_t n, double* __restrict__ acc) {
+  double s = 0.0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    double2 v = x[i];
+    s = fma(v.x, v.x, s);
+    s = fma(v.y, v.y, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ double ws[32];
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) ws[warp] = s;
+  __syncthreads();
+  if (warp == 0) {
+    s = (lane < (int)(blockDim.x >> 5)) ? ws[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) atomicAdd(acc, s);
+  }
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    check_cuda(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  }
+  return n;
+}
+
+}  // namespace qtnh_impl
+
+using namespace qtnh_impl;
+
+extern "C" {
+
+const char* qtnh_last_error(void) { return g_last_error.c_str(); }
+int qtnh_abi_version(void) { return QTNH_ABI_VERSION; }
+uint64_t qtnh_kernel_launch_count(void) { return g_launches.load(); }
+
+int qtnh_device_count(int* count) {
+  return guarded([&]() -> int {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) n = 0, cudaGetLastError();
+    *count = n;
+    return QTNH_OK;
+  });
+}
+
+int qtnh_set_device(int device) {
+  return guarded([&]() -> int {
+    check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_malloc(void** ptr, size_t bytes) {
+  return guarded([&]() -> int {
+    *ptr = nullptr;
+    if (bytes == 0) bytes = 16;
+    check_cuda(cudaMalloc(ptr, bytes), "cudaMalloc");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_free(void* ptr) {
+  return guarded([&]() -> int {
+    if (ptr) check_cuda(cudaFree(ptr), "cudaFree");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_memcpy_h2d(void* dst, const void* src_host, size_t bytes, void* stream) {
+  return guarded([&]() -> int {
+    if (bytes) check_cuda(cudaMemcpyAsync(dst, src_host, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream), "h2d copy");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_memcpy_d2h(void* dst_host, const void* src, size_t bytes, void* stream) {
+  return guarded([&]() -> int {
+    if (bytes) check_cuda(cudaMemcpyAsync(dst_host, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "d2h copy");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream) {
+  return guarded([&]() -> int {
+    if (bytes) check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream), "d2d copy");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_memset(void* dst, int value, size_t bytes, void* stream) {
+  return guarded([&]() -> int {
+    if (bytes) check_cuda(cudaMemsetAsync(dst, value, bytes, (cudaStream_t)stream), "memset");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_stream_synchronize(void* stream) {
+  return guarded([&]() -> int {
+    check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "stream synchronize");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream) {
+  return guarded([&]() -> int {
+    cudaStream_t s = (cudaStream_t)stream;
+    double* acc = (double*)workspace_alloc(sizeof(double), stream);
+    check_cuda(cudaMemsetAsync(acc, 0, sizeof(double), s), "memset");
+    if (n) {
+      int grid = sm_count() * 4;
+      norm2_kernel<<<grid, 512, 0, s>>>((const double2*)x, n, acc);
+      count_launch();
+      check_cuda(cudaGetLastError(), "norm2 launch");
+    }
+    check_cuda(cudaMemcpyAsync(result_host, acc, sizeof(double), cudaMemcpyDeviceToHost, s), "d2h copy");
+    workspace_free(acc, stream);
+    check_cuda(cudaStreamSynchronize(s), "stream synchronize");
+    return QTNH_OK;
+  });
+}
+
+}  // extern "C"

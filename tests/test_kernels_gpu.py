@@ -1,0 +1,263 @@
+"""GPU parity of the C ABI against the oracle (and the reference's golden vectors).
+
+Data movement (permute, swap, delta contractions) must be bit-exact; contractions
+within 1e-12 relative L2 (the plain complex128 bar), goldens within the
+reference's own 1e-5 (tests/c2-tensor.cpp:157)."""
+import json
+import math
+import os
+import random
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import qtnh_gb300 as q
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+RT = json.load(open(os.path.join(HERE, "golden", "random_tensors.json")))["groups"]
+REL_TOL = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _setup():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    orc.build()
+    q.lib()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128).reshape(-1)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def rel_l2(a, b):
+    a, b = np.asarray(a).reshape(-1), np.asarray(b).reshape(-1)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def crandn(rng, shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+def _els(info):
+    a = np.array(info["els"], dtype=np.float64)
+    return (a[:, 0] + 1j * a[:, 1]).astype(np.complex128)
+
+
+# ---- permute / swap -----------------------------------------------------------------
+
+def _perm_cases():
+    rng = random.Random(1)
+    cases = []
+    for _ in range(40):
+        r = rng.randint(1, 6)
+        dims = [rng.choice([1, 2, 3, 4, 5, 7, 16, 33, 64]) for _ in range(r)]
+        while np.prod(dims) > 2 ** 20:
+            dims[rng.randrange(r)] = 2
+        p = list(range(r))
+        rng.shuffle(p)
+        cases.append((dims, p))
+    for n in (10, 14, 20):  # qubit tensors
+        for _ in range(4):
+            p = list(range(n))
+            rng.shuffle(p)
+            cases.append(([2] * n, p))
+        p = list(range(n))
+        for k in range(3):  # exchange 3 top axes with 3 low axes
+            p[k], p[n - 1 - 2 * k] = p[n - 1 - 2 * k], p[k]
+        cases.append(([2] * n, p))
+    cases.append(([2] * 20, [1, 0, 2] + list(range(3, 20))))  # run copy
+    cases.append(([4096, 3], [1, 0]))                           # gather fallback (huge inner axis)
+    return cases
+
+
+@pytest.mark.parametrize("dims,ptup", _perm_cases())
+def test_permute_bit_exact(dims, ptup):
+    rng = np.random.default_rng(len(dims) * 7 + sum(ptup))
+    a = crandn(rng, dims)
+    ref = orc.permute(a, ptup)
+    out = host(q.permute(dev(a), dims, ptup))
+    assert np.array_equal(out.view(np.uint64), ref.reshape(-1).view(np.uint64))
+
+
+def test_swap_bit_exact_and_asymmetric():
+    rng = np.random.default_rng(2)
+    dims = [3, 2, 3, 4]
+    a = crandn(rng, dims)
+    out = host(q.swap(dev(a), dims, 0, 2))
+    assert np.array_equal(out, orc.swap(a, 0, 2).reshape(-1))
+    with pytest.raises(q.QtnhError):
+        q.swap(dev(a), dims, 0, 1)
+
+
+# ---- contractions on the reference's golden vectors ----------------------------------
+
+def _run_contract(t1, t2, wires):
+    o1 = orc.Tensor({q.DENSE: orc.DENSE, q.SYMM: orc.SYMM, q.SWAP: orc.SWAP, q.IDEN: orc.IDEN, q.DIAG: orc.DIAG}[t1[0]],
+                    t1[1], t1[2], t1[3], t1[4])
+    o2 = orc.Tensor({q.DENSE: orc.DENSE, q.SYMM: orc.SYMM, q.SWAP: orc.SWAP, q.IDEN: orc.IDEN, q.DIAG: orc.DIAG}[t2[0]],
+                    t2[1], t2[2], t2[3], t2[4])
+    ref, r1, r2 = orc.contract(o1, o2, wires)
+    g1 = q.Tensor(t1[0], t1[1], t1[2], dev(t1[3]) if t1[3] is not None else None, t1[4])
+    g2 = q.Tensor(t2[0], t2[1], t2[2], dev(t2[3]) if t2[3] is not None else None, t2[4])
+    res, q1, q2, st = q.contract(g1, g2, wires)
+    assert res.dis == ref.dis and res.loc == ref.loc
+    assert q1 == r1 and q2 == r2 and st == ref.bc[0]
+    return host(res.data), ref.els
+
+
+@pytest.mark.parametrize("i", range(20))
+def test_golden_dense(i):
+    cv = RT["dense_vals"][i]
+    out, ref = _run_contract((q.DENSE, [], cv["t1"]["dims"], _els(cv["t1"]), 0),
+                             (q.DENSE, [], cv["t2"]["dims"], _els(cv["t2"]), 0), [tuple(w) for w in cv["wires"]])
+    assert np.all(np.abs(out - _els(cv["t3"])) < 1e-5)
+    assert rel_l2(out, ref) < REL_TOL
+
+
+@pytest.mark.parametrize("i", range(10))
+def test_golden_swap_bit_exact(i):
+    cv = RT["swap_vals"][i]
+    n = cv["t2"]["dims"][0]
+    out, ref = _run_contract((q.DENSE, [], cv["t1"]["dims"], _els(cv["t1"]), 0), (q.SWAP, [], [n] * 4, None, 0),
+                             [tuple(w) for w in cv["wires"]])
+    assert np.all(np.abs(out - _els(cv["t3"])) < 1e-5)
+    assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("i", range(10))
+def test_golden_identity_bit_exact(i):
+    cv = RT["id_vals"][i]
+    out, ref = _run_contract((q.DENSE, [], cv["t1"]["dims"], _els(cv["t1"]), 0),
+                             (q.IDEN, [], cv["t2"]["dims"], None, 0), [tuple(w) for w in cv["wires"]])
+    assert np.all(np.abs(out - _els(cv["t3"])) < 1e-5)
+    assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_golden_invalid_swaps(i):
+    cv = RT["invalid_swaps"][i]
+    n = cv["t2"]["dims"][0]
+    with pytest.raises(q.QtnhError):
+        q.contract(q.Tensor(q.DENSE, [], cv["t1"]["dims"], dev(_els(cv["t1"]))), q.Tensor(q.SWAP, [], [n] * 4),
+                   [tuple(w) for w in cv["wires"]])
+
+
+@pytest.mark.parametrize("group,s1,s2", [("mpi2r_vals", 1, 0), ("mpi3r_vals", 1, 0), ("mpi4r_vals", 1, 1),
+                                         ("mpi6r_vals", 1, 1), ("mpi8r_vals", 2, 1)])
+def test_golden_distributed(group, s1, s2):
+    for cv in RT[group]:
+        d1, d2 = cv["t1"]["dims"], cv["t2"]["dims"]
+        out, ref = _run_contract((q.DENSE, d1[:s1], d1[s1:], _els(cv["t1"]), 0),
+                                 (q.DENSE, d2[:s2], d2[s2:], _els(cv["t2"]), 0), [tuple(w) for w in cv["wires"]])
+        assert np.all(np.abs(out - _els(cv["t3"])) < 1e-5)
+        assert rel_l2(out, ref) < REL_TOL
+
+
+# ---- seeded random contractions against the oracle -----------------------------------
+
+def test_random_dense_contractions():
+    rng = random.Random(3)
+    nrng = np.random.default_rng(3)
+    for _ in range(60):
+        dis1 = [rng.choice([2, 3, 4]) for _ in range(rng.randint(0, 2))]
+        loc1 = [rng.choice([2, 3, 4, 5]) for _ in range(rng.randint(0, 4))]
+        dis2 = [rng.choice([2, 3, 4]) for _ in range(rng.randint(0, 2))]
+        loc2 = [rng.choice([2, 3, 4, 5]) for _ in range(rng.randint(0, 4))]
+        wires = []
+        for i in range(len(dis1)):  # some distributed wires (the reference's "reduced" indices)
+            cands = [j for j in range(len(dis2)) if dis2[j] == dis1[i] and j not in [w[1] for w in wires]]
+            if cands and rng.random() < 0.5:
+                wires.append((i, rng.choice(cands)))
+        for i in range(len(loc1)):
+            cands = [j for j in range(len(loc2)) if loc2[j] == loc1[i] and len(dis2) + j not in [w[1] for w in wires]]
+            if cands and rng.random() < 0.6:
+                wires.append((len(dis1) + i, len(dis2) + rng.choice(cands)))
+        a = crandn(nrng, dis1 + loc1)
+        b = crandn(nrng, dis2 + loc2)
+        out, ref = _run_contract((q.DENSE, dis1, loc1, a, 0), (q.DENSE, dis2, loc2, b, 0), wires)
+        assert rel_l2(out, ref) < REL_TOL
+
+
+def test_large_gemm_contraction():
+    nrng = np.random.default_rng(9)
+    a = crandn(nrng, [16, 32, 64, 4])
+    b = crandn(nrng, [64, 8, 16, 3])
+    out, ref = _run_contract((q.DENSE, [], [16, 32, 64, 4], a, 0), (q.DENSE, [], [64, 8, 16, 3], b, 0), [(2, 0), (0, 2)])
+    assert rel_l2(out, ref) < REL_TOL
+
+
+def haar(rng, d):
+    z = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / math.sqrt(2)
+    qm, r = np.linalg.qr(z)
+    return qm * (np.diag(r) / np.abs(np.diag(r)))
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4])
+def test_symmetric_gate_in_place(k):
+    nrng = np.random.default_rng(20 + k)
+    n = 12
+    psi = crandn(nrng, [2] * n)
+    u = haar(nrng, 2 ** k)
+    els = u.T.reshape(-1)  # SymmTensor layout [in..., out...]: els[in, out] = U[out, in]
+    targets = list(nrng.choice(n, size=k, replace=False))
+    wires = [(int(t), j) for j, t in enumerate(targets)]
+    out, ref = _run_contract((q.DENSE, [], [2] * n, psi, 0), (q.SYMM, [], [2] * (2 * k), els, 0), wires)
+    assert rel_l2(out, ref) < REL_TOL
+
+
+def test_gate_kernel_direct_matches_oracle():
+    nrng = np.random.default_rng(4)
+    n = 16
+    psi = crandn(nrng, [2] * n)
+    u = haar(nrng, 4)
+    els = u.T.reshape(-1)
+    st = dev(psi)
+    q.apply_gate(st, [2] * n, [3, 15], dev(els))
+    ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], [2] * n, psi), orc.Tensor(orc.SYMM, [], [2] * 4, els),
+                             [(3, 0), (15, 1)])
+    assert rel_l2(host(st), ref.els) < REL_TOL
+
+
+def test_diagonal_in_place_and_layer():
+    nrng = np.random.default_rng(6)
+    n = 14
+    psi = crandn(nrng, [2] * n)
+    d = np.exp(1j * nrng.uniform(0, 2 * np.pi, 4))
+    out, ref = _run_contract((q.DENSE, [], [2] * n, psi, 0), (q.DIAG, [], [2] * 4, d, 0), [(5, 0), (2, 1)])
+    assert rel_l2(out, ref) < REL_TOL
+    # a whole layer of single-qubit phases equals n successive rank-2 diagonal contractions
+    phases = nrng.uniform(0, 2 * np.pi, n)
+    factors = np.stack([np.ones(n), np.exp(1j * phases)], axis=1).reshape(-1)
+    st = dev(psi)
+    q.apply_diag_layer(st, [2] * n, list(range(n)), dev(factors))
+    cur = orc.Tensor(orc.DENSE, [], [2] * n, psi)
+    for j in range(n):
+        cur, _, _ = orc.contract(cur, orc.Tensor(orc.DIAG, [], [2, 2], factors[2 * j:2 * j + 2]), [(j, 0)])
+    assert rel_l2(host(st), cur.els) < REL_TOL
+
+
+def test_norm2():
+    nrng = np.random.default_rng(8)
+    a = crandn(nrng, [1 << 18])
+    assert abs(q.norm2(dev(a)) - np.vdot(a, a).real) < 1e-9 * np.vdot(a, a).real
+
+
+def test_distributed_identity_moves_index():
+    # IdenTensor with one distributed and one local index ("DIST" in the reference's QFT):
+    # contracting a state index with its local index moves it into the distributed prefix.
+    nrng = np.random.default_rng(10)
+    psi = crandn(nrng, [2, 2, 2])
+    out, ref = _run_contract((q.DENSE, [], [2, 2, 2], psi, 0), (q.IDEN, [2], [2], None, 0), [(1, 1)])
+    assert np.array_equal(out, ref)
