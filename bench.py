@@ -1,0 +1,334 @@
+#!/usr/bin/env python
+"""Gate-layers/s of the plain complex128 engine on the random layered circuit.
+
+Workload (the configuration the headline metric is quoted on): n = 28 qubits
+(2^28 complex128 amplitudes, 4 GiB), depth 40; every layer 14 Haar-random
+two-qubit SymmTensor gates on a seeded random pairing; every 4th layer a layer of
+per-qubit phase DiagTensors; every 8th layer a rescatter of the top 3 indices and a
+seeded permutation exchanging them with 3 local indices. A step is one pass of the
+whole circuit over the state. Inputs (4 GiB) are far larger than L2 (129 MB), so no
+L2 flush is needed between steps.
+
+value : gate-layers/s with the state resident in HBM (CUDA events on the launch stream).
+e2e   : the same through the C ABI with host buffers: every step copies the initial
+        state from pinned host memory to the device and the result back.
+roofline: the dominant kernel (the two-qubit gate kernel), algorithmic bytes
+        32 * 2^n per launch over its event-timed average duration, against the
+        measured HBM copy bandwidth.
+cpu_baseline: the oracle port of the reference's contraction path on one host core,
+        on a bounded sample (n = 20, 4 layers), extrapolated to n = 28.
+
+`--impl reference` times that CPU port with every host core (one replica per core,
+the reference's slab-per-rank parallelism without communication) and prints the
+same metric.
+Multi-GPU (torchrun): independent replicas, one per GPU ("replicas only").
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "gate-layers/s"
+UNIT = "gate-layers/s"
+CPU_SAMPLE_N = 20
+CPU_SAMPLE_LAYERS = 4
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=28)
+    p.add_argument("--depth", type=int, default=40)
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def _config(a, cpu_cores=None):
+    return {
+        "workload": "random layered circuit, n=%d qubits, depth %d, 14 Haar 2-qubit SymmTensor gates/layer, "
+                    "phase DiagTensor layer every 4th, rescatter+permute of top 3 indices every 8th" % (a.n, a.depth),
+        "qubits": a.n,
+        "depth": a.depth,
+        "gates_per_layer": a.n // 2,
+        "element": "complex128",
+        "state_bytes": 16 * (2 ** a.n),
+        "l2_flush": "not needed: 4 GiB state is larger than the 129 MB L2",
+        "parallelism": "replicas" if a.gpus > 1 else "single GPU",
+    }
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel, n):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, scaled to 2^n."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            d = json.load(f)
+        e = d[kernel]
+        return float(e["bytes_per_launch"]) * (2 ** n) / float(e["elements"])
+    except Exception:
+        return None
+
+
+class _Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/qtnh_clocks_bench.csv"
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        loaded = sorted(sm)[len(sm) // 4:] if sm else []
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def _cpu_sample(n, layers, seed, reps=1):
+    """Oracle port on one core: seconds per gate-layer at n qubits over `layers` layers."""
+    from oracle import oracle as orc
+    from qtnh_gb300 import workload as wl
+    orc.build()
+    c = wl.random_circuit(n, layers, seed=seed)
+    psi = wl.random_state(n, seed=seed + 1)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        orc.run_circuit(psi, c)
+    return (time.perf_counter() - t0) / (layers * reps)
+
+
+def _extrapolate(sec_per_layer, n_sample, n_target):
+    # work per layer ~ gates_per_layer * 2^n
+    return sec_per_layer * (2.0 ** (n_target - n_sample)) * ((n_target // 2) / (n_sample // 2))
+
+
+def _sample_desc(n_target, cores):
+    return ("oracle port of the reference's Tensor::contract path (scalar C++), %d layer(s) of the same circuit family "
+            "at n=%d on %d core(s), extrapolated to n=%d by 2^%d x gates/layer" %
+            (CPU_SAMPLE_LAYERS, CPU_SAMPLE_N, cores, n_target, n_target - CPU_SAMPLE_N))
+
+
+def _worker(args):
+    n, layers, seed = args
+    return _cpu_sample(n, layers, seed)
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import oracle as orc
+    orc.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(cores) as pool:
+        for step in range(a.warmup + a.steps):
+            t0 = time.perf_counter()
+            pool.map(_worker, [(CPU_SAMPLE_N, CPU_SAMPLE_LAYERS, a.seed)] * cores)
+            dt = time.perf_counter() - t0
+            if step >= a.warmup:
+                times.append(dt)
+    sec_per_layer_sample = statistics.median(times) / (CPU_SAMPLE_LAYERS * cores)
+    value = 1.0 / _extrapolate(sec_per_layer_sample, CPU_SAMPLE_N, a.n)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": statistics.median(times) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)", "config": _config(a),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": _sample_desc(a.n, cores) + "; one independent replica per core"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+
+    import torch
+    import qtnh_gb300 as q
+    from qtnh_gb300.circuit import DeviceCircuit
+    from qtnh_gb300 import workload as wl
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    # CPU baseline first (before any GPU work, single core), rank 0 only.
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        spl = _cpu_sample(CPU_SAMPLE_N, CPU_SAMPLE_LAYERS, a.seed)
+        cpu = {"value": 1.0 / _extrapolate(spl, CPU_SAMPLE_N, a.n), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": _sample_desc(a.n, 1)}
+
+    circ = wl.random_circuit(a.n, a.depth, seed=a.seed)
+    dc = DeviceCircuit(circ, device=dev)
+    N = 2 ** a.n
+    g = torch.Generator(device=dev)
+    g.manual_seed(a.seed + 1)
+    state = torch.randn(N, dtype=torch.complex128, device=dev, generator=g)
+    state /= torch.linalg.vector_norm(state)
+    scratch = torch.empty_like(state)
+    host_in = torch.empty(N, dtype=torch.complex128, pin_memory=True)
+    host_in.copy_(state)
+    host_out = torch.empty(N, dtype=torch.complex128, pin_memory=True)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up
+    cur, oth = state, scratch
+    for _ in range(a.warmup):
+        res = dc.run(cur, oth)
+        if res is not cur:
+            cur, oth = oth, cur
+    torch.cuda.synchronize()
+
+    # timed region: device-resident
+    clocks = _Clocks(local)
+    events = {}
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = q.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        res = dc.run(cur, oth, events=events)
+        if res is not cur:
+            cur, oth = oth, cur
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ck = clocks.stop()
+    launches = q.launches() - l0
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / a.steps
+    value = world * a.depth * a.steps / (ms / 1e3)
+
+    # roofline of the dominant kernel (two-qubit gate kernel)
+    gate_ms = [s.elapsed_time(e) for s, e in events.get("gates", [])]
+    gates_per_call = a.n // 2
+    gate_launch_ms = (sum(gate_ms) / len(gate_ms)) / gates_per_call if gate_ms else None
+    alg_bytes = 32.0 * N
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (gate_launch_ms * 1e-3) / 1e9 if gate_launch_ms else None
+    share = {k: sum(s.elapsed_time(e) for s, e in v) / ms for k, v in events.items()}
+
+    # e2e through the C ABI with host buffers
+    barrier()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(a.steps):
+        q.check(q.lib().qtnh_memcpy_h2d(q._ptr(cur), q._ptr(host_in), q.ctypes.c_size_t(16 * N), q._stream()))
+        res = dc.run(cur, oth)
+        if res is not cur:
+            cur, oth = oth, cur
+        q.check(q.lib().qtnh_memcpy_d2h(q._ptr(host_out), q._ptr(cur), q.ctypes.c_size_t(16 * N), q._stream()))
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ems = f0.elapsed_time(f1)
+    if dist is not None:
+        t = torch.tensor([ems], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ems = float(t.item())
+    e2e = world * a.depth * a.steps / (ems / 1e3)
+    norm = q.norm2(cur)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic (seeded circuit; state i.i.d. complex Gaussian, unit L2)",
+            "config": _config(a),
+            "roofline": {"bound": "hbm", "kernel": "gate_kernel<4>", "achieved": achieved, "peak": peak,
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                         "traffic": _traffic("gate_kernel<4>", a.n), "alg_bytes_per_launch": alg_bytes,
+                         "launch_ms": gate_launch_ms, "time_share": share},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
+            "clocks": ck,
+            "gpu_launches": launches,
+            "final_norm2": norm,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

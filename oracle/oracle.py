@@ -217,3 +217,21 @@ class Network:
         _check(lib().orc_tn_get(self._h, ctypes.c_uint32(tid), ctypes.byref(ndis), ctypes.byref(nloc), dims, bc,
                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_uint64(n)))
         return Tensor(DENSE, d[:ndis.value], d[ndis.value:], out, bc=(bc[0], bc[1], bc[2]))
+
+
+def run_circuit(psi, circuit, layers=None):
+    """Apply a layered circuit (qtnh_gb300.workload.Circuit) the way a qtnh user would:
+    one Tensor::contract per gate (SymmTensor, in-place rule), one per single-qubit
+    DiagTensor, and Tensor::permute for a redistribution. Returns the final state."""
+    n = circuit.n
+    cur = Tensor(DENSE, [], [2] * n, psi)
+    for layer in circuit.layers[:layers]:
+        for (a, b), els in zip(layer.pairs, layer.gates):
+            cur, _, _ = contract(cur, Tensor(SYMM, [], [2, 2, 2, 2], els), [(a, 0), (b, 1)])
+        if layer.phases is not None:
+            for qb in range(n):
+                d = np.array([1.0, np.exp(1j * layer.phases[qb])], dtype=np.complex128)
+                cur, _, _ = contract(cur, Tensor(DIAG, [], [2, 2], d), [(qb, 0)])
+        if layer.ptup is not None:
+            cur = Tensor(DENSE, [], [2] * n, permute(cur.els.reshape([2] * n), layer.ptup))
+    return cur.els

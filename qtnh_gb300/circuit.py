@@ -1,0 +1,76 @@
+"""Run a layered circuit on a device-resident state through the C ABI.
+
+Each layer is the sequence of contractions a qtnh user would write:
+``Tensor::contract(state, gate, {{q_a, 0}, {q_b, 1}})`` for every gate (in-place
+rule, src/tensor/contract.cpp:250-289), one rank-2 DiagTensor contraction per
+qubit for a phase layer, and ``Tensor::rescatter`` / ``Tensor::permute`` /
+``Tensor::rescatter`` for a redistribution. The runner issues them as the
+batched entry points of the C ABI (qtnh_apply_gate_layer, qtnh_apply_diag_layer,
+qtnh_permute); rescatter is metadata-only with all slabs resident.
+All argument arrays are built once so the timed loop is only library calls.
+"""
+import ctypes
+
+import numpy as np
+
+from . import (_stream, _u16, _u64, check, lib)
+from .workload import phase_factors
+
+
+class DeviceCircuit:
+    def __init__(self, circuit, device="cuda"):
+        import torch
+        self.n = circuit.n
+        self.dims = _u64(circuit.dims)
+        self.rank = ctypes.c_int32(circuit.n)
+        all_gates = [g for l in circuit.layers for g in l.gates]
+        self.gates = torch.from_numpy(np.concatenate(all_gates) if all_gates else np.zeros(1, np.complex128)).to(device)
+        base = self.gates.data_ptr()
+        self.steps = []
+        gi = 0
+        for layer in circuit.layers:
+            ng = len(layer.gates)
+            if ng:
+                ks = (ctypes.c_int32 * ng)(*([2] * ng))
+                tg = _u16([x for p in layer.pairs for x in p])
+                ptrs = (ctypes.c_void_p * ng)(*[base + 16 * 16 * (gi + j) for j in range(ng)])
+                self.steps.append(("gates", (ctypes.c_int32(ng), ks, tg, ptrs)))
+                gi += ng
+            if layer.phases is not None:
+                f = torch.from_numpy(phase_factors(layer.phases)).to(device)
+                axes = _u16(range(self.n))
+                self.steps.append(("diag", (ctypes.c_int32(self.n), axes, f)))
+            if layer.ptup is not None:
+                self.steps.append(("perm", _u16(layer.ptup)))
+        self.layers = len(circuit.layers)
+        self.gate_count = gi
+
+    def run(self, state, scratch, stream=None, events=None):
+        """Apply the circuit; returns the buffer holding the result (state or scratch).
+
+        events: optional dict of kind -> list of (start, end) CUDA event pairs recorded
+        around every library call on the launch stream (for per-kernel timing)."""
+        L = lib()
+        st = _stream(stream)
+        cur, other = state, scratch
+        for kind, args in self.steps:
+            ev = None
+            if events is not None:
+                import torch
+                ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                ev[0].record(stream)
+            if kind == "gates":
+                ng, ks, tg, ptrs = args
+                check(L.qtnh_apply_gate_layer(ctypes.c_void_p(cur.data_ptr()), self.rank, self.dims, ng, ks, tg, ptrs, st))
+            elif kind == "diag":
+                nf, axes, f = args
+                check(L.qtnh_apply_diag_layer(ctypes.c_void_p(cur.data_ptr()), self.rank, self.dims, nf, axes,
+                                              ctypes.c_void_p(f.data_ptr()), st))
+            else:
+                check(L.qtnh_permute(ctypes.c_void_p(cur.data_ptr()), ctypes.c_void_p(other.data_ptr()), self.rank,
+                                     self.dims, args, st))
+                cur, other = other, cur
+            if ev is not None:
+                ev[1].record(stream)
+                events.setdefault(kind, []).append(ev)
+        return cur

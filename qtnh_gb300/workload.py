@@ -1,0 +1,109 @@
+"""Seeded synthetic workloads in the shapes of the benchmark configurations.
+
+``random_circuit`` builds the layered random circuit used for gate-layers/s:
+n qubits, every layer a seeded random pairing of the qubits with one Haar-random
+two-qubit SymmTensor gate per pair; every 4th layer also a layer of per-qubit
+phase DiagTensors (phases uniform in [0, 2pi)); every 8th layer also a
+redistribution: the top 3 indices are made distributed (rescatter +3), exchanged
+with 3 seeded random local indices by a permutation (the single-GPU form of the
+reference's mixed distributed/local swap, src/tensor/dense.cpp:220-257), and
+gathered back (rescatter -3).
+
+Gates follow the SymmTensor element layout [in_0, in_1, out_0, out_1]
+(include/tensor/symm.hpp:22-45): contraction sums over the inputs, so a unitary
+U acting as psi' = U psi is stored as els[in, out] = U[out, in].
+Haar sampling: QR of a complex Gaussian matrix with the phase fix
+Q diag(R_ii / |R_ii|) (Mezzadri, "How to generate random matrices from the
+classical compact groups", 2007).
+"""
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def haar_unitary(rng, d):
+    z = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / math.sqrt(2.0)
+    qm, r = np.linalg.qr(z)
+    dr = np.diag(r)
+    return qm * (dr / np.abs(dr))
+
+
+def gate_elements(u):
+    """SymmTensor elements of a k-qubit unitary (els[in, out] = U[out, in])."""
+    return np.ascontiguousarray(u.T).reshape(-1).astype(np.complex128)
+
+
+@dataclass
+class Layer:
+    pairs: list                  # [(q_a, q_b)] — gate g acts with input 0 on q_a, input 1 on q_b
+    gates: list                  # SymmTensor elements (16 complex each)
+    phases: np.ndarray = None    # per-qubit phases for the diagonal layer, or None
+    ptup: list = None            # permutation after the layer, or None
+
+
+@dataclass
+class Circuit:
+    n: int
+    layers: list = field(default_factory=list)
+
+    @property
+    def dims(self):
+        return [2] * self.n
+
+    def gate_count(self):
+        return sum(len(l.gates) for l in self.layers)
+
+
+def random_circuit(n, depth, seed=2026, diag_every=4, perm_every=8, n_dis=3):
+    rng = np.random.default_rng(seed)
+    c = Circuit(n)
+    for l in range(depth):
+        order = rng.permutation(n)
+        pairs = [(int(order[2 * j]), int(order[2 * j + 1])) for j in range(n // 2)]
+        gates = [gate_elements(haar_unitary(rng, 4)) for _ in pairs]
+        layer = Layer(pairs, gates)
+        if diag_every and (l + 1) % diag_every == 0:
+            layer.phases = rng.uniform(0.0, 2.0 * math.pi, n)
+        if perm_every and (l + 1) % perm_every == 0:
+            local = rng.choice(np.arange(n_dis, n), size=n_dis, replace=False)
+            ptup = list(range(n))
+            for k in range(n_dis):
+                ptup[k], ptup[int(local[k])] = int(local[k]), k
+            layer.ptup = ptup
+        c.layers.append(layer)
+    return c
+
+
+def phase_factors(phases):
+    """Concatenated per-qubit diagonals (1, e^{i phi}) for a diagonal layer."""
+    return np.stack([np.ones_like(phases), np.exp(1j * phases)], axis=1).reshape(-1).astype(np.complex128)
+
+
+def inverse_circuit(c):
+    """The circuit that undoes ``c`` (layers reversed, U -> U^dagger, phases negated,
+    permutations inverted)."""
+    inv = Circuit(c.n)
+    for layer in reversed(c.layers):
+        # A layer runs gates, then phases, then the permutation; undo them in reverse.
+        if layer.ptup is not None:
+            ptup_inv = [0] * c.n
+            for i, p in enumerate(layer.ptup):
+                ptup_inv[p] = i
+            inv.layers.append(Layer([], [], None, ptup_inv))
+        if layer.phases is not None:
+            inv.layers.append(Layer([], [], -layer.phases, None))
+        gates = []
+        for els in reversed(layer.gates):
+            u = els.reshape(4, 4).T          # U[out, in]
+            gates.append(gate_elements(u.conj().T))
+        inv.layers.append(Layer(list(reversed(layer.pairs)), gates))
+    return inv
+
+
+def random_state(n, seed=7):
+    """i.i.d. complex Gaussian amplitudes normalised to unit L2 (numpy, host)."""
+    rng = np.random.default_rng(seed)
+    psi = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+    psi /= np.linalg.norm(psi)
+    return psi
