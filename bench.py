@@ -52,6 +52,9 @@ def _args():
     p.add_argument("--depth", type=int, default=40)
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--arith", default="f32x2", choices=["f32x2", "fp64"],
+                   help="arithmetic of the gate/diagonal kernels (storage is complex128 either way)")
+    p.add_argument("--no-arith-check", action="store_true")
     return p.parse_args()
 
 
@@ -227,6 +230,7 @@ def main():
         cpu = {"value": 1.0 / _extrapolate(spl, CPU_SAMPLE_N, a.n), "unit": UNIT, "cores": 1, "kind": "port",
                "sample": _sample_desc(a.n, 1)}
 
+    q.set_arithmetic(q.ARITH_F32X2 if a.arith == "f32x2" else q.ARITH_FP64)
     circ = wl.random_circuit(a.n, a.depth, seed=a.seed)
     dc = DeviceCircuit(circ, device=dev)
     N = 2 ** a.n
@@ -309,21 +313,38 @@ def main():
     e2e = world * a.depth * a.steps / (ems / 1e3)
     norm = q.norm2(cur)
 
+    # circuit-level cross-check of the two arithmetic modes on the same input
+    arith_check = None
+    if not a.no_arith_check:
+        outs = {}
+        for mode in ("f32x2", "fp64"):
+            q.set_arithmetic(q.ARITH_F32X2 if mode == "f32x2" else q.ARITH_FP64)
+            cur.copy_(host_in)
+            res = dc.run(cur, oth)
+            outs[mode] = res.clone()
+        q.set_arithmetic(q.ARITH_F32X2 if a.arith == "f32x2" else q.ARITH_FP64)
+        diff = torch.linalg.vector_norm(outs["f32x2"] - outs["fp64"]).item()
+        arith_check = {"circuit_rel_l2_f32x2_vs_fp64": diff / torch.linalg.vector_norm(outs["fp64"]).item(),
+                       "gates": dc.gate_count, "qubits": a.n}
+        del outs
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128", "data": "synthetic (seeded circuit; state i.i.d. complex Gaussian, unit L2)",
+            "dtype": "c128", "arith": a.arith,
+            "data": "synthetic (seeded circuit; state i.i.d. complex Gaussian, unit L2)",
             "config": _config(a),
-            "roofline": {"bound": "hbm", "kernel": "gate_kernel<4>", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": ("gate_kernel_f32x2<4>" if a.arith == "f32x2" else "gate_kernel<4>"), "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": _traffic("gate_kernel<4>", a.n), "alg_bytes_per_launch": alg_bytes,
+                         "traffic": _traffic("gate_kernel_f32x2<4>" if a.arith == "f32x2" else "gate_kernel<4>", a.n), "alg_bytes_per_launch": alg_bytes,
                          "launch_ms": gate_launch_ms, "time_share": share},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
             "clocks": ck,
             "gpu_launches": launches,
             "final_norm2": norm,
+            "arith_check": arith_check,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -87,6 +87,16 @@ int qtnh_stream_synchronize(void* stream);
 /* Number of kernels this library has launched since load (all entry points). */
 uint64_t qtnh_kernel_launch_count(void);
 
+/* Arithmetic of the complex128 gate and diagonal kernels (storage is always complex128).
+ * QTNH_ARITH_F32X2 (default): products and sums as compensated FP32 pairs (error-free
+ *   transformations) on the FP32 pipe; ~48-bit significands, per-contraction relative
+ *   error ~1e-14; groups with elements outside 2^-90..2^90 fall back to FP64.
+ * QTNH_ARITH_FP64: native FP64 fused multiply-adds.
+ * The environment variable QTNH_ARITH=fp64|f32x2 sets the initial mode. Process-wide. */
+enum { QTNH_ARITH_FP64 = 0, QTNH_ARITH_F32X2 = 1 };
+int qtnh_set_arithmetic(int mode);
+int qtnh_get_arithmetic(void);
+
 /* ---- data movement: TIDense kernels ------------------------------------------------ */
 
 /* Tensor::permute / TIDense::_permute_internal (src/tensor/dense.cpp:152-169, 354-488):

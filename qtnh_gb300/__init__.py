@@ -231,3 +231,15 @@ def norm2(x, stream=None):
     r = ctypes.c_double()
     check(lib().qtnh_norm2(_ptr(x), ctypes.c_uint64(x.numel()), ctypes.byref(r), _stream(stream)))
     return r.value
+
+
+ARITH_FP64, ARITH_F32X2 = 0, 1
+
+
+def set_arithmetic(mode):
+    """QTNH_ARITH_FP64 (0) or QTNH_ARITH_F32X2 (1) for the gate/diagonal kernels."""
+    check(lib().qtnh_set_arithmetic(ctypes.c_int(mode)))
+
+
+def get_arithmetic():
+    return int(lib().qtnh_get_arithmetic())

@@ -22,6 +22,7 @@
 #include <numeric>
 
 #include "cuda_common.cuh"
+#include "df32.cuh"
 
 namespace qtnh_impl {
 
@@ -32,7 +33,26 @@ constexpr int GATE_MAX_D = 16;
 struct GateParams {
   RestDesc other;              // indices that are not gate targets, merged, with state strides in s_in
   int64_t off[GATE_MAX_D];     // offsets of the D amplitudes of a group (row-major over targets)
+  // When every dimension is a power of two, the group base is the group index with
+  // zero bits inserted at the targets' bit positions (ascending): nins insertions of
+  // ins_width[j] zero bits at bit ins_pos[j].
+  int nins;
+  uint32_t ins_pos[8], ins_width[8];
 };
+
+__device__ __forceinline__ uint64_t group_base(uint64_t grp, const GateParams& p) {
+  if (p.nins >= 0) {
+    uint64_t b = grp;
+    for (int j = 0; j < p.nins; ++j) {
+      const uint64_t low = b & ((1ull << p.ins_pos[j]) - 1);
+      b = ((b >> p.ins_pos[j]) << (p.ins_pos[j] + p.ins_width[j])) | low;
+    }
+    return b;
+  }
+  uint64_t base, unused;
+  decode(grp, p.other, base, unused);
+  return base;
+}
 
 template <int D>
 __global__ void __launch_bounds__(256) gate_kernel(c128* __restrict__ psi, const c128* __restrict__ gate,
@@ -42,8 +62,7 @@ __global__ void __launch_bounds__(256) gate_kernel(c128* __restrict__ psi, const
   __syncthreads();
   for (uint64_t grp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; grp < p.other.total;
        grp += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t base, unused;
-    decode(grp, p.other, base, unused);
+    const uint64_t base = group_base(grp, p);
     c128 x[D];
 #pragma unroll
     for (int i = 0; i < D; ++i) x[i] = psi[base + p.off[i]];
@@ -53,6 +72,78 @@ __global__ void __launch_bounds__(256) gate_kernel(c128* __restrict__ psi, const
 #pragma unroll
       for (int i = 0; i < D; ++i) acc = cfma(g[i * D + o], x[i], acc);  // SymmTensor layout [in, out]
       psi[base + p.off[o]] = acc;
+    }
+  }
+}
+
+// FP64 fallback for one group (kept out of line so the float-float path is never
+// predicated over it; it re-reads the group, which has not been written yet).
+template <int D>
+__device__ __noinline__ void gate_group_fp64(c128* __restrict__ psi, uint64_t base, const int64_t* off,
+                                             const c128* __restrict__ g) {
+  c128 x[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) x[i] = psi[base + off[i]];
+#pragma unroll
+  for (int o = 0; o < D; ++o) {
+    c128 acc = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int i = 0; i < D; ++i) acc = cfma(g[i * D + o], x[i], acc);
+    psi[base + off[o]] = acc;
+  }
+}
+
+// Float-float variant (see df32.cuh): the FP32 pipe does the arithmetic, complex128 in
+// HBM. A warp whose groups have any element outside the split range takes the FP64
+// path (a warp-uniform branch); so does every group when a gate element is out of range.
+template <int D>
+__global__ void __launch_bounds__(256, (D <= 4 ? 3 : 1)) gate_kernel_f32x2(c128* __restrict__ psi,
+                                                                         const c128* __restrict__ gate,
+                                                                         const __grid_constant__ GateParams p) {
+  __shared__ c128 g[D * D];
+  __shared__ df::cf2 gs[D * D];
+  __shared__ int gate_ok;
+  if (threadIdx.x == 0) gate_ok = 1;
+  __syncthreads();
+  for (int t = threadIdx.x; t < D * D; t += blockDim.x) {
+    c128 v = gate[t];
+    g[t] = v;
+    bool ok = df::in_range_gate(v.x) && df::in_range_gate(v.y);
+    if (!ok) gate_ok = 0;
+    gs[t] = ok ? df::csplit(v.x, v.y) : df::cf2{{0.f, 0.f}, {0.f, 0.f}};
+  }
+  __syncthreads();
+  const bool gok = gate_ok != 0;
+  for (uint64_t grp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; grp < p.other.total;
+       grp += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t base = group_base(grp, p);
+    c128 x[D];
+    bool ok = gok;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      x[i] = psi[base + p.off[i]];
+      ok = ok && df::in_range_state(x[i].x) && df::in_range_state(x[i].y);
+    }
+    if (__all_sync(__activemask(), ok)) {
+      df::cf2 xs[D];
+#pragma unroll
+      for (int i = 0; i < D; ++i) xs[i] = df::csplit(x[i].x, x[i].y);
+#pragma unroll
+      for (int o = 0; o < D; ++o) {
+        df::acc re, im;
+        df::cmul_acc(gs[o], xs[0], re, im);
+#pragma unroll
+        for (int i = 1; i < D; ++i) {
+          const df::cf2 gi = gs[i * D + o];
+          df::acc_mac(re, gi.re, xs[i].re);
+          df::acc_mac(re, df::neg(gi.im), xs[i].im);
+          df::acc_mac(im, gi.re, xs[i].im);
+          df::acc_mac(im, gi.im, xs[i].re);
+        }
+        psi[base + p.off[o]] = make_double2(df::to_double(re), df::to_double(im));
+      }
+    } else {
+      gate_group_fp64<D>(psi, base, p.off, g);
     }
   }
 }
@@ -75,6 +166,28 @@ __global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const
     uint64_t idx = 0;
     for (int j = 0; j < p.k; ++j) idx += digit(e, p.stride[j], p.stride_log2[j], p.dim[j], p.dim_log2[j]) * p.mult[j];
     psi[e] = cmul(psi[e], __ldg(d + idx));
+  }
+}
+
+__device__ __noinline__ c128 cmul_fp64_outofline(c128 a, c128 b) { return cmul(a, b); }
+
+// a * b in float-float when both are in range (warp-uniform decision), else FP64.
+__device__ __forceinline__ c128 cmul_f32x2(c128 a, c128 b) {
+  bool ok = df::in_range_state(a.x) && df::in_range_state(a.y) && df::in_range_gate(b.x) && df::in_range_gate(b.y);
+  if (__all_sync(__activemask(), ok)) {
+    df::acc re, im;
+    df::cmul_acc(df::csplit(a.x, a.y), df::csplit(b.x, b.y), re, im);
+    return make_double2(df::to_double(re), df::to_double(im));
+  }
+  return cmul_fp64_outofline(a, b);
+}
+
+__global__ void __launch_bounds__(256) diag_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ d,
+                                                         const __grid_constant__ DiagParams p) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.n; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t idx = 0;
+    for (int j = 0; j < p.k; ++j) idx += digit(e, p.stride[j], p.stride_log2[j], p.dim[j], p.dim_log2[j]) * p.mult[j];
+    psi[e] = cmul_f32x2(psi[e], __ldg(d + idx));
   }
 }
 
@@ -113,6 +226,41 @@ __global__ void __launch_bounds__(256) layer_apply_kernel(c128* __restrict__ psi
     else h = e / lo_size, l = e % lo_size;
     c128 ph = cmul(__ldg(hi + h), __ldg(lo + l));
     psi[e] = cmul(psi[e], ph);
+  }
+}
+
+// Split copy of a phase table (float pairs) plus a per-entry range flag in the sign of
+// nothing: entries out of the gate range are kept as FP64 and flagged with NaN hi parts.
+__global__ void table_split_kernel(const c128* __restrict__ t, df::cf2* __restrict__ ts, uint64_t n) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+    c128 v = t[j];
+    if (df::in_range_gate(v.x) && df::in_range_gate(v.y)) ts[j] = df::csplit(v.x, v.y);
+    else ts[j] = df::cf2{{__int_as_float(0x7FC00000), 0.f}, {0.f, 0.f}};
+  }
+}
+
+__global__ void __launch_bounds__(256) layer_apply_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ hi,
+                                                                const c128* __restrict__ lo,
+                                                                const df::cf2* __restrict__ his,
+                                                                const df::cf2* __restrict__ los, uint64_t n,
+                                                                uint64_t lo_size, uint32_t lo_log2) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t h, l;
+    if (lo_log2 != 0xFFFFFFFFu) h = e >> lo_log2, l = e & (lo_size - 1);
+    else h = e / lo_size, l = e % lo_size;
+    c128 x = psi[e];
+    df::cf2 a = his[h], b = los[l];
+    bool ok = a.re.h == a.re.h && b.re.h == b.re.h && df::in_range_state(x.x) && df::in_range_state(x.y);
+    if (__all_sync(__activemask(), ok)) {
+      df::acc pr, pi;
+      df::cmul_acc(a, b, pr, pi);
+      df::cf2 ph{df::renorm(pr), df::renorm(pi)};
+      df::acc re, im;
+      df::cmul_acc(df::csplit(x.x, x.y), ph, re, im);
+      psi[e] = make_double2(df::to_double(re), df::to_double(im));
+    } else {
+      psi[e] = cmul_fp64_outofline(x, cmul_fp64_outofline(__ldg(hi + h), __ldg(lo + l)));
+    }
   }
 }
 
@@ -157,6 +305,20 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
   GateParams p;
   other_axes(dims, targets, p.other);
   dims_t st = row_strides(dims);
+  p.nins = -1;
+  {
+    bool pow2 = targets.size() <= 8;
+    for (auto d : dims) pow2 = pow2 && log2_or_none(d) != 0xFFFFFFFFu;
+    if (pow2) {
+      std::vector<uint16_t> ts(targets);
+      std::sort(ts.begin(), ts.end(), [&](uint16_t a, uint16_t b) { return st[a] < st[b]; });
+      p.nins = (int)ts.size();
+      for (size_t j = 0; j < ts.size(); ++j) {
+        p.ins_pos[j] = log2_or_none(st[ts[j]]);
+        p.ins_width[j] = log2_or_none(dims[ts[j]]);
+      }
+    }
+  }
   for (uint64_t c = 0; c < D && D <= GATE_MAX_D; ++c) {
     uint64_t rem = c, off = 0;
     for (int j = (int)targets.size() - 1; j >= 0; --j) {
@@ -170,16 +332,23 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
   c128* psi = static_cast<c128*>(state);
   const c128* g = static_cast<const c128*>(gate);
   int grid = grid_for((p.other.total + 255) / 256, 8);
+  const bool ff = arithmetic_mode() == QTNH_ARITH_F32X2;
+#define QTNH_GATE_CASE(DD)                                                  \
+  case DD:                                                                  \
+    if (ff) gate_kernel_f32x2<DD><<<grid, 256, 0, s>>>(psi, g, p);          \
+    else gate_kernel<DD><<<grid, 256, 0, s>>>(psi, g, p);                   \
+    break;
   switch (D) {
-    case 1: gate_kernel<1><<<grid, 256, 0, s>>>(psi, g, p); break;
-    case 2: gate_kernel<2><<<grid, 256, 0, s>>>(psi, g, p); break;
-    case 3: gate_kernel<3><<<grid, 256, 0, s>>>(psi, g, p); break;
-    case 4: gate_kernel<4><<<grid, 256, 0, s>>>(psi, g, p); break;
-    case 8: gate_kernel<8><<<grid, 256, 0, s>>>(psi, g, p); break;
-    case 9: gate_kernel<9><<<grid, 256, 0, s>>>(psi, g, p); break;
-    case 16: gate_kernel<16><<<grid, 256, 0, s>>>(psi, g, p); break;
+    QTNH_GATE_CASE(1)
+    QTNH_GATE_CASE(2)
+    QTNH_GATE_CASE(3)
+    QTNH_GATE_CASE(4)
+    QTNH_GATE_CASE(8)
+    QTNH_GATE_CASE(9)
+    QTNH_GATE_CASE(16)
     default: throw Error(QTNH_ERR_UNSUPPORTED, "gate size outside the register-blocked kernel");
   }
+#undef QTNH_GATE_CASE
   count_launch();
   check_cuda(cudaGetLastError(), "gate_kernel launch");
 }
@@ -205,7 +374,10 @@ void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16
   }
   cudaStream_t s = (cudaStream_t)stream;
   int grid = grid_for((n + 255) / 256, 8);
-  diag_kernel<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
+  if (arithmetic_mode() == QTNH_ARITH_F32X2)
+    diag_kernel_f32x2<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
+  else
+    diag_kernel<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
   count_launch();
   check_cuda(cudaGetLastError(), "diag_kernel launch");
 }
@@ -241,13 +413,24 @@ void apply_diag_layer_device(void* state, const dims_t& dims, const std::vector<
     ++t.nf;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  c128* tables = static_cast<c128*>(workspace_alloc((lo_size + hi_size) * sizeof(c128), stream));
+  const bool ff = arithmetic_mode() == QTNH_ARITH_F32X2;
+  const size_t tab = lo_size + hi_size;
+  c128* tables = static_cast<c128*>(workspace_alloc(tab * sizeof(c128) * (ff ? 2 : 1), stream));
   const c128* fac = static_cast<const c128*>(factors);
   layer_table_kernel<<<grid_for((lo_size + 255) / 256, 4), 256, 0, s>>>(fac, tables, *lo);
   layer_table_kernel<<<grid_for((hi_size + 255) / 256, 4), 256, 0, s>>>(fac, tables + lo_size, *hi);
-  layer_apply_kernel<<<grid_for((n + 255) / 256, 8), 256, 0, s>>>(static_cast<c128*>(state), tables + lo_size, tables, n,
-                                                                  lo_size, log2_or_none(lo_size));
-  count_launch(3);
+  if (ff) {
+    df::cf2* split_tab = reinterpret_cast<df::cf2*>(tables + tab);
+    table_split_kernel<<<grid_for((tab + 255) / 256, 4), 256, 0, s>>>(tables, split_tab, tab);
+    layer_apply_kernel_f32x2<<<grid_for((n + 255) / 256, 8), 256, 0, s>>>(
+        static_cast<c128*>(state), tables + lo_size, tables, split_tab + lo_size, split_tab, n, lo_size,
+        log2_or_none(lo_size));
+    count_launch(4);
+  } else {
+    layer_apply_kernel<<<grid_for((n + 255) / 256, 8), 256, 0, s>>>(static_cast<c128*>(state), tables + lo_size, tables,
+                                                                    n, lo_size, log2_or_none(lo_size));
+    count_launch(3);
+  }
   cudaError_t e = cudaGetLastError();
   workspace_free(tables, stream);
   check_cuda(e, "diagonal layer launch");

@@ -32,6 +32,7 @@ int guarded(F&& f) {
 }
 
 extern std::atomic<uint64_t> g_launches;
+int arithmetic_mode();  // QTNH_ARITH_*
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 inline uint64_t product(const dims_t& d) {

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -18,6 +19,18 @@ static thread_local std::string g_last_error = "";
 std::atomic<uint64_t> g_launches{0};
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+static std::atomic<int> g_arith{-1};
+
+int arithmetic_mode() {
+  int m = g_arith.load(std::memory_order_relaxed);
+  if (m < 0) {
+    const char* e = std::getenv("QTNH_ARITH");
+    m = (e && std::strcmp(e, "fp64") == 0) ? QTNH_ARITH_FP64 : QTNH_ARITH_F32X2;
+    g_arith.store(m);
+  }
+  return m;
+}
 
 int status_from_current_exception() {
   try {
@@ -94,6 +107,16 @@ extern "C" {
 const char* qtnh_last_error(void) { return g_last_error.c_str(); }
 int qtnh_abi_version(void) { return QTNH_ABI_VERSION; }
 uint64_t qtnh_kernel_launch_count(void) { return g_launches.load(); }
+
+int qtnh_set_arithmetic(int mode) {
+  return guarded([&]() -> int {
+    if (mode != QTNH_ARITH_FP64 && mode != QTNH_ARITH_F32X2) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown arithmetic mode");
+    g_arith.store(mode);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_get_arithmetic(void) { return arithmetic_mode(); }
 
 int qtnh_device_count(int* count) {
   return guarded([&]() -> int {

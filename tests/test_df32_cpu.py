@@ -1,0 +1,16 @@
+"""Compensated FP32 ("float-float") arithmetic of the complex128 kernels, checked on the
+host: the header is __host__ __device__, so the same code compiles with g++."""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def test_df32_error_bounds(tmp_path):
+    exe = str(tmp_path / "df32_check")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "qtnh_gb300", "csrc"),
+                           "-o", exe, os.path.join(HERE, "cpp", "df32_check.cpp")])
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "ok" in out.stdout

@@ -31,6 +31,14 @@ def _setup():
     q.lib()
 
 
+@pytest.fixture(params=[q.ARITH_F32X2, q.ARITH_FP64], ids=["f32x2", "fp64"])
+def arith(request):
+    old = q.get_arithmetic()
+    q.set_arithmetic(request.param)
+    yield request.param
+    q.set_arithmetic(old)
+
+
 def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128).reshape(-1)).cuda()
 
@@ -42,6 +50,8 @@ def host(t):
 
 def rel_l2(a, b):
     a, b = np.asarray(a).reshape(-1), np.asarray(b).reshape(-1)
+    scale = max(np.max(np.abs(b)) if b.size else 0.0, 1e-300)
+    a, b = a / scale, b / scale
     nb = np.linalg.norm(b)
     return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
 
@@ -205,7 +215,7 @@ def haar(rng, d):
 
 
 @pytest.mark.parametrize("k", [1, 2, 3, 4])
-def test_symmetric_gate_in_place(k):
+def test_symmetric_gate_in_place(k, arith):
     nrng = np.random.default_rng(20 + k)
     n = 12
     psi = crandn(nrng, [2] * n)
@@ -217,7 +227,7 @@ def test_symmetric_gate_in_place(k):
     assert rel_l2(out, ref) < REL_TOL
 
 
-def test_gate_kernel_direct_matches_oracle():
+def test_gate_kernel_direct_matches_oracle(arith):
     nrng = np.random.default_rng(4)
     n = 16
     psi = crandn(nrng, [2] * n)
@@ -230,7 +240,7 @@ def test_gate_kernel_direct_matches_oracle():
     assert rel_l2(host(st), ref.els) < REL_TOL
 
 
-def test_diagonal_in_place_and_layer():
+def test_diagonal_in_place_and_layer(arith):
     nrng = np.random.default_rng(6)
     n = 14
     psi = crandn(nrng, [2] * n)
@@ -261,3 +271,70 @@ def test_distributed_identity_moves_index():
     psi = crandn(nrng, [2, 2, 2])
     out, ref = _run_contract((q.DENSE, [], [2, 2, 2], psi, 0), (q.IDEN, [2], [2], None, 0), [(1, 1)])
     assert np.array_equal(out, ref)
+
+
+def test_f32x2_falls_back_to_fp64_out_of_range():
+    # tiny and huge magnitudes, zeros and subnormals in one state: groups outside the
+    # split range take the FP64 path, the rest the float-float path; all within tolerance
+    old = q.get_arithmetic()
+    q.set_arithmetic(q.ARITH_F32X2)
+    try:
+        nrng = np.random.default_rng(12)
+        n = 10
+        psi = crandn(nrng, [2] * n).reshape(-1)
+        psi[:64] *= 1e-200
+        psi[64:128] *= 1e200
+        psi[128:160] = 0.0
+        psi[160] = 5e-324
+        u = haar(nrng, 4)
+        els = u.T.reshape(-1)
+        st = dev(psi)
+        q.apply_gate(st, [2] * n, [2, 9], dev(els))
+        ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], [2] * n, psi), orc.Tensor(orc.SYMM, [], [2] * 4, els),
+                                 [(2, 0), (9, 1)])
+        out = host(st)
+        for sl in (slice(0, 64), slice(64, 128), slice(128, 1024)):
+            assert rel_l2(out[sl], ref.els[sl]) < REL_TOL
+    finally:
+        q.set_arithmetic(old)
+
+
+def test_circuit_inverse_returns_state(arith):
+    # size-independent property: circuit followed by its inverse is the identity
+    from qtnh_gb300 import workload as wl
+    from qtnh_gb300.circuit import DeviceCircuit
+    n = 20
+    c = wl.random_circuit(n, 16, seed=5)
+    psi = wl.random_state(n, seed=6)
+    st = dev(psi)
+    scratch = torch.empty_like(st)
+    out = DeviceCircuit(c).run(st, scratch)
+    other = scratch if out is st else st
+    back = DeviceCircuit(wl.inverse_circuit(c)).run(out, other)
+    assert rel_l2(host(back), psi) < 1e-12
+
+
+def test_circuit_matches_oracle(arith):
+    from qtnh_gb300 import workload as wl
+    from qtnh_gb300.circuit import DeviceCircuit
+    n = 14
+    c = wl.random_circuit(n, 16, seed=8)
+    psi = wl.random_state(n, seed=9)
+    st = dev(psi)
+    out = DeviceCircuit(c).run(st, torch.empty_like(st))
+    ref = orc.run_circuit(psi, c)
+    assert rel_l2(host(out), ref) < 1e-12
+
+
+@pytest.mark.parametrize("k", [1, 2])
+def test_symmetric_gate_qutrits(k, arith):
+    # non-power-of-two dimensions take the general index decode and the D=3 / D=9 kernels
+    nrng = np.random.default_rng(30 + k)
+    dims = [3, 2, 3, 3, 2, 3]
+    psi = crandn(nrng, dims)
+    u = haar(nrng, 3 ** k)
+    els = u.T.reshape(-1)
+    targets = [0, 3] if k == 2 else [5]
+    wires = [(t, j) for j, t in enumerate(targets)]
+    out, ref = _run_contract((q.DENSE, [], dims, psi, 0), (q.SYMM, [], [3] * (2 * k), els, 0), wires)
+    assert rel_l2(out, ref) < REL_TOL
