@@ -84,6 +84,13 @@ int qtnh_memcpy_d2h(void* dst_host, const void* src, size_t bytes, void* stream)
 int qtnh_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream);
 int qtnh_memset(void* dst, int value, size_t bytes, void* stream);
 int qtnh_stream_synchronize(void* stream);
+int qtnh_device_synchronize(void);
+int qtnh_stream_create(void** stream);  /* non-blocking stream */
+int qtnh_stream_destroy(void* stream);
+/* Stream-ordered allocation from the device's memory pool (cudaMallocAsync): cheap
+ * for the many small tensors of a network, reused without device synchronisation. */
+int qtnh_malloc_async(void** ptr, size_t bytes, void* stream);
+int qtnh_free_async(void* ptr, void* stream);
 /* Number of kernels this library has launched since load (all entry points). */
 uint64_t qtnh_kernel_launch_count(void);
 

@@ -1,6 +1,9 @@
 """Build the engine's shared libraries in-tree.
 
 ``libqtnh_cuda.so``  C ABI + CUDA kernels (sm_103a), from ``csrc/*.cu`` and ``csrc/*.cpp``.
+``libqtnh.so``       the qtnh C++ API (``include/qtnh.hpp``), from ``cpp/*.cpp``; calls only
+                     the C ABI and needs no CUDA headers.
+``tests/cpp/_build/api_test``  the C++ API test driver.
 
 Every .cu file is compiled with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo`` in parallel; the CUDA
@@ -19,6 +22,11 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 INCLUDE = os.path.join(ROOT, "include")
 CUDA_LIB = "libqtnh_cuda.so"
+API_LIB = "libqtnh.so"
+CPP = os.path.join(HERE, "cpp")
+TEST_SRC = os.path.join(ROOT, "tests", "cpp", "api_test.cpp")
+TEST_BIN = os.path.join(ROOT, "tests", "cpp", "_build", "api_test")
+CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-I", INCLUDE, "-I", CPP]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
@@ -66,9 +74,48 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    api = _build_api(lib, force)
+    _build_test(api, force)
     if verbose:
-        print("built", lib)
+        print("built", lib, api, TEST_BIN)
     return lib
+
+
+def _newer(target, deps):
+    return os.path.exists(target) and os.path.getmtime(target) >= max(os.path.getmtime(d) for d in deps)
+
+
+def _api_headers():
+    hs = []
+    for d, _, fs in os.walk(INCLUDE):
+        hs += [os.path.join(d, f) for f in fs if f.endswith((".hpp", ".h"))]
+    hs += [os.path.join(CPP, f) for f in os.listdir(CPP) if f.endswith(".hpp")]
+    return hs
+
+
+def _build_api(cuda_lib, force):
+    srcs = sorted(os.path.join(CPP, f) for f in os.listdir(CPP) if f.endswith(".cpp"))
+    api = os.path.join(LIBDIR, API_LIB)
+    if not force and _newer(api, srcs + _api_headers() + [cuda_lib]):
+        return api
+    cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-shared", "-o", api] + srcs + [
+        "-L", LIBDIR, "-lqtnh_cuda", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("API library build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return api
+
+
+def _build_test(api, force):
+    os.makedirs(os.path.dirname(TEST_BIN), exist_ok=True)
+    if not force and _newer(TEST_BIN, [TEST_SRC, api] + _api_headers()):
+        return TEST_BIN
+    cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-o", TEST_BIN, TEST_SRC, "-L", LIBDIR, "-lqtnh", "-lqtnh_cuda",
+                                                        "-Wl,-rpath," + LIBDIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("API test build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return TEST_BIN
 
 
 if __name__ == "__main__":

@@ -1,0 +1,409 @@
+// QTNHEnv, utils, TIndexing and the device array behind every stored tensor.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+
+#include "qtnh.hpp"
+#include "qtnh_cuda.h"
+#include "facade_internal.hpp"
+
+namespace qtnh {
+
+namespace detail {
+
+void check(int rc) {
+  if (rc == QTNH_OK) return;
+  std::string msg = qtnh_last_error();
+  switch (rc) {
+    case QTNH_ERR_INVALID_ARGUMENT: throw std::invalid_argument(msg);
+    case QTNH_ERR_OUT_OF_RANGE: throw std::out_of_range(msg);
+    case QTNH_ERR_NO_MEMORY: throw std::bad_alloc();
+    default: throw std::runtime_error(msg);
+  }
+}
+
+// Host mirrors above this size are dropped after upload (re-read on demand).
+static const std::size_t kKeepMirrorElems = (std::size_t)16 << 20;
+
+DeviceArray::DeviceArray(const QTNHEnv& env, std::vector<tel>&& host) : env_(&env), n_(host.size()) {
+  check(qtnh_malloc_async(&dev_, std::max<std::size_t>(n_, 1) * sizeof(tel), env.stream));
+  if (n_) check(qtnh_memcpy_h2d(dev_, host.data(), n_ * sizeof(tel), env.stream));
+  if (n_ <= kKeepMirrorElems) {
+    host_ = std::move(host);
+    host_valid_ = true;
+  }
+}
+
+DeviceArray::DeviceArray(const QTNHEnv& env, std::size_t n) : env_(&env), n_(n) {
+  check(qtnh_malloc_async(&dev_, std::max<std::size_t>(n_, 1) * sizeof(tel), env.stream));
+}
+
+DeviceArray::~DeviceArray() {
+  if (dev_) qtnh_free_async(dev_, env_->stream);
+}
+
+DeviceArray::DeviceArray(DeviceArray&& o) noexcept
+    : env_(o.env_), dev_(o.dev_), n_(o.n_), host_(std::move(o.host_)), host_valid_(o.host_valid_),
+      host_dirty_(o.host_dirty_) {
+  o.dev_ = nullptr;
+  o.n_ = 0;
+  o.host_valid_ = o.host_dirty_ = false;
+}
+
+DeviceArray& DeviceArray::operator=(DeviceArray&& o) noexcept {
+  if (this != &o) {
+    if (dev_) qtnh_free_async(dev_, env_->stream);
+    env_ = o.env_;
+    dev_ = o.dev_;
+    n_ = o.n_;
+    host_ = std::move(o.host_);
+    host_valid_ = o.host_valid_;
+    host_dirty_ = o.host_dirty_;
+    o.dev_ = nullptr;
+    o.n_ = 0;
+    o.host_valid_ = o.host_dirty_ = false;
+  }
+  return *this;
+}
+
+void DeviceArray::flush() const {
+  if (host_dirty_ && dev_) {
+    check(qtnh_memcpy_h2d(dev_, host_.data(), n_ * sizeof(tel), env_->stream));
+    check(qtnh_stream_synchronize(env_->stream));  // the mirror may change right after
+    host_dirty_ = false;
+  }
+}
+
+void DeviceArray::pull() const {
+  if (host_valid_) return;
+  if (!dev_) throw std::runtime_error("tensor has no storage");
+  host_.resize(n_);
+  if (n_) check(qtnh_memcpy_d2h(host_.data(), dev_, n_ * sizeof(tel), env_->stream));
+  check(qtnh_stream_synchronize(env_->stream));
+  host_valid_ = true;
+}
+
+const void* DeviceArray::read() const {
+  flush();
+  return dev_;
+}
+
+void* DeviceArray::write() {
+  flush();
+  host_valid_ = false;
+  host_.clear();
+  host_.shrink_to_fit();
+  return dev_;
+}
+
+const tel& DeviceArray::host_at(std::size_t i) const {
+  pull();
+  return host_.at(i);
+}
+
+tel& DeviceArray::host_ref(std::size_t i) {
+  pull();
+  tel& r = host_.at(i);
+  host_dirty_ = true;
+  return r;
+}
+
+std::vector<tel> DeviceArray::to_host() const {
+  pull();
+  return host_;
+}
+
+DeviceArray DeviceArray::clone() const {
+  DeviceArray c(*env_, n_);
+  flush();
+  if (n_) check(qtnh_memcpy_d2d(c.dev_, dev_, n_ * sizeof(tel), env_->stream));
+  if (host_valid_ && !host_dirty_) {
+    c.host_ = host_;
+    c.host_valid_ = true;
+  }
+  return c;
+}
+
+}  // namespace detail
+
+QTNHEnv::QTNHEnv() : proc_id(0), num_processes(1), device(0), stream(nullptr) {
+  int n = 0;
+  detail::check(qtnh_device_count(&n));
+  if (n == 0) throw std::runtime_error("QTNHEnv: no CUDA device is visible");
+  if (const char* d = std::getenv("QTNH_DEVICE")) device = std::atoi(d);
+  detail::check(qtnh_set_device(device));
+  detail::check(qtnh_stream_create(&stream));
+}
+
+QTNHEnv::~QTNHEnv() {
+  if (stream) {
+    qtnh_stream_synchronize(stream);
+    qtnh_stream_destroy(stream);
+  }
+}
+
+void QTNHEnv::synchronize() const { detail::check(qtnh_stream_synchronize(stream)); }
+
+void QTNHEnv::print() const {
+  std::cout << "Process ID: " << proc_id << std::endl;
+  std::cout << "Process count: " << num_processes << std::endl;
+  std::cout << "Device: " << device << std::endl;
+}
+
+namespace utils {
+
+void throw_unimplemented() { throw std::runtime_error("Unimplemented function!"); }
+
+bool is_root() { return true; }
+
+void barrier() { detail::check(qtnh_device_synchronize()); }
+
+std::size_t dims_to_size(qtnh::tidx_tup dims) {
+  std::size_t s = 1;
+  for (auto d : dims) s *= d;
+  return s;
+}
+
+std::size_t idxs_to_i(qtnh::tidx_tup idxs, qtnh::tidx_tup dims) {
+  std::size_t i = 0, base = 1;
+  for (int j = (int)idxs.size() - 1; j >= 0; --j) {
+    i += idxs.at(j) * base;
+    base *= dims.at(j);
+  }
+  return i;
+}
+
+qtnh::tidx_tup i_to_idxs(std::size_t i, qtnh::tidx_tup dims) {
+  qtnh::tidx_tup idxs(dims.size());
+  for (int j = (int)dims.size() - 1; j >= 0; --j) {
+    idxs.at(j) = i % dims.at(j);
+    i /= dims.at(j);
+  }
+  return idxs;
+}
+
+qtnh::tidx_tup concat_dims(qtnh::tidx_tup dims1, qtnh::tidx_tup dims2) {
+  dims1.insert(dims1.end(), dims2.begin(), dims2.end());
+  return dims1;
+}
+
+std::pair<qtnh::tidx_tup, qtnh::tidx_tup> split_dims(qtnh::tidx_tup dims, qtnh::tidx_tup_st n) {
+  if (n > dims.size()) throw std::out_of_range("split_dims: position beyond the tuple");
+  return {qtnh::tidx_tup(dims.begin(), dims.begin() + n), qtnh::tidx_tup(dims.begin() + n, dims.end())};
+}
+
+std::vector<qtnh::wire> invert_wires(std::vector<qtnh::wire> ws) {
+  for (auto& w : ws) std::swap(w.first, w.second);
+  return ws;
+}
+
+bool equal(qtnh::tel a, qtnh::tel b, double tol) {
+  const double dr = a.real() - b.real(), di = a.imag() - b.imag();
+  return std::sqrt(dr * dr + di * di) < tol;
+}
+
+}  // namespace utils
+
+// ---- TIndexing ---------------------------------------------------------------------
+
+namespace ops {
+std::ostream& operator<<(std::ostream& out, const qtnh::tidx_tup& o) {
+  out << "(";
+  for (std::size_t i = 0; i < o.size(); ++i) out << o[i] << (i + 1 < o.size() ? ", " : "");
+  return out << ")";
+}
+std::ostream& operator<<(std::ostream& out, const TIFlag& o) { return out << "(" << o.tag << ", " << o.label << ")"; }
+}  // namespace ops
+
+// Fastest-first order: descending tag; among equal tags the last index first.
+static std::vector<std::size_t> order_of(const std::vector<TIFlag>& ifls) {
+  std::vector<std::size_t> m(ifls.size());
+  std::iota(m.begin(), m.end(), 0);
+  std::stable_sort(m.begin(), m.end(), [&](std::size_t a, std::size_t b) { return ifls[a].tag < ifls[b].tag; });
+  std::reverse(m.begin(), m.end());
+  return m;
+}
+
+TIndexing::TIndexing(qtnh::tidx_tup dims) : TIndexing(dims, std::vector<TIFlag>(dims.size(), {"default", 0})) {}
+TIndexing::TIndexing(qtnh::tidx_tup dims, std::vector<TIFlag> ifls) : dims_(dims), ifls_(ifls), maps_(order_of(ifls_)) {}
+
+bool TIndexing::isValid(qtnh::tidx_tup idxs) const {
+  if (idxs.size() != dims_.size()) return false;
+  for (std::size_t i = 0; i < idxs.size(); ++i)
+    if (idxs[i] >= dims_[i]) return false;
+  return true;
+}
+
+bool TIndexing::isEqual(qtnh::tidx_tup a, qtnh::tidx_tup b, std::string label) const {
+  for (std::size_t i = 0; i < a.size(); ++i)
+    if (ifls_.at(i).label == label && a[i] != b.at(i)) return false;
+  return true;
+}
+
+bool TIndexing::isLast(qtnh::tidx_tup idxs, std::string label) const {
+  for (std::size_t i = 0; i < idxs.size(); ++i)
+    if (ifls_.at(i).label == label && idxs[i] != dims_.at(i) - 1) return false;
+  return true;
+}
+
+qtnh::tidx_tup TIndexing::next(qtnh::tidx_tup idxs, std::string label) const {
+  for (std::size_t i = 0; i < idxs.size(); ++i) {
+    std::size_t k = maps_.at(i);
+    if (ifls_.at(k).label != label) continue;
+    if (idxs.at(k) < dims_.at(k) - 1) {
+      ++idxs[k];
+      return idxs;
+    }
+    if (idxs[k] == dims_[k] - 1) {
+      idxs[k] = 0;
+      continue;
+    }
+    break;
+  }
+  throw std::out_of_range("Tuple is outside of indexing.");
+}
+
+qtnh::tidx_tup TIndexing::prev(qtnh::tidx_tup idxs, std::string label) const {
+  for (std::size_t i = 0; i < idxs.size(); ++i) {
+    std::size_t k = maps_.at(i);
+    if (ifls_.at(k).label != label) continue;
+    if (idxs.at(k) == 0) {
+      idxs[k] = dims_.at(k) - 1;
+      continue;
+    }
+    if (idxs[k] < dims_.at(k)) {
+      --idxs[k];
+      return idxs;
+    }
+    break;
+  }
+  throw std::out_of_range("Tuple is outside of indexing.");
+}
+
+qtnh::tidx_tup TIndexing::reset(qtnh::tidx_tup idxs, std::string label) const {
+  for (std::size_t i = 0; i < idxs.size(); ++i)
+    if (ifls_.at(i).label == label) idxs[i] = 0;
+  return idxs;
+}
+
+TIndexing TIndexing::cut(std::string label) const {
+  qtnh::tidx_tup d;
+  std::vector<TIFlag> f;
+  for (std::size_t i = 0; i < dims_.size(); ++i)
+    if (ifls_[i].label != label) d.push_back(dims_[i]), f.push_back(ifls_[i]);
+  return TIndexing(d, f);
+}
+
+TIndexing TIndexing::keep(std::string label) const {
+  qtnh::tidx_tup d;
+  std::vector<TIFlag> f;
+  for (std::size_t i = 0; i < dims_.size(); ++i)
+    if (ifls_[i].label == label) d.push_back(dims_[i]), f.push_back(ifls_[i]);
+  return TIndexing(d, f);
+}
+
+TIndexing::TupIterator::TupIterator(qtnh::tidx_tup dims, std::vector<std::size_t> order, qtnh::tidx_tup start, bool is_end)
+    : dims_(dims), order_(order), current_(start), is_end_(is_end) {}
+
+TIndexing::TupIterator TIndexing::TupIterator::begin() {
+  auto s = current_;
+  for (auto k : order_) s.at(k) = 0;
+  return TupIterator(dims_, order_, s, false);
+}
+
+TIndexing::TupIterator TIndexing::TupIterator::end() { return TupIterator(dims_, order_, current_, true); }
+
+TIndexing::TupIterator& TIndexing::TupIterator::operator++() {
+  for (auto k : order_) {
+    if (current_.at(k) < dims_.at(k) - 1) {
+      ++current_[k];
+      return *this;
+    }
+    if (current_[k] == dims_[k] - 1) current_[k] = 0;
+  }
+  is_end_ = true;
+  return *this;
+}
+
+TIndexing::TupIterator TIndexing::TupIterator::operator++(int) {
+  auto old = *this;
+  ++*this;
+  return old;
+}
+
+TIndexing::NumIterator::NumIterator(qtnh::tidx_tup dims, std::vector<std::size_t> incrs, std::size_t zero,
+                                    qtnh::tidx_tup current_idxs, bool is_end)
+    : dims_(dims), incrs_(incrs), zero_(zero), current_idxs_(current_idxs), is_end_(is_end) {}
+
+TIndexing::NumIterator TIndexing::NumIterator::begin() {
+  return NumIterator(dims_, incrs_, zero_, qtnh::tidx_tup(current_idxs_.size(), 0), false);
+}
+
+TIndexing::NumIterator TIndexing::NumIterator::end() { return NumIterator(dims_, incrs_, zero_, current_idxs_, true); }
+
+TIndexing::NumIterator& TIndexing::NumIterator::operator++() {
+  for (std::size_t i = 0; i < current_idxs_.size(); ++i) {
+    if (current_idxs_[i] < dims_.at(i) - 1) {
+      ++current_idxs_[i];
+      return *this;
+    }
+    if (current_idxs_[i] == dims_[i] - 1) current_idxs_[i] = 0;
+  }
+  is_end_ = true;
+  return *this;
+}
+
+TIndexing::NumIterator TIndexing::NumIterator::operator++(int) {
+  auto old = *this;
+  ++*this;
+  return old;
+}
+
+std::size_t TIndexing::NumIterator::operator*() const {
+  std::size_t r = zero_;
+  for (std::size_t i = 0; i < current_idxs_.size(); ++i) r += current_idxs_[i] * incrs_.at(i);
+  return r;
+}
+
+TIndexing::TupIterator TIndexing::tup(std::string label) const { return tup(label, qtnh::tidx_tup(dims_.size(), 0)); }
+
+TIndexing::TupIterator TIndexing::tup(std::string label, qtnh::tidx_tup start) const {
+  std::vector<std::size_t> order;
+  for (auto k : maps_)
+    if (ifls_.at(k).label == label) order.push_back(k);
+  return TupIterator(dims_, order, start, false);
+}
+
+TIndexing::NumIterator TIndexing::num(std::string label) const { return num(label, qtnh::tidx_tup(dims_.size(), 0)); }
+
+TIndexing::NumIterator TIndexing::num(std::string label, qtnh::tidx_tup start) const {
+  const std::size_t n = dims_.size();
+  std::vector<std::size_t> all(n);
+  std::size_t zero = 0, base = 1;
+  for (std::size_t i = 0; i < n; ++i) {
+    std::size_t k = n - i - 1;
+    all[k] = base;
+    if (ifls_.at(k).label != label) zero += start.at(k) * base;
+    base *= dims_[k];
+  }
+  qtnh::tidx_tup d, cur;
+  std::vector<std::size_t> inc;
+  for (auto k : maps_)
+    if (ifls_.at(k).label == label) d.push_back(dims_[k]), inc.push_back(all[k]), cur.push_back(start.at(k));
+  return NumIterator(d, inc, zero, cur, false);
+}
+
+TIndexing TIndexing::_app(const TIndexing& a, const TIndexing& b) {
+  auto d = a.dims_;
+  auto f = a.ifls_;
+  d.insert(d.end(), b.dims_.begin(), b.dims_.end());
+  f.insert(f.end(), b.ifls_.begin(), b.ifls_.end());
+  return TIndexing(d, f);
+}
+
+}  // namespace qtnh

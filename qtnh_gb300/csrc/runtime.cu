@@ -186,6 +186,45 @@ int qtnh_stream_synchronize(void* stream) {
   });
 }
 
+int qtnh_device_synchronize(void) {
+  return guarded([&]() -> int {
+    check_cuda(cudaDeviceSynchronize(), "device synchronize");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_stream_create(void** stream) {
+  return guarded([&]() -> int {
+    cudaStream_t s = nullptr;
+    check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    *stream = (void*)s;
+    return QTNH_OK;
+  });
+}
+
+int qtnh_stream_destroy(void* stream) {
+  return guarded([&]() -> int {
+    if (stream) check_cuda(cudaStreamDestroy((cudaStream_t)stream), "cudaStreamDestroy");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_malloc_async(void** ptr, size_t bytes, void* stream) {
+  return guarded([&]() -> int {
+    *ptr = nullptr;
+    if (bytes == 0) bytes = 16;
+    check_cuda(cudaMallocAsync(ptr, bytes, (cudaStream_t)stream), "cudaMallocAsync");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_free_async(void* ptr, void* stream) {
+  return guarded([&]() -> int {
+    if (ptr) check_cuda(cudaFreeAsync(ptr, (cudaStream_t)stream), "cudaFreeAsync");
+    return QTNH_OK;
+  });
+}
+
 int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream) {
   return guarded([&]() -> int {
     cudaStream_t s = (cudaStream_t)stream;

@@ -101,6 +101,37 @@ def parse_random_tn(src):
     return groups
 
 
+def _tensor_tokens(info):
+    out = [str(len(info["dims"]))] + [str(d) for d in info["dims"]] + [str(len(info["els"]))]
+    for re_, im_ in info["els"]:
+        out += [repr(re_), repr(im_)]
+    return out
+
+
+def write_text_fixtures(here, rt, tn):
+    """Whitespace-separated copies of the fixtures for the C++ API test driver
+    (tests/cpp/api_test.cpp): no JSON parser needed there."""
+    with open(os.path.join(here, "random_tensors.txt"), "w") as f:
+        for name, cases in rt.items():
+            f.write("group %s %d\n" % (name, len(cases)))
+            for c in cases:
+                toks = _tensor_tokens(c["t1"]) + _tensor_tokens(c["t2"]) + _tensor_tokens(c["t3"])
+                toks += [str(len(c["wires"]))] + [str(x) for w in c["wires"] for x in w]
+                f.write(" ".join(toks) + "\n")
+    with open(os.path.join(here, "random_tn.txt"), "w") as f:
+        for name, cases in tn.items():
+            f.write("group %s %d\n" % (name, len(cases)))
+            for c in cases:
+                toks = [str(len(c["tensors"]))]
+                for t in c["tensors"]:
+                    toks += _tensor_tokens(t)
+                toks += [str(len(c["bonds"]))]
+                for b in c["bonds"]:
+                    toks += [str(b["t1"]), str(b["t2"]), str(len(b["wires"]))] + [str(x) for w in b["wires"] for x in w]
+                toks += _tensor_tokens(c["result"])
+                f.write(" ".join(toks) + "\n")
+
+
 def main(argv):
     ref = argv[1] if len(argv) > 1 else os.environ.get("QTNH_REFERENCE", "/root/reference")
     here = os.path.dirname(os.path.abspath(__file__))
@@ -117,6 +148,7 @@ def main(argv):
     meta = dict(meta, source="reference tests/gen/random-tn.hpp (numpy seed 9457, two-decimal text)")
     with open(os.path.join(here, "random_tn.json"), "w") as f:
         json.dump({"meta": meta, "groups": tn}, f, separators=(",", ":"))
+    write_text_fixtures(here, rt, tn)
     for k, v in rt.items():
         print("random_tensors", k, len(v))
     for k, v in tn.items():
