@@ -155,6 +155,25 @@ int qtnh_contract_dense(const void* a, int32_t rank_a, const uint64_t* dims_a, c
                         const uint64_t* dims_b, int32_t nwires, const uint16_t* wires, const uint16_t* out_pos_a,
                         const uint16_t* out_pos_b, void* c, void* stream);
 
+/* Same contraction as qtnh_contract_dense, for callers that cannot allocate device
+ * memory while they run: hosts whose device memory is owned by their own allocator or
+ * fixed budget, and latency-critical loops where a cudaMalloc would stall or fragment.
+ * It has no counterpart in the reference (which contracts on host memory over MPI).
+ * The permuted copies of A, B and C live in one scratch array that the library defines
+ * at file scope in device memory (QTNH_NOALLOC_SCRATCH_ELEMS complex128 elements,
+ * 16 MiB, held by every GPU that loads the library until the process exits). The call
+ * allocates nothing; contractions whose permuted copies need more elements than that
+ * fail with QTNH_ERR_UNSUPPORTED before any work is issued. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress, with that device current);
+ * make that first call before any stream capture. Every call shares the one array and
+ * it keeps the previous call's contents (nothing in it needs to start at zero): calls
+ * that can overlap on the GPU, on different streams or threads, race on it and must be
+ * serialised by the caller. */
+#define QTNH_NOALLOC_SCRATCH_ELEMS (1u << 20)
+int qtnh_contract_dense_noalloc(const void* a, int32_t rank_a, const uint64_t* dims_a, const void* b, int32_t rank_b,
+                                const uint64_t* dims_b, int32_t nwires, const uint16_t* wires,
+                                const uint16_t* out_pos_a, const uint16_t* out_pos_b, void* c, void* stream);
+
 /* ---- symmetric gates and diagonals (the in-place rule, contract.cpp:250-289) -------- */
 
 /* psi'[.., o_j at targets[j], ..] = sum_in G[in, o] psi[.., in_j at targets[j], ..] where

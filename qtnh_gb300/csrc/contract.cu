@@ -133,6 +133,11 @@ bool is_identity(const std::vector<uint16_t>& p) {
 
 }  // namespace
 
+// GEMM launcher shared with the allocation-free contraction (noalloc.cu).
+void zgemm_launch(const c128* A, const c128* B, c128* C, uint64_t M, uint64_t N, uint64_t K, cudaStream_t s) {
+  zgemm(A, B, C, M, N, K, s);
+}
+
 void materialise_device(const TensorMeta& t, const void* data, void* out, void* stream) {
   MaterialiseParams p;
   dims_t tot = t.tot();
