@@ -14,3 +14,12 @@ def test_df32_error_bounds(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "ok" in out.stdout
+
+
+def test_ozaki_slices_exact_and_accurate(tmp_path):
+    exe = str(tmp_path / "ozaki_check")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "qtnh_gb300", "csrc"),
+                           "-o", exe, os.path.join(HERE, "cpp", "ozaki_check.cpp")])
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "ok" in out.stdout
