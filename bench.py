@@ -1,5 +1,5 @@
 #!/usr/bin/env python
-"""Gate-layers/s of the plain complex128 engine on the random layered circuit.
+"""Gate-layers/s of the complex128 contraction engine on the random layered circuit.
 
 Workload (the configuration the headline metric is quoted on): n = 28 qubits
 (2^28 complex128 amplitudes, 4 GiB), depth 40; every layer 14 Haar-random
@@ -12,9 +12,14 @@ L2 flush is needed between steps.
 value : gate-layers/s with the state resident in HBM (CUDA events on the launch stream).
 e2e   : the same through the C ABI with host buffers: every step copies the initial
         state from pinned host memory to the device and the result back.
-roofline: the dominant kernel (the two-qubit gate kernel), algorithmic bytes
-        32 * 2^n per launch over its event-timed average duration, against the
-        measured HBM copy bandwidth.
+arith : default bf16x6: each layer's gates applied as fused pairs (two disjoint
+        two-qubit gates = one 16x16 unitary) on the bf16 tensor cores with error-free
+        8-bit digits (complex128 in and out, ~1e-14 relative error per pair);
+        `--arith f32x2|fp64` times the per-gate float-float / native FP64 kernels.
+roofline: the dominant kernel (the fused gate-pair kernel; with f32x2/fp64 the
+        two-qubit gate kernel), algorithmic bytes 32 * 2^n per launch (the state read
+        and written once) over its event-timed average duration, against the measured
+        HBM copy bandwidth.
 cpu_baseline: the oracle port of the reference's contraction path on one host core,
         on a bounded sample (n = 20, 4 layers), extrapolated to n = 28.
 
@@ -52,7 +57,7 @@ def _args():
     p.add_argument("--depth", type=int, default=40)
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--arith", default="f32x2", choices=["f32x2", "fp64"],
+    p.add_argument("--arith", default="bf16x6", choices=["bf16x6", "f32x2", "fp64"],
                    help="arithmetic of the gate/diagonal kernels (storage is complex128 either way)")
     p.add_argument("--no-arith-check", action="store_true")
     return p.parse_args()
@@ -230,7 +235,7 @@ def main():
         cpu = {"value": 1.0 / _extrapolate(spl, CPU_SAMPLE_N, a.n), "unit": UNIT, "cores": 1, "kind": "port",
                "sample": _sample_desc(a.n, 1)}
 
-    q.set_arithmetic(q.ARITH_F32X2 if a.arith == "f32x2" else q.ARITH_FP64)
+    q.set_arithmetic(q.ARITH_NAMES[a.arith])
     circ = wl.random_circuit(a.n, a.depth, seed=a.seed)
     dc = DeviceCircuit(circ, device=dev)
     N = 2 ** a.n
@@ -282,9 +287,11 @@ def main():
     ms_per_step = ms / a.steps
     value = world * a.depth * a.steps / (ms / 1e3)
 
-    # roofline of the dominant kernel (two-qubit gate kernel)
+    # roofline of the dominant kernel (two-qubit gate kernel; with bf16x6 the fused
+    # gate-pair kernel, one launch per pair of gates)
     gate_ms = [s.elapsed_time(e) for s, e in events.get("gates", [])]
-    gates_per_call = a.n // 2
+    gates_per_call = (a.n // 2 + 1) // 2 if a.arith == "bf16x6" else a.n // 2
+    kernel = {"f32x2": "gate_kernel_f32x2<4>", "fp64": "gate_kernel<4>", "bf16x6": "gate_pair_tc_kernel"}[a.arith]
     gate_launch_ms = (sum(gate_ms) / len(gate_ms)) / gates_per_call if gate_ms else None
     alg_bytes = 32.0 * N
     peak, peak_kind = _peaks()
@@ -313,18 +320,19 @@ def main():
     e2e = world * a.depth * a.steps / (ems / 1e3)
     norm = q.norm2(cur)
 
-    # circuit-level cross-check of the two arithmetic modes on the same input
+    # circuit-level cross-check of the timed arithmetic against native FP64 on the same input
     arith_check = None
     if not a.no_arith_check:
         outs = {}
-        for mode in ("f32x2", "fp64"):
-            q.set_arithmetic(q.ARITH_F32X2 if mode == "f32x2" else q.ARITH_FP64)
+        mode = a.arith if a.arith != "fp64" else "f32x2"
+        for m in (mode, "fp64"):
+            q.set_arithmetic(q.ARITH_NAMES[m])
             cur.copy_(host_in)
             res = dc.run(cur, oth)
-            outs[mode] = res.clone()
-        q.set_arithmetic(q.ARITH_F32X2 if a.arith == "f32x2" else q.ARITH_FP64)
-        diff = torch.linalg.vector_norm(outs["f32x2"] - outs["fp64"]).item()
-        arith_check = {"circuit_rel_l2_f32x2_vs_fp64": diff / torch.linalg.vector_norm(outs["fp64"]).item(),
+            outs[m] = res.clone()
+        q.set_arithmetic(q.ARITH_NAMES[a.arith])
+        diff = torch.linalg.vector_norm(outs[mode] - outs["fp64"]).item()
+        arith_check = {"circuit_rel_l2_%s_vs_fp64" % mode: diff / torch.linalg.vector_norm(outs["fp64"]).item(),
                        "gates": dc.gate_count, "qubits": a.n}
         del outs
 
@@ -335,9 +343,9 @@ def main():
             "dtype": "c128", "arith": a.arith,
             "data": "synthetic (seeded circuit; state i.i.d. complex Gaussian, unit L2)",
             "config": _config(a),
-            "roofline": {"bound": "hbm", "kernel": ("gate_kernel_f32x2<4>" if a.arith == "f32x2" else "gate_kernel<4>"), "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": _traffic("gate_kernel_f32x2<4>" if a.arith == "f32x2" else "gate_kernel<4>", a.n), "alg_bytes_per_launch": alg_bytes,
+                         "traffic": _traffic(kernel, a.n), "alg_bytes_per_launch": alg_bytes,
                          "launch_ms": gate_launch_ms, "time_share": share},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},

@@ -95,12 +95,20 @@ int qtnh_free_async(void* ptr, void* stream);
 uint64_t qtnh_kernel_launch_count(void);
 
 /* Arithmetic of the complex128 gate and diagonal kernels (storage is always complex128).
- * QTNH_ARITH_F32X2 (default): products and sums as compensated FP32 pairs (error-free
+ * QTNH_ARITH_BF16X6 (default): qtnh_apply_gate_layer fuses consecutive disjoint pairs of
+ *   two-qubit gates (all dims 2) into 16x16 unitaries applied on the bf16 tensor cores:
+ *   each operand is cut into six error-free balanced 8-bit digits, every digit-product
+ *   level is summed exactly in FP32 (Ozaki scheme), and the levels are recombined to ~48
+ *   bits; relative error ~1e-14 per fused pair. Groups whose largest magnitude lies
+ *   outside 2^-200..2^200 (or holds an infinity/NaN) take FP64; subnormal amplitudes
+ *   count as zero there. Every other gate and diagonal runs as QTNH_ARITH_F32X2.
+ * QTNH_ARITH_F32X2: products and sums as compensated FP32 pairs (error-free
  *   transformations) on the FP32 pipe; ~48-bit significands, per-contraction relative
  *   error ~1e-14; groups with elements outside 2^-90..2^90 fall back to FP64.
  * QTNH_ARITH_FP64: native FP64 fused multiply-adds.
- * The environment variable QTNH_ARITH=fp64|f32x2 sets the initial mode. Process-wide. */
-enum { QTNH_ARITH_FP64 = 0, QTNH_ARITH_F32X2 = 1 };
+ * The environment variable QTNH_ARITH=fp64|f32x2|bf16x6 sets the initial mode.
+ * Process-wide. */
+enum { QTNH_ARITH_FP64 = 0, QTNH_ARITH_F32X2 = 1, QTNH_ARITH_BF16X6 = 2 };
 int qtnh_set_arithmetic(int mode);
 int qtnh_get_arithmetic(void);
 

@@ -233,11 +233,13 @@ def norm2(x, stream=None):
     return r.value
 
 
-ARITH_FP64, ARITH_F32X2 = 0, 1
+ARITH_FP64, ARITH_F32X2, ARITH_BF16X6 = 0, 1, 2
+ARITH_NAMES = {"fp64": ARITH_FP64, "f32x2": ARITH_F32X2, "bf16x6": ARITH_BF16X6}
 
 
 def set_arithmetic(mode):
-    """QTNH_ARITH_FP64 (0) or QTNH_ARITH_F32X2 (1) for the gate/diagonal kernels."""
+    """QTNH_ARITH_FP64 (0), QTNH_ARITH_F32X2 (1) or QTNH_ARITH_BF16X6 (2) for the
+    gate/diagonal kernels."""
     check(lib().qtnh_set_arithmetic(ctypes.c_int(mode)))
 
 

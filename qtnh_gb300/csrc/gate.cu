@@ -332,7 +332,7 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
   c128* psi = static_cast<c128*>(state);
   const c128* g = static_cast<const c128*>(gate);
   int grid = grid_for((p.other.total + 255) / 256, 8);
-  const bool ff = arithmetic_mode() == QTNH_ARITH_F32X2;
+  const bool ff = arithmetic_mode() != QTNH_ARITH_FP64;
 #define QTNH_GATE_CASE(DD)                                                  \
   case DD:                                                                  \
     if (ff) gate_kernel_f32x2<DD><<<grid, 256, 0, s>>>(psi, g, p);          \
@@ -374,7 +374,7 @@ void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16
   }
   cudaStream_t s = (cudaStream_t)stream;
   int grid = grid_for((n + 255) / 256, 8);
-  if (arithmetic_mode() == QTNH_ARITH_F32X2)
+  if (arithmetic_mode() != QTNH_ARITH_FP64)
     diag_kernel_f32x2<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
   else
     diag_kernel<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
@@ -413,7 +413,7 @@ void apply_diag_layer_device(void* state, const dims_t& dims, const std::vector<
     ++t.nf;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const bool ff = arithmetic_mode() == QTNH_ARITH_F32X2;
+  const bool ff = arithmetic_mode() != QTNH_ARITH_FP64;
   const size_t tab = lo_size + hi_size;
   c128* tables = static_cast<c128*>(workspace_alloc(tab * sizeof(c128) * (ff ? 2 : 1), stream));
   const c128* fac = static_cast<const c128*>(factors);
@@ -456,11 +456,17 @@ int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32
   return guarded([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK || ngates < 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     dims_t d(dims, dims + rank);
+    std::vector<std::vector<uint16_t>> tl((size_t)ngates);
     size_t o = 0;
     for (int32_t g = 0; g < ngates; ++g) {
       if (gate_k[g] < 0 || gate_k[g] > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "gate arity out of range");
-      apply_gate_device(state, d, std::vector<uint16_t>(targets + o, targets + o + gate_k[g]), gates[g], stream);
+      tl[g].assign(targets + o, targets + o + gate_k[g]);
       o += (size_t)gate_k[g];
+    }
+    if (arithmetic_mode() == QTNH_ARITH_BF16X6) {
+      apply_gate_layer_tc(state, d, tl, std::vector<const void*>(gates, gates + ngates), stream);
+    } else {
+      for (int32_t g = 0; g < ngates; ++g) apply_gate_device(state, d, tl[g], gates[g], stream);
     }
     return QTNH_OK;
   });

@@ -1,0 +1,338 @@
+// Two disjoint two-qubit gates fused into one 16x16 unitary, applied in place on the
+// tensor cores with error-free bf16 digits (ozaki.cuh).
+//
+// A gate layer holds disjoint gates, which commute, so consecutive pairs of a
+// qtnh_apply_gate_layer call fuse into U = U_a (x) U_b acting on the 16 amplitudes of a
+// group (the four target bits varying). In real form the group update is y = R x with
+// R = [[Re U, -Im U], [Im U, Re U]] (32 x 32) and x the 32 reals of the group. Per warp,
+// eight groups form the N = 8 columns of mma.sync.m16n8k16 tiles:
+//   * each lane fetches four complex amplitudes (2t, 2t+1, 2t+8, 2t+9 of group g =
+//     lane / 4, t = lane % 4) -- exactly the B-fragment rows it owns for both k-tiles
+//     (real parts k-tile 0, imaginary parts k-tile 1) -- two tiles ahead with cp.async,
+//     takes the group's largest exponent with two shuffles and cuts its 8 reals into 6
+//     balanced bf16 digits each;
+//   * R's six digits (per-row exponents) are laid out once per CTA in shared memory as
+//     per-lane A fragments;
+//   * 21 digit pairs (i + j <= 5) x 2 m-tiles x 2 k-tiles = 84 MMAs accumulate six exact
+//     FP32 level sums per output;
+//   * every output real is recombined (compensated adds) and written back.
+// A warp whose groups hold an infinity/NaN or a largest magnitude outside 2^-200..2^201
+// takes an FP64 path for its eight groups (warp-uniform branch). Subnormal amplitudes
+// (below 2^-1022) contribute zero digits: their weight against the group scale is below
+// 2^-822.
+
+#include <algorithm>
+#include <vector>
+
+#include "cuda_common.cuh"
+#include "ozaki.cuh"
+
+namespace qtnh_impl {
+
+namespace {
+
+constexpr int TC_THREADS = 256;
+constexpr int TC_WARPS = TC_THREADS / 32;
+constexpr int TC_STAGES = 2;
+
+struct PairParams {
+  uint64_t ntiles;      // groups / 8
+  uint32_t ins_pos[4];  // the four target bit positions, ascending
+  int64_t off[16];      // offset of amplitude (a0 a1 b0 b1) of a group
+};
+
+// Shared memory of one CTA (dynamic, 16-byte aligned).
+struct TcSmem {
+  uint4 afrag[oz::NS][2][2][32];              // digit, m-tile, k-tile, lane
+  double2 U16[256];                           // fused unitary, U16[o * 16 + i]
+  double2 stage[TC_STAGES][TC_WARPS][4][32];  // prefetched amplitudes: stage, warp, q, lane
+  int32_t erow[16];                           // max exponent of row o of R (= of row 16 + o)
+  int gate_ok;
+};
+
+// Index of the first amplitude of group `grp`: zero bits inserted at the target positions.
+template <typename IT>
+__device__ __forceinline__ IT pair_base(IT grp, const PairParams& p) {
+  IT b = grp;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const IT low = b & ((IT(1) << p.ins_pos[j]) - 1);
+    b = ((b >> p.ins_pos[j]) << (p.ins_pos[j] + 1)) | low;
+  }
+  return b;
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint4& a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// A group's (or a gate row's) largest biased exponent must lie in [TC_EMIN, TC_EMAX]
+// (magnitudes 2^-200 .. 2^201) unless it is 0 (zeros and subnormals only); infinities
+// and NaNs (exponent 0x7FF) fail. Then the level sums, scaled by 2^(Esum - 2060) through
+// the exponent field, stay normal doubles.
+constexpr uint32_t TC_EMIN = 823, TC_EMAX = 1224;
+
+// Gate entries: zero or a normal double (no subnormal, infinity or NaN).
+__device__ __forceinline__ bool tc_element_ok(df::dwords w) {
+  const uint32_t e = oz::exponent(w);
+  return e == 0 ? (((w.hi << 1) | w.lo) == 0u) : (e != 0x7FFu);
+}
+
+__device__ __forceinline__ bool tc_scale_ok(uint32_t emax) { return emax == 0 || (emax >= TC_EMIN && emax <= TC_EMAX); }
+
+// FP64 path for one warp's eight groups (all loads before the first store); gbase is
+// the lane's group base.
+template <typename IT>
+__device__ __noinline__ void pair_tile_fp64(double2* __restrict__ psi, IT gbase, const PairParams& p,
+                                            const double2* U16) {
+  const int lane = threadIdx.x & 31;
+  double2 x[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) x[i] = psi[gbase + (IT)p.off[i]];
+  __syncwarp();
+  const int o0 = (lane & 3) * 4;
+#pragma unroll
+  for (int oo = 0; oo < 4; ++oo) {
+    double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) acc = cfma(U16[(o0 + oo) * 16 + i], x[i], acc);
+    psi[gbase + (IT)p.off[o0 + oo]] = acc;
+  }
+}
+
+// Element (r, k) of the real form R of U16.
+__device__ __forceinline__ double real_form(const double2* U16, int r, int k) {
+  const double2 u = U16[(r & 15) * 16 + (k & 15)];
+  if (r < 16) return k < 16 ? u.x : -u.y;
+  return k < 16 ? u.y : u.x;
+}
+
+// Two CTAs per SM: up to 128 registers a thread, none spilled (three CTAs spill and run
+// slower).
+template <typename IT>
+__global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __restrict__ psi,
+                                                                     const double2* __restrict__ ga,
+                                                                     const double2* __restrict__ gb,
+                                                                     const __grid_constant__ PairParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
+  const int tid = threadIdx.x;
+
+  // ---- the fused gate: U16, row exponents, A fragments of its six digits ----
+  if (tid == 0) sm.gate_ok = 1;
+  for (int t = tid; t < 256; t += TC_THREADS) {
+    const int o = t >> 4, i = t & 15;
+    // SymmTensor layout G[in * 4 + out] = U[out][in]; U16[o][i] = Ua[oa][ia] Ub[ob][ib]
+    sm.U16[t] = cmul(ga[(i >> 2) * 4 + (o >> 2)], gb[(i & 3) * 4 + (o & 3)]);
+  }
+  __syncthreads();
+  if (tid < 16) {
+    uint32_t e = 0;
+    bool ok = true;
+    for (int i = 0; i < 16; ++i) {
+      const double2 u = sm.U16[tid * 16 + i];
+      const df::dwords wr = df::words(u.x), wi = df::words(u.y);
+      ok = ok && tc_element_ok(wr) && tc_element_ok(wi);
+      e = max(e, max(oz::exponent(wr), oz::exponent(wi)));
+    }
+    sm.erow[tid] = (int32_t)e;
+    if (!ok || !tc_scale_ok(e)) sm.gate_ok = 0;
+  }
+  __syncthreads();
+  // entries (r, k), (r, k + 1) of digit i form half 0 / 1 of register
+  // (r % 16) / 8 + 2 ((k % 16) / 8) of lane (r % 8) * 4 + (k % 8) / 2 in afrag[i][r / 16][k / 16]
+  for (int t = tid; t < 512; t += TC_THREADS) {
+    const int r = t >> 4, k = (t & 15) * 2;
+    const uint32_t E = (uint32_t)sm.erow[r & 15];
+    float d0[oz::NS], d1[oz::NS];
+    oz::digits(df::words(real_form(sm.U16, r, k)), E, d0);
+    oz::digits(df::words(real_form(sm.U16, r, k + 1)), E, d1);
+    const int rr = r & 15, kk = k & 15;
+    const int lane = (rr & 7) * 4 + ((kk & 7) >> 1);
+    const int reg = (rr >> 3) + 2 * (kk >> 3);
+#pragma unroll
+    for (int i = 0; i < oz::NS; ++i)
+      reinterpret_cast<uint32_t*>(&sm.afrag[i][r >> 4][k >> 4][lane])[reg] = oz::pack(d0[i], d1[i]);
+  }
+  __syncthreads();
+  const bool gok = sm.gate_ok != 0;
+
+  // ---- per-lane constants ----
+  const int lane = tid & 31, warp = tid >> 5, g = lane >> 2, t = lane & 3;
+  IT ld_off[4];  // the lane's four amplitudes relative to the tile base
+  {
+    const IT gb0 = pair_base<IT>((IT)g, p);
+    const int am[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ld_off[q] = gb0 + (IT)p.off[am[q]];
+  }
+  IT st_off[4];  // outputs c: row g + 8 (c / 2) of group 2t + (c % 2)
+  {
+    const IT c0 = pair_base<IT>((IT)(2 * t), p), c1 = pair_base<IT>((IT)(2 * t + 1), p);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) st_off[c] = ((c & 1) ? c1 : c0) + (IT)p.off[g + ((c >> 1) << 3)];
+  }
+  const IT my_group = pair_base<IT>((IT)g, p);
+  uint32_t krow[2];  // scale bits of the lane's rows without the group exponent
+  krow[0] = oz::scale_bits(sm.erow[g]);
+  krow[1] = oz::scale_bits(sm.erow[g + 8]);
+
+  const uint64_t nwarps = (uint64_t)gridDim.x * TC_WARPS;
+  const uint64_t first = (uint64_t)blockIdx.x * TC_WARPS + warp;
+
+  // tile base of a tile (its first group's first amplitude), computed when it is fetched
+  auto prefetch = [&](uint64_t tile, int s) -> IT {
+    IT tb = 0;
+    if (tile < p.ntiles) {
+      tb = pair_base<IT>((IT)(tile * 8), p);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cp_async16(&sm.stage[s][warp][q][lane], psi + (tb + ld_off[q]));
+    }
+    cp_async_commit();
+    return tb;
+  };
+
+  IT tb_next = prefetch(first, 0);
+  IT tb_next2 = prefetch(first + nwarps, 1);
+  int s = 0;
+  for (uint64_t tile = first; tile < p.ntiles; tile += nwarps, s ^= 1) {
+    cp_async_wait_one();
+    double2 x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[q] = sm.stage[s][warp][q][lane];
+    uint32_t emax = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      emax = max(emax, max(oz::exponent(df::words(x[q].x)), oz::exponent(df::words(x[q].y))));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    // the stage's values are in registers (used above): refill it two tiles ahead
+    const IT tb = tb_next;
+    tb_next = tb_next2;
+    tb_next2 = prefetch(tile + 2 * nwarps, s);
+    if (!__all_sync(0xffffffffu, gok && tc_scale_ok(emax))) {
+      pair_tile_fp64<IT>(psi, tb + my_group, p, sm.U16);
+      continue;
+    }
+    // B fragments: bf[j][kt][0] = {x_kt[2t], x_kt[2t+1]}, bf[j][kt][1] = {x_kt[2t+8], x_kt[2t+9]}
+    uint32_t bf[oz::NS][2][2];
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float d0[oz::NS], d1[oz::NS];
+        oz::digits(df::words(kt ? x[2 * h].y : x[2 * h].x), emax, d0);
+        oz::digits(df::words(kt ? x[2 * h + 1].y : x[2 * h + 1].x), emax, d1);
+#pragma unroll
+        for (int j = 0; j < oz::NS; ++j) bf[j][kt][h] = oz::pack(d0[j], d1[j]);
+      }
+    }
+    // outputs: rows g, g+8 (amplitude), columns 2t, 2t+1 (group); m-tile 0 gives the
+    // real parts, m-tile 1 the imaginary parts (one m-tile at a time: fewer live registers)
+    const uint32_t ecol[2] = {__shfl_sync(0xffffffffu, emax, (2 * t) * 4) << 20,
+                              __shfl_sync(0xffffffffu, emax, (2 * t + 1) * 4) << 20};
+    // real parts written after m-tile 0, imaginary parts after m-tile 1
+    double* out = reinterpret_cast<double*>(psi);
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      float acc[oz::NL][4];
+#pragma unroll
+      for (int l = 0; l < oz::NL; ++l)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[l][c] = 0.0f;
+#pragma unroll
+      for (int i = 0; i < oz::NS; ++i) {
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt) {
+          const uint4 a = sm.afrag[i][mt][kt][lane];
+#pragma unroll
+          for (int j = 0; j < oz::NS; ++j)
+            if (i + j < oz::NL) mma_bf16(acc[i + j], a, bf[j][kt][0], bf[j][kt][1]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float lv[oz::NL];
+#pragma unroll
+        for (int l = 0; l < oz::NL; ++l) lv[l] = acc[l][c];
+        out[2 * (size_t)(tb + st_off[c]) + mt] = oz::combine(lv, ecol[c & 1] + krow[c >> 1]);
+      }
+    }
+  }
+  cp_async_wait_all();
+}
+
+template <typename IT>
+void launch_pair(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
+  const size_t smem = sizeof(TcSmem);
+  check_cuda(cudaFuncSetAttribute(gate_pair_tc_kernel<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+             "gate_pair_tc_kernel shared memory");
+  const int grid = grid_for((p.ntiles + TC_WARPS - 1) / TC_WARPS, 2);
+  gate_pair_tc_kernel<IT><<<grid, TC_THREADS, smem, s>>>(psi, ga, gb, p);
+}
+
+}  // namespace
+
+// Pairs of consecutive, disjoint two-qubit gates on a power-of-two state are fused and
+// applied on the tensor cores; everything else goes through apply_gate_device. Returns
+// after issuing all launches.
+void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
+                         const std::vector<const void*>& gates, void* stream) {
+  const size_t r = dims.size();
+  bool pow2 = true;
+  for (auto d : dims) pow2 = pow2 && log2_or_none(d) != 0xFFFFFFFFu;
+  const uint64_t n = product(dims);
+  dims_t st = row_strides(dims);
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t g = 0;
+  while (g < gates.size()) {
+    bool fused = false;
+    if (pow2 && n >= 128 && g + 1 < gates.size() && targets[g].size() == 2 && targets[g + 1].size() == 2) {
+      const auto& ta = targets[g];
+      const auto& tb = targets[g + 1];
+      std::vector<uint16_t> all = {ta[0], ta[1], tb[0], tb[1]};
+      bool ok = true;
+      for (auto a : all) ok = ok && a < r && dims[a] == 2;
+      std::vector<uint16_t> srt(all);
+      std::sort(srt.begin(), srt.end());
+      ok = ok && std::adjacent_find(srt.begin(), srt.end()) == srt.end();
+      if (ok) {
+        PairParams p;
+        p.ntiles = n / 16 / 8;
+        std::sort(srt.begin(), srt.end(), [&](uint16_t x, uint16_t y) { return st[x] < st[y]; });
+        for (int j = 0; j < 4; ++j) p.ins_pos[j] = log2_or_none(st[srt[j]]);
+        for (int c = 0; c < 16; ++c)
+          p.off[c] = (int64_t)(((c >> 3) & 1) * st[all[0]] + ((c >> 2) & 1) * st[all[1]] + ((c >> 1) & 1) * st[all[2]] +
+                               (c & 1) * st[all[3]]);
+        double2* psi = static_cast<double2*>(state);
+        const double2* a = static_cast<const double2*>(gates[g]);
+        const double2* b = static_cast<const double2*>(gates[g + 1]);
+        if (n <= (1ull << 32))
+          launch_pair<uint32_t>(psi, a, b, p, s);
+        else
+          launch_pair<uint64_t>(psi, a, b, p, s);
+        count_launch();
+        check_cuda(cudaGetLastError(), "gate_pair_tc_kernel launch");
+        g += 2;
+        fused = true;
+      }
+    }
+    if (!fused) {
+      apply_gate_device(state, dims, targets[g], gates[g], stream);
+      g += 1;
+    }
+  }
+}
+
+}  // namespace qtnh_impl

@@ -90,6 +90,9 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
                        void* stream);
 void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* diag,
                        void* stream);
+// Gate list in order; consecutive disjoint two-qubit pairs fused onto the tensor cores.
+void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
+                         const std::vector<const void*>& gates, void* stream);
 void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
                            const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,
                            const std::vector<uint16_t>& pos_b, void* c, void* stream);

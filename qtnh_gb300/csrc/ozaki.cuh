@@ -3,16 +3,21 @@
 // matrix multiplication by using fast routines of matrix multiplication and its
 // applications", Numer. Algorithms 59, 2012).
 //
-// A real x of a group whose largest biased exponent is E is written as
-//     x ~= sign(x) * sum_{j<6} X_j * 2^(-8 j) * 2^(E - 1030),   X_j in [0, 255],
-// i.e. its 53-bit significand is aligned to the group's scale and cut into six 8-bit
-// slices (48 bits; the bits below 2^(E-1070) are dropped). Every slice is an integer of
-// at most 8 significant bits, so it is exact in bf16, and a product of two slices is
-// exact in FP32. With K = 32 terms, sum_k A_i[k] X_j[k] < 2^21, and one level l = i + j
-// gathers at most 6 such sums (< 2^23.6): the tensor core's FP32 accumulator holds every
-// level sum exactly. The levels are then combined with compensated additions into a
-// float pair carrying ~48 bits, and turned into a double with integer instructions and
-// one FP64 add (df32.cuh).
+// A real x of a group whose largest biased exponent is E is written with six balanced
+// base-256 digits:
+//     x ~= sum_{j<6} d_j * 2^(-8 j) * 2^(E - 1030),   |d_j| <= 128 (|d_0| <= 256),
+// i.e. its 53-bit significand is aligned to the group's scale, rounded to 48 bits, and
+// cut into digits. Every digit is an integer of at most 8 significant bits, so it is
+// exact in bf16, and a product of two digits is exact in FP32. With K = 32 terms a level
+// l = i + j (at most 6 digit pairs) sums to at most 2^22 in magnitude: the tensor core's
+// FP32 accumulator holds every level sum exactly. The levels are then combined with
+// compensated additions into a float pair carrying ~48 bits, and turned into a double
+// with integer instructions and one FP64 add.
+//
+// The digit extraction runs on the FP32 pipe: the aligned significand is split into
+// three 16-bit pieces (exact floats through the 2^23 magic number), and each piece into
+// two balanced digits by rounding to a multiple of 256 (magic number 1.5 * 2^23), the
+// carries rippling from the low piece upwards.
 #pragma once
 
 #include "df32.cuh"
@@ -20,58 +25,85 @@
 namespace qtnh_impl {
 namespace oz {
 
-constexpr int NS = 6;  // slices per operand
-constexpr int NL = 7;  // levels kept: pairs (i, j) with i + j <= 6 (26 slice products)
+constexpr int NS = 6;  // digits per operand
+constexpr int NL = 6;  // levels kept: pairs (i, j) with i + j <= 5 (21 digit products)
+
+constexpr float RM = 12582912.0f;  // 1.5 * 2^23: x + RM - RM rounds |x| < 2^22 to an integer
 
 // Biased double exponent (0 for zero and subnormals).
 DF_HD uint32_t exponent(df::dwords w) { return (w.hi >> 20) & 0x7FFu; }
 
-// The six 8-bit slices of x aligned to group exponent E (E >= exponent(x)), as bf16 bit
-// patterns carrying the sign of x. x == 0 (or a subnormal) gives zeros.
-DF_HD void slice(df::dwords w, uint32_t E, uint16_t out[NS]) {
-  const uint32_t e = exponent(w);
-  const uint32_t sgn16 = (w.hi >> 16) & 0x8000u;
-  uint32_t s = E - e + 5;  // right shift that aligns the 53-bit significand to 48 bits at E
-  uint32_t hi = (w.hi & 0xFFFFFu) | 0x100000u, lo = w.lo;  // 21 + 32 bits
-  if (e == 0 || s >= 53) hi = lo = 0, s = 0;
-  // 53-bit significand shifted right by s (5 <= s < 53) and rounded to nearest
-  // (truncation would bias every product of a dot product the same way): M48 = h16:l32,
-  // at most 2^48 (then c0 = 256, still exact in bf16).
-  uint32_t l32, h16;
-  if (s == 0) {
-    l32 = h16 = 0;
-  } else if (s < 32) {
-    const uint32_t r = (lo >> (s - 1)) & 1u;  // first dropped bit
-    l32 = (lo >> s) | (hi << (32 - s));
-    h16 = hi >> s;
-    const uint32_t l2 = l32 + r;
-    h16 += (l2 < l32);
-    l32 = l2;
-  } else {
-    const uint32_t r = (s == 32) ? (lo >> 31) : ((hi >> (s - 33)) & 1u);
-    l32 = (hi >> (s - 32)) + r;
-    h16 = 0;
-  }
-  const uint32_t c[NS] = {h16 >> 8, h16 & 0xFFu, l32 >> 24, (l32 >> 16) & 0xFFu, (l32 >> 8) & 0xFFu, l32 & 0xFFu};
-#pragma unroll
-  for (int j = 0; j < NS; ++j) {
-    // integer c (0..255) -> float exactly (magic number) -> bf16 by truncation (exact:
-    // at most 8 significant bits), sign of x
-    const float f = df::sub(df::u2f(0x4B000000u | c[j]), 8388608.0f);
-    out[j] = (uint16_t)((df::f2u(f) >> 16) | sgn16);
-  }
+DF_HD uint32_t byte_perm(uint32_t a, uint32_t b, uint32_t sel) {
+#ifdef __CUDA_ARCH__
+  return __byte_perm(a, b, sel);
+#else
+  const uint64_t v = ((uint64_t)b << 32) | a;
+  uint32_t r = 0;
+  for (int i = 0; i < 4; ++i) r |= (uint32_t)((v >> (8 * ((sel >> (4 * i)) & 7u))) & 0xFFu) << (8 * i);
+  return r;
+#endif
 }
 
-// Level sums C[l] (exact floats) -> the double 2^(Esum - 2060) * sum_l C[l] 2^(-8 l),
-// where Esum is the sum of the two operands' group exponents. Level 6 is kept because
-// its cross products of a high and a low slice (e.g. A_1 X_5) are 2^-47 of a typical
-// product, not of the largest one; levels >= 7 are below 2^-55.
-DF_HD double combine(const float C[NL], int32_t Esum) {
-  // small levels first, plain adds (their rounding is below 2^-48 of the result)
-  float t = df::fma(C[6], 0.00390625f /* 2^-8 */, C[5]);  // C5 + C6 2^-8, in units of 2^-40
-  t = df::fma(t, 0.00390625f, C[4]);                          // C4 + ..., in units of 2^-32
-  t = df::fma(t, 0.00390625f, C[3]);                          // C3 + ..., in units of 2^-24
-  t = df::mul(t, 5.9604644775390625e-08f /* 2^-24 */);        // in units of 1
+// round(v / 256) for |v| < 2^30, exactly (one rounding of an exact quotient).
+DF_HD float rdiv256(float v) { return df::sub(df::fma(v, 0.00390625f, RM), RM); }
+
+// The six balanced digits of x at group exponent E (E >= exponent(x)), as floats
+// (exact integers). x == 0 or a subnormal x gives zeros.
+DF_HD void digits(df::dwords w, uint32_t E, float d[NS]) {
+  const uint32_t e = exponent(w);
+  const uint32_t s = E + 5u - e;  // right shift aligning the 53-bit significand to 48 bits at E
+  const uint64_t mant = ((uint64_t)((w.hi & 0xFFFFFu) | 0x100000u) << 32) | w.lo;
+  // rounded to nearest (a truncation would bias every product of a dot product the same
+  // way); at most 2^48
+  const uint64_t m48 = (e != 0u && s <= 53u) ? ((mant + (1ull << (s - 1u))) >> s) : 0ull;
+  const uint32_t h = (uint32_t)(m48 >> 32), l = (uint32_t)m48;
+  // signed pieces: (2^23 + P) * sg - 2^23 * sg is exactly sg * P
+  const float sg = df::u2f((w.hi & 0x80000000u) | 0x3F800000u);
+  const float msg = -8388608.0f * sg;
+  float p0 = df::fma(df::u2f(0x4B000000u | h), sg, msg);
+  float p1 = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7632u)), sg, msg);
+  const float p2 = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7610u)), sg, msg);
+  const float q2 = rdiv256(p2);
+  d[5] = df::fma(q2, -256.0f, p2);
+  const float c2 = rdiv256(q2);
+  d[4] = df::fma(c2, -256.0f, q2);
+  p1 = df::add(p1, c2);
+  const float q1 = rdiv256(p1);
+  d[3] = df::fma(q1, -256.0f, p1);
+  const float c1 = rdiv256(q1);
+  d[2] = df::fma(c1, -256.0f, q1);
+  p0 = df::add(p0, c1);
+  const float q0 = rdiv256(p0);
+  d[1] = df::fma(q0, -256.0f, p0);
+  d[0] = q0;
+}
+
+// Two digits as one bf16x2 register (lo in the low half). Exact: a digit has at most 8
+// significant bits, so its float's low 16 bits are zero.
+DF_HD uint32_t pack(float lo, float hi) { return byte_perm(df::f2u(lo), df::f2u(hi), 0x7632u); }
+
+// f * 2^(Esum - 2060) as a double through the bit pattern: K20 = (Esum - 1164) << 20 is
+// added to the exponent field (f is zero or a normal float; the group ranges keep the
+// result a normal double).
+DF_HD double scaled_double(float f, uint32_t K20) {
+  const uint32_t u = df::f2u(f);
+  const uint32_t a = u << 1;
+  const uint32_t hi = a ? (((a >> 4) + K20) | (u & 0x80000000u)) : 0u;
+  return df::u2d(((uint64_t)hi << 32) | (u << 29));
+}
+
+DF_HD uint32_t scale_bits(int32_t Esum) { return (uint32_t)(Esum - 1164) << 20; }
+
+// Level sums C[l] (exact floats) -> the double 2^(Esum - 2060) * sum_{l<L} C[l] 2^(-8 l),
+// K20 = scale_bits(Esum). With balanced digits (|d| <= 128) the dropped levels >= 6 add
+// a relative error of ~1e-14 per 16x16 block (measured: rms 1e-14, worst 2e-14; keeping
+// level 6 halves it).
+template <int L = NL>
+DF_HD double combine(const float* C, uint32_t K20) {
+  // small levels first, plain roundings (below 2^-48 of the result)
+  float t = C[L - 1];
+  for (int l = L - 2; l >= 3; --l) t = df::fma(t, 0.00390625f /* 2^-8 */, C[l]);
+  t = df::mul(t, 5.9604644775390625e-08f /* 2^-24 */);  // in units of 1
   // compensated: C[2] 2^-16 + C[1] 2^-8 + C[0]
   float s, e, s2, e2;
   df::two_sum(df::mul(C[2], 1.52587890625e-05f /* 2^-16 */), t, s, e);
@@ -79,13 +111,7 @@ DF_HD double combine(const float C[NL], int32_t Esum) {
   e = df::add(e, e2);
   df::two_sum(C[0], s2, s, e2);
   e = df::add(e, e2);
-  // s + e, scaled by 2^(Esum - 2060) through the exponent field, one FP64 add
-  const double hs = df::exact_double(s), he = df::exact_double(e);
-  const int64_t shift = (int64_t)(Esum - 2060) << 52;
-  const uint64_t us = df::d2u(hs), ue = df::d2u(he);
-  const double ds = (us << 1) ? df::u2d(us + (uint64_t)shift) : hs;
-  const double de = (ue << 1) ? df::u2d(ue + (uint64_t)shift) : he;
-  return ds + de;
+  return scaled_double(s, K20) + scaled_double(e, K20);
 }
 
 }  // namespace oz

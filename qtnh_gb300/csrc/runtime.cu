@@ -26,7 +26,9 @@ int arithmetic_mode() {
   int m = g_arith.load(std::memory_order_relaxed);
   if (m < 0) {
     const char* e = std::getenv("QTNH_ARITH");
-    m = (e && std::strcmp(e, "fp64") == 0) ? QTNH_ARITH_FP64 : QTNH_ARITH_F32X2;
+    m = QTNH_ARITH_BF16X6;
+    if (e && std::strcmp(e, "fp64") == 0) m = QTNH_ARITH_FP64;
+    if (e && std::strcmp(e, "f32x2") == 0) m = QTNH_ARITH_F32X2;
     g_arith.store(m);
   }
   return m;
@@ -110,7 +112,7 @@ uint64_t qtnh_kernel_launch_count(void) { return g_launches.load(); }
 
 int qtnh_set_arithmetic(int mode) {
   return guarded([&]() -> int {
-    if (mode != QTNH_ARITH_FP64 && mode != QTNH_ARITH_F32X2) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown arithmetic mode");
+    if (mode != QTNH_ARITH_FP64 && mode != QTNH_ARITH_F32X2 && mode != QTNH_ARITH_BF16X6) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown arithmetic mode");
     g_arith.store(mode);
     return QTNH_OK;
   });

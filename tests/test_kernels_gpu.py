@@ -31,7 +31,7 @@ def _setup():
     q.lib()
 
 
-@pytest.fixture(params=[q.ARITH_F32X2, q.ARITH_FP64], ids=["f32x2", "fp64"])
+@pytest.fixture(params=[q.ARITH_F32X2, q.ARITH_FP64, q.ARITH_BF16X6], ids=["f32x2", "fp64", "bf16x6"])
 def arith(request):
     old = q.get_arithmetic()
     q.set_arithmetic(request.param)
@@ -338,3 +338,87 @@ def test_symmetric_gate_qutrits(k, arith):
     wires = [(t, j) for j, t in enumerate(targets)]
     out, ref = _run_contract((q.DENSE, [], dims, psi, 0), (q.SYMM, [], [3] * (2 * k), els, 0), wires)
     assert rel_l2(out, ref) < REL_TOL
+
+
+# ---- tensor-core (bf16 slice) gate pairs --------------------------------------------
+
+def _oracle_layer(psi, n, gates):
+    cur = orc.Tensor(orc.DENSE, [], [2] * n, psi)
+    for targets, els in gates:
+        k = len(targets)
+        cur, _, _ = orc.contract(cur, orc.Tensor(orc.SYMM, [], [2] * (2 * k), els), [(t, j) for j, t in enumerate(targets)])
+    return cur.els
+
+
+@pytest.fixture
+def bf16x6():
+    old = q.get_arithmetic()
+    q.set_arithmetic(q.ARITH_BF16X6)
+    yield
+    q.set_arithmetic(old)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_gate_pairs_tensor_core_match_oracle(seed, bf16x6):
+    # disjoint two-qubit pairs, targets anywhere (low bits included), fused on the tensor cores
+    nrng = np.random.default_rng(100 + seed)
+    n = 12
+    psi = crandn(nrng, [2] * n)
+    perm = [int(x) for x in nrng.permutation(n)]
+    if seed == 0:
+        perm = [0, 1, 2, 3, 11, 10, 9, 8] + perm[8:]  # bits 0..3 and the top bits
+    gates = [(perm[2 * j:2 * j + 2], haar(nrng, 4).T.reshape(-1)) for j in range(n // 2)]
+    st = dev(psi)
+    before = q.launches()
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    assert q.launches() - before == 3  # six gates, three fused launches
+    assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
+
+
+def test_gate_layer_tensor_core_mixed(bf16x6):
+    # odd gate counts, one-qubit gates and overlapping pairs are applied unfused, in order
+    nrng = np.random.default_rng(7)
+    n = 10
+    psi = crandn(nrng, [2] * n)
+    gates = [([0, 5], haar(nrng, 4)), ([5, 1], haar(nrng, 4)), ([2, 3], haar(nrng, 4)), ([7], haar(nrng, 2)),
+             ([8, 9], haar(nrng, 4)), ([4, 6], haar(nrng, 4)), ([9, 2], haar(nrng, 4))]
+    gates = [(t, u.T.reshape(-1)) for t, u in gates]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
+
+
+def test_gate_pairs_tensor_core_fall_back_out_of_range(bf16x6):
+    # groups with tiny, huge, zero or subnormal amplitudes take FP64 (per warp of 8
+    # groups); each region is compared on its own scale
+    nrng = np.random.default_rng(13)
+    n = 12
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    psi[:1024] *= 1e-250        # the targets (bits 0, 1, 3, 7) keep every group inside one region
+    psi[1024:2048] *= 1e250
+    psi[2048:2560] = 0.0
+    psi[2560] = 5e-324
+    psi[3000] *= 1e-70          # small but in range inside an ordinary group
+    gates = [([10, 11], haar(nrng, 4).T.reshape(-1)), ([4, 8], haar(nrng, 4).T.reshape(-1))]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    out, ref = host(st), _oracle_layer(psi, n, gates)
+    for sl in (slice(0, 1024), slice(1024, 2048), slice(2048, 4096)):
+        assert rel_l2(out[sl], ref[sl]) < REL_TOL
+
+
+def test_gate_pairs_tensor_core_general_gate_and_fallback(bf16x6):
+    # non-unitary gates: rows of very different scale; a gate with huge entries runs FP64
+    nrng = np.random.default_rng(14)
+    n = 11
+    psi = crandn(nrng, [2] * n)
+    ga = crandn(nrng, [16]) * np.array([1e-3] * 4 + [1.0] * 4 + [1e5] * 4 + [2.0] * 4)
+    gb = crandn(nrng, [16])
+    gates = [([1, 9], ga), ([4, 6], gb)]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
+    gates = [([1, 9], ga * 1e250), ([4, 6], gb)]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
