@@ -94,6 +94,13 @@ int qtnh_free_async(void* ptr, void* stream);
 /* Number of kernels this library has launched since load (all entry points). */
 uint64_t qtnh_kernel_launch_count(void);
 
+/* Device-side error flags of the kernels whose waits are bounded (the tcgen05 gate-pair
+ * kernel: bit 0 = a wait for converted digits expired, bit 1 = a wait for MMA completion
+ * expired, bit 2 = a wait for the other half of a group expired; the kernel then stops
+ * early and its output is incomplete). Synchronizes the device, returns the flags
+ * raised since the previous call and clears them. */
+int qtnh_take_device_errors(uint32_t* flags);
+
 /* Arithmetic of the complex128 gate and diagonal kernels (storage is always complex128).
  * QTNH_ARITH_BF16X6 (default): qtnh_apply_gate_layer fuses consecutive disjoint pairs of
  *   two-qubit gates (all dims 2) into 16x16 unitaries applied on the bf16 tensor cores:

@@ -226,6 +226,13 @@ def apply_diag_layer(state, dims, axes, factors, stream=None):
     return state
 
 
+def take_device_errors():
+    """Device error flags raised since the last call (0: none); synchronizes."""
+    f = ctypes.c_uint32()
+    check(lib().qtnh_take_device_errors(ctypes.byref(f)))
+    return int(f.value)
+
+
 def norm2(x, stream=None):
     _check_c128(x)
     r = ctypes.c_double()

@@ -1,0 +1,100 @@
+// Shared pieces of the fused gate-pair kernels (gate_tc.cu: mma.sync, gate_umma.cu:
+// tcgen05): two disjoint two-qubit gates of a layer act on a group of 16 amplitudes (the
+// four target bits varying) as one 16x16 unitary U16 = Ua (x) Ub, in real form
+// R = [[Re U16, -Im U16], [Im U16, Re U16]] (32 x 32) on the group's 32 reals
+// (real parts k = 0..15, imaginary parts k = 16..31), through bf16 digits (ozaki.cuh).
+#pragma once
+
+#include "cuda_common.cuh"
+#include "ozaki.cuh"
+
+namespace qtnh_impl {
+
+struct PairParams {
+  uint64_t ngroups;     // state size / 16
+  uint32_t ins_pos[4];  // the four target bit positions, ascending
+  int64_t off[16];      // offset of amplitude (a0 a1 b0 b1) of a group from its base
+};
+
+// Index of the first amplitude of group `grp`: zero bits inserted at the target positions.
+template <typename IT>
+__device__ __forceinline__ IT pair_base(IT grp, const PairParams& p) {
+  IT b = grp;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const IT low = b & ((IT(1) << p.ins_pos[j]) - 1);
+    b = ((b >> p.ins_pos[j]) << (p.ins_pos[j] + 1)) | low;
+  }
+  return b;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// A group's (or a gate row's) largest biased exponent must lie in [TC_EMIN, TC_EMAX]
+// (magnitudes 2^-200 .. 2^201) unless it is 0 (zeros and subnormals only); infinities
+// and NaNs (exponent 0x7FF) fail. Then the level sums, scaled by 2^(Esum - 2060) through
+// the exponent field, stay normal doubles.
+constexpr uint32_t TC_EMIN = 823, TC_EMAX = 1224;
+
+// Gate entries: zero or a normal double (no subnormal, infinity or NaN).
+__device__ __forceinline__ bool tc_element_ok(df::dwords w) {
+  const uint32_t e = oz::exponent(w);
+  return e == 0 ? (((w.hi << 1) | w.lo) == 0u) : (e != 0x7FFu);
+}
+
+__device__ __forceinline__ bool tc_scale_ok(uint32_t emax) { return emax == 0 || (emax >= TC_EMIN && emax <= TC_EMAX); }
+
+// U16[o * 16 + i] = Ua[oa][ia] Ub[ob][ib] (o = oa * 4 + ob, i = ia * 4 + ib) from two
+// gates in SymmTensor layout G[in * 4 + out] = U[out][in].
+__device__ __forceinline__ double2 fused_entry(const double2* __restrict__ ga, const double2* __restrict__ gb, int t) {
+  const int o = t >> 4, i = t & 15;
+  return cmul(ga[(i >> 2) * 4 + (o >> 2)], gb[(i & 3) * 4 + (o & 3)]);
+}
+
+// Element (r, k) of the real form R of U16.
+__device__ __forceinline__ double real_form(const double2* U16, int r, int k) {
+  const double2 u = U16[(r & 15) * 16 + (k & 15)];
+  if (r < 16) return k < 16 ? u.x : -u.y;
+  return k < 16 ? u.y : u.x;
+}
+
+// Largest exponent of row o of U16 (shared by rows o and 16 + o of R) and whether the
+// row is usable by the digit path.
+__device__ __forceinline__ uint32_t row_exponent(const double2* U16, int o, bool& ok) {
+  uint32_t e = 0;
+  ok = true;
+#pragma unroll 4
+  for (int i = 0; i < 16; ++i) {
+    const double2 u = U16[o * 16 + i];
+    const df::dwords wr = df::words(u.x), wi = df::words(u.y);
+    ok = ok && tc_element_ok(wr) && tc_element_ok(wi);
+    e = max(e, max(oz::exponent(wr), oz::exponent(wi)));
+  }
+  ok = ok && tc_scale_ok(e);
+  return e;
+}
+
+// The 16 outputs of one group in FP64 (U16 in shared memory).
+__device__ __forceinline__ double2 group_output_fp64(const double2* U16, const double2 (&x)[16], int o) {
+  double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) acc = cfma(U16[o * 16 + i], x[i], acc);
+  return acc;
+}
+
+// Host side: the pair's parameters (targets of gate a, then gate b; all dims 2).
+PairParams make_pair_params(const dims_t& dims, const uint16_t all[4]);
+
+// tcgen05 kernel for states of at least 2048 amplitudes; false if it does not apply.
+bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s);
+
+// Reads and clears the tcgen05 kernel's device error flags (bounded waits that expired).
+uint32_t take_umma_error();
+
+}  // namespace qtnh_impl

@@ -1,5 +1,7 @@
 // Two disjoint two-qubit gates fused into one 16x16 unitary, applied in place on the
-// tensor cores with error-free bf16 digits (ozaki.cuh).
+// tensor cores with error-free bf16 digits (ozaki.cuh) -- the mma.sync kernel, used for
+// states below 2048 amplitudes (gate_umma.cu holds the tcgen05 kernel for the rest; the
+// two run at the same speed on large states and give identical results).
 //
 // A gate layer holds disjoint gates, which commute, so consecutive pairs of a
 // qtnh_apply_gate_layer call fuse into U = U_a (x) U_b acting on the 16 amplitudes of a
@@ -24,8 +26,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "cuda_common.cuh"
-#include "ozaki.cuh"
+#include "gate_pair.cuh"
 
 namespace qtnh_impl {
 
@@ -34,12 +35,6 @@ namespace {
 constexpr int TC_THREADS = 256;
 constexpr int TC_WARPS = TC_THREADS / 32;
 constexpr int TC_STAGES = 2;
-
-struct PairParams {
-  uint64_t ntiles;      // groups / 8
-  uint32_t ins_pos[4];  // the four target bit positions, ascending
-  int64_t off[16];      // offset of amplitude (a0 a1 b0 b1) of a group
-};
 
 // Shared memory of one CTA (dynamic, 16-byte aligned).
 struct TcSmem {
@@ -50,46 +45,12 @@ struct TcSmem {
   int gate_ok;
 };
 
-// Index of the first amplitude of group `grp`: zero bits inserted at the target positions.
-template <typename IT>
-__device__ __forceinline__ IT pair_base(IT grp, const PairParams& p) {
-  IT b = grp;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const IT low = b & ((IT(1) << p.ins_pos[j]) - 1);
-    b = ((b >> p.ins_pos[j]) << (p.ins_pos[j] + 1)) | low;
-  }
-  return b;
-}
-
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint4& a, uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
 }
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// A group's (or a gate row's) largest biased exponent must lie in [TC_EMIN, TC_EMAX]
-// (magnitudes 2^-200 .. 2^201) unless it is 0 (zeros and subnormals only); infinities
-// and NaNs (exponent 0x7FF) fail. Then the level sums, scaled by 2^(Esum - 2060) through
-// the exponent field, stay normal doubles.
-constexpr uint32_t TC_EMIN = 823, TC_EMAX = 1224;
-
-// Gate entries: zero or a normal double (no subnormal, infinity or NaN).
-__device__ __forceinline__ bool tc_element_ok(df::dwords w) {
-  const uint32_t e = oz::exponent(w);
-  return e == 0 ? (((w.hi << 1) | w.lo) == 0u) : (e != 0x7FFu);
-}
-
-__device__ __forceinline__ bool tc_scale_ok(uint32_t emax) { return emax == 0 || (emax >= TC_EMIN && emax <= TC_EMAX); }
 
 // FP64 path for one warp's eight groups (all loads before the first store); gbase is
 // the lane's group base.
@@ -111,13 +72,6 @@ __device__ __noinline__ void pair_tile_fp64(double2* __restrict__ psi, IT gbase,
   }
 }
 
-// Element (r, k) of the real form R of U16.
-__device__ __forceinline__ double real_form(const double2* U16, int r, int k) {
-  const double2 u = U16[(r & 15) * 16 + (k & 15)];
-  if (r < 16) return k < 16 ? u.x : -u.y;
-  return k < 16 ? u.y : u.x;
-}
-
 // Two CTAs per SM: up to 128 registers a thread, none spilled (three CTAs spill and run
 // slower).
 template <typename IT>
@@ -131,30 +85,19 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __
 
   // ---- the fused gate: U16, row exponents, A fragments of its six digits ----
   if (tid == 0) sm.gate_ok = 1;
-  for (int t = tid; t < 256; t += TC_THREADS) {
-    const int o = t >> 4, i = t & 15;
-    // SymmTensor layout G[in * 4 + out] = U[out][in]; U16[o][i] = Ua[oa][ia] Ub[ob][ib]
-    sm.U16[t] = cmul(ga[(i >> 2) * 4 + (o >> 2)], gb[(i & 3) * 4 + (o & 3)]);
-  }
+  for (int t = tid; t < 256; t += TC_THREADS) sm.U16[t] = fused_entry(ga, gb, t);
   __syncthreads();
   if (tid < 16) {
-    uint32_t e = 0;
-    bool ok = true;
-    for (int i = 0; i < 16; ++i) {
-      const double2 u = sm.U16[tid * 16 + i];
-      const df::dwords wr = df::words(u.x), wi = df::words(u.y);
-      ok = ok && tc_element_ok(wr) && tc_element_ok(wi);
-      e = max(e, max(oz::exponent(wr), oz::exponent(wi)));
-    }
-    sm.erow[tid] = (int32_t)e;
-    if (!ok || !tc_scale_ok(e)) sm.gate_ok = 0;
+    bool ok;
+    sm.erow[tid] = (int32_t)row_exponent(sm.U16, tid, ok);
+    if (!ok) sm.gate_ok = 0;
   }
   __syncthreads();
   // entries (r, k), (r, k + 1) of digit i form half 0 / 1 of register
   // (r % 16) / 8 + 2 ((k % 16) / 8) of lane (r % 8) * 4 + (k % 8) / 2 in afrag[i][r / 16][k / 16]
   for (int t = tid; t < 512; t += TC_THREADS) {
     const int r = t >> 4, k = (t & 15) * 2;
-    const uint32_t E = (uint32_t)sm.erow[r & 15];
+    const uint32_t E = oz::digit_scale((uint32_t)sm.erow[r & 15]);
     float d0[oz::NS], d1[oz::NS];
     oz::digits(df::words(real_form(sm.U16, r, k)), E, d0);
     oz::digits(df::words(real_form(sm.U16, r, k + 1)), E, d1);
@@ -190,11 +133,12 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __
 
   const uint64_t nwarps = (uint64_t)gridDim.x * TC_WARPS;
   const uint64_t first = (uint64_t)blockIdx.x * TC_WARPS + warp;
+  const uint64_t ntiles = p.ngroups / 8;
 
   // tile base of a tile (its first group's first amplitude), computed when it is fetched
   auto prefetch = [&](uint64_t tile, int s) -> IT {
     IT tb = 0;
-    if (tile < p.ntiles) {
+    if (tile < ntiles) {
       tb = pair_base<IT>((IT)(tile * 8), p);
 #pragma unroll
       for (int q = 0; q < 4; ++q) cp_async16(&sm.stage[s][warp][q][lane], psi + (tb + ld_off[q]));
@@ -206,17 +150,18 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __
   IT tb_next = prefetch(first, 0);
   IT tb_next2 = prefetch(first + nwarps, 1);
   int s = 0;
-  for (uint64_t tile = first; tile < p.ntiles; tile += nwarps, s ^= 1) {
+  for (uint64_t tile = first; tile < ntiles; tile += nwarps, s ^= 1) {
     cp_async_wait_one();
     double2 x[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) x[q] = sm.stage[s][warp][q][lane];
-    uint32_t emax = 0;
+    uint32_t key = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-      emax = max(emax, max(oz::exponent(df::words(x[q].x)), oz::exponent(df::words(x[q].y))));
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+      key = max(key, max(oz::group_key(df::words(x[q].x)), oz::group_key(df::words(x[q].y))));
+    key = max(key, __shfl_xor_sync(0xffffffffu, key, 1));
+    key = max(key, __shfl_xor_sync(0xffffffffu, key, 2));
+    const uint32_t emax = oz::key_exponent(key), escale = oz::digit_scale(emax);
     // the stage's values are in registers (used above): refill it two tiles ahead
     const IT tb = tb_next;
     tb_next = tb_next2;
@@ -232,8 +177,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         float d0[oz::NS], d1[oz::NS];
-        oz::digits(df::words(kt ? x[2 * h].y : x[2 * h].x), emax, d0);
-        oz::digits(df::words(kt ? x[2 * h + 1].y : x[2 * h + 1].x), emax, d1);
+        oz::digits(df::words(kt ? x[2 * h].y : x[2 * h].x), escale, d0);
+        oz::digits(df::words(kt ? x[2 * h + 1].y : x[2 * h + 1].x), escale, d1);
 #pragma unroll
         for (int j = 0; j < oz::NS; ++j) bf[j][kt][h] = oz::pack(d0[j], d1[j]);
       }
@@ -278,11 +223,24 @@ void launch_pair(double2* psi, const double2* ga, const double2* gb, const PairP
   const size_t smem = sizeof(TcSmem);
   check_cuda(cudaFuncSetAttribute(gate_pair_tc_kernel<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
              "gate_pair_tc_kernel shared memory");
-  const int grid = grid_for((p.ntiles + TC_WARPS - 1) / TC_WARPS, 2);
+  const int grid = grid_for(((p.ngroups / 8) + TC_WARPS - 1) / TC_WARPS, 2);
   gate_pair_tc_kernel<IT><<<grid, TC_THREADS, smem, s>>>(psi, ga, gb, p);
 }
 
 }  // namespace
+
+PairParams make_pair_params(const dims_t& dims, const uint16_t all[4]) {
+  const dims_t st = row_strides(dims);
+  PairParams p;
+  p.ngroups = product(dims) / 16;
+  uint16_t srt[4] = {all[0], all[1], all[2], all[3]};
+  std::sort(srt, srt + 4, [&](uint16_t x, uint16_t y) { return st[x] < st[y]; });
+  for (int j = 0; j < 4; ++j) p.ins_pos[j] = log2_or_none(st[srt[j]]);
+  for (int c = 0; c < 16; ++c)
+    p.off[c] = (int64_t)(((c >> 3) & 1) * st[all[0]] + ((c >> 2) & 1) * st[all[1]] + ((c >> 1) & 1) * st[all[2]] +
+                         (c & 1) * st[all[3]]);
+  return p;
+}
 
 // Pairs of consecutive, disjoint two-qubit gates on a power-of-two state are fused and
 // applied on the tensor cores; everything else goes through apply_gate_device. Returns
@@ -293,7 +251,6 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
   bool pow2 = true;
   for (auto d : dims) pow2 = pow2 && log2_or_none(d) != 0xFFFFFFFFu;
   const uint64_t n = product(dims);
-  dims_t st = row_strides(dims);
   cudaStream_t s = (cudaStream_t)stream;
   size_t g = 0;
   while (g < gates.size()) {
@@ -308,22 +265,20 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
       std::sort(srt.begin(), srt.end());
       ok = ok && std::adjacent_find(srt.begin(), srt.end()) == srt.end();
       if (ok) {
-        PairParams p;
-        p.ntiles = n / 16 / 8;
-        std::sort(srt.begin(), srt.end(), [&](uint16_t x, uint16_t y) { return st[x] < st[y]; });
-        for (int j = 0; j < 4; ++j) p.ins_pos[j] = log2_or_none(st[srt[j]]);
-        for (int c = 0; c < 16; ++c)
-          p.off[c] = (int64_t)(((c >> 3) & 1) * st[all[0]] + ((c >> 2) & 1) * st[all[1]] + ((c >> 1) & 1) * st[all[2]] +
-                               (c & 1) * st[all[3]]);
+        const uint16_t tg[4] = {ta[0], ta[1], tb[0], tb[1]};
+        const PairParams p = make_pair_params(dims, tg);
         double2* psi = static_cast<double2*>(state);
         const double2* a = static_cast<const double2*>(gates[g]);
         const double2* b = static_cast<const double2*>(gates[g + 1]);
-        if (n <= (1ull << 32))
-          launch_pair<uint32_t>(psi, a, b, p, s);
-        else
-          launch_pair<uint64_t>(psi, a, b, p, s);
+        // tcgen05 kernel from one 128-group tile up, mma.sync kernel below
+        if (!launch_pair_umma(psi, a, b, p, s)) {
+          if (n <= (1ull << 32))
+            launch_pair<uint32_t>(psi, a, b, p, s);
+          else
+            launch_pair<uint64_t>(psi, a, b, p, s);
+        }
         count_launch();
-        check_cuda(cudaGetLastError(), "gate_pair_tc_kernel launch");
+        check_cuda(cudaGetLastError(), "gate pair kernel launch");
         g += 2;
         fused = true;
       }

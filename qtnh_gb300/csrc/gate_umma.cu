@@ -1,0 +1,381 @@
+// Fused gate pairs on the 5th-generation tensor cores (tcgen05): the same error-free bf16
+// digit scheme as gate_tc.cu, with the MMA issued by one thread into tensor memory.
+//
+// A tile is 128 groups (16 amplitudes each). Per tile, D_l[g][o] = sum over digit pairs
+// (i, j), i + j = l, of X_j[g][k] * R_i[o][k] (M = 128 groups, N = 32 output reals, K = 32
+// input reals) -- 21 digit pairs x 2 K-steps = 42 tcgen05.mma (kind::f16, bf16 operands,
+// FP32 accumulators) into six level column blocks of TMEM.
+//
+// CTA = two teams of eight warps + one MMA warp, one CTA per SM (persistent):
+//   * team t handles every other tile of the CTA; group r of its tile belongs to two
+//     threads (warp quarter q = r / 32 of the team's first and second four warps), each
+//     owning 8 of the group's 16 amplitudes: it fetches them one tile ahead with
+//     cp.async, the two exchange their largest exponents through shared memory (an
+//     mbarrier), and each writes its 6 x 16 digits into shared memory in the UMMA
+//     K-major core-matrix layout (8 rows x 16 bytes) and arrives on full[t];
+//   * the MMA warp waits on full[t], issues the 42 MMAs into team t's TMEM columns and
+//     commits them to done[t];
+//   * team t waits on done[t], and each thread reads the level sums of its 8 amplitudes
+//     from its TMEM lane with tcgen05.ld, recombines and stores them.
+// While one team converts, the other's MMAs run. Every wait is bounded by a clock limit;
+// on expiry the CTA records an error flag, stops and frees its tensor memory.
+//
+// Groups with an infinity/NaN or a largest magnitude outside 2^-200..2^201, and all
+// groups when the gate has such entries, are computed in FP64 by their two threads.
+
+#include <algorithm>
+
+#include "gate_pair.cuh"
+
+namespace qtnh_impl {
+
+// bit 0: a wait for digits expired, bit 1: a wait for MMA completion expired, bit 2: a
+// wait for the partner half's exponent expired
+__device__ unsigned int g_umma_error;
+
+namespace {
+
+constexpr int UM_WG = 2;                 // teams, one tile in flight each
+constexpr int UM_TEAM = 256;             // threads of a team (two per group)
+constexpr int UM_THREADS = UM_WG * UM_TEAM + 32;
+constexpr int UM_M = 128;                // groups per tile (MMA M)
+constexpr int UM_N = 32;                 // output reals per group (MMA N)
+constexpr int UM_COLS = 256;             // TMEM column stride of a team (its level sums use 32 * NL)
+constexpr uint32_t UM_TMEM_COLS = 512;   // allocation (power of two >= UM_WG * UM_COLS)
+static_assert(oz::NL * UM_N <= UM_COLS, "level sums exceed a team's TMEM columns");
+constexpr long long UM_WAIT_CYCLES = 1ll << 31;  // ~1 s at 2 GHz
+
+// Shared memory of one CTA (dynamic). Operand layout (K-major, no swizzle): an 8-row x
+// 16-byte core matrix is 128 contiguous bytes (row at 16 * row); for one K-step of 16,
+// core (row group rg, K half kh) sits at rg * 256 + kh * 128: LBO = 128, SBO = 256.
+struct UmSmem {
+  uint8_t adig[UM_WG][oz::NS][2][UM_M * 32];  // state digits: team, digit, K-step (4 KB each)
+  uint8_t bdig[oz::NS][2][UM_N * 32];         // gate digits: digit, K-step (1 KB each)
+  double2 stage[UM_WG][16][UM_M];             // fetched amplitudes: team, amplitude, group
+  uint32_t key[UM_WG][2][UM_M];               // largest exponent key of each half group
+  double2 U16[256];                           // fused unitary, U16[o * 16 + i]
+  int32_t erow[16];                           // largest exponent of row o of U16
+  uint32_t krow[16];                          // oz::scale_bits(erow[o])
+  uint64_t keyx[UM_WG];                       // both halves' keys (and fetched amplitudes) are visible
+  uint64_t full[UM_WG];                       // digits of team t's tile are ready
+  uint64_t done[UM_WG];                       // MMAs of team t's tile are complete
+  uint32_t tmem_base;
+  int gate_ok;
+  int abort;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Warp-uniform bounded wait for the phase of parity `parity`; false on expiry or abort.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  const long long t0 = clock64();
+  while (true) {
+    const bool ok = mbar_try_wait(bar, parity);
+    if (__all_sync(0xffffffffu, ok)) return true;
+    if (__any_sync(0xffffffffu, *abort != 0 || clock64() - t0 > UM_WAIT_CYCLES)) return false;
+  }
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, no swizzle, LBO 128 B (K direction), SBO
+// 256 B (8-row groups), descriptor version 1 (bits 46-47).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(256u >> 4) << 32) |
+         (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12
+// = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(UM_N >> 3) << 17) |
+                              ((uint32_t)(UM_M >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(UM_IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// 4 consecutive 32-bit TMEM columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&v)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// FP64 outputs 8 h .. 8 h + 7 of one group whose 16 amplitudes are in the stage
+// (stride UM_M); the two halves' inputs are all read before either thread writes.
+template <typename IT>
+__device__ __noinline__ void half_group_fp64(double2* __restrict__ psi, IT gbase, const PairParams& p,
+                                             const double2* U16, const double2* stage_r, int h) {
+  double2 x[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) x[c] = stage_r[c * UM_M];
+#pragma unroll 1
+  for (int o = 8 * h; o < 8 * h + 8; ++o) psi[gbase + (IT)p.off[o]] = group_output_fp64(U16, x, o);
+}
+
+template <typename IT>
+__global__ void __launch_bounds__(UM_THREADS, 1) gate_pair_umma_kernel(double2* __restrict__ psi,
+                                                                       const double2* __restrict__ ga,
+                                                                       const double2* __restrict__ gb,
+                                                                       const __grid_constant__ PairParams p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  UmSmem& sm = *reinterpret_cast<UmSmem*>(smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint64_t ntiles = p.ngroups / UM_M;
+
+  // ---- setup: barriers, tensor memory, the fused gate and its digits ----
+  if (tid == 0) {
+    sm.gate_ok = 1;
+    sm.abort = 0;
+    for (int w = 0; w < UM_WG; ++w) {
+      mbar_init(&sm.keyx[w], UM_TEAM);
+      mbar_init(&sm.full[w], UM_TEAM);
+      mbar_init(&sm.done[w], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == UM_WG * 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(UM_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  for (int t = tid; t < 256; t += UM_THREADS) sm.U16[t] = fused_entry(ga, gb, t);
+  __syncthreads();
+  if (tid < 16) {
+    bool ok;
+    const uint32_t e = row_exponent(sm.U16, tid, ok);
+    sm.erow[tid] = (int32_t)e;
+    sm.krow[tid] = oz::scale_bits((int32_t)e);
+    if (!ok) sm.gate_ok = 0;
+  }
+  __syncthreads();
+  if (tid < 128) {  // gate digits: output row o, K core kc (input reals 8 kc .. 8 kc + 7)
+    const int o = tid >> 2, kc = tid & 3;
+    const uint32_t E = oz::digit_scale((uint32_t)sm.erow[o & 15]);
+    float d[8][oz::NS];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) oz::digits(df::words(real_form(sm.U16, o, kc * 8 + e)), E, d[e]);
+#pragma unroll
+    for (int j = 0; j < oz::NS; ++j) {
+      const uint4 v = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]), oz::pack(d[4][j], d[5][j]),
+                                 oz::pack(d[6][j], d[7][j]));
+      *reinterpret_cast<uint4*>(&sm.bdig[j][kc >> 1][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) = v;
+    }
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  const bool gok = sm.gate_ok != 0;
+  auto tile_of = [&](uint64_t m) -> uint64_t { return (uint64_t)blockIdx.x + m * gridDim.x; };
+
+  if (warp < UM_WG * 8) {
+    // ---- team: fetch, digits, (MMA), recombination, store ----
+    const int t = warp >> 3, v = warp & 7, q = v & 3, h = v >> 2;
+    const int r = q * 32 + lane;  // group row of the tile (TMEM lane)
+    const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16);
+    auto fetch = [&](uint64_t T) {
+      if (T < ntiles) {
+        const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
+#pragma unroll
+        for (int c = 8 * h; c < 8 * h + 8; ++c) cp_async16(&sm.stage[t][c][r], psi + (gbase + (IT)p.off[c]));
+      }
+      cp_async_commit();
+    };
+    fetch(tile_of(t));
+    uint32_t it = 0;
+    for (uint64_t m = t; tile_of(m) < ntiles; m += UM_WG, ++it) {
+      const IT gbase = pair_base<IT>((IT)(tile_of(m) * UM_M + r), p);
+      cp_async_wait_all();
+      double2 x[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) x[c] = sm.stage[t][8 * h + c][r];
+      uint32_t key = 0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) key = max(key, max(oz::group_key(df::words(x[c].x)), oz::group_key(df::words(x[c].y))));
+      sm.key[t][h][r] = key;
+      mbar_arrive(&sm.keyx[t]);  // both halves' keys and fetched amplitudes become visible
+      if (!mbar_wait_warp(&sm.keyx[t], it & 1u, &sm.abort)) {
+        atomicOr(&g_umma_error, 4u);
+        sm.abort = 1;
+        break;
+      }
+      key = max(key, sm.key[t][h ^ 1][r]);
+      const uint32_t emax = oz::key_exponent(key), escale = oz::digit_scale(emax);
+      const bool ok = gok && tc_scale_ok(emax);
+      // digits of this thread's 16 reals: K core h (real parts of amplitudes 8h..8h+7)
+      // and K core 2 + h (their imaginary parts)
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        const int kc = 2 * part + h;
+        float d[8][oz::NS];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          if (ok) {
+            oz::digits(df::words(part ? x[e].y : x[e].x), escale, d[e]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < oz::NS; ++j) d[e][j] = 0.0f;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < oz::NS; ++j) {
+          const uint4 vv = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]),
+                                      oz::pack(d[4][j], d[5][j]), oz::pack(d[6][j], d[7][j]));
+          *reinterpret_cast<uint4*>(&sm.adig[t][j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
+        }
+      }
+      if (!ok) half_group_fp64<IT>(psi, gbase, p, sm.U16, &sm.stage[t][0][r], h);
+      fence_proxy_async();
+      mbar_arrive(&sm.full[t]);
+      if (!mbar_wait_warp(&sm.done[t], it & 1u, &sm.abort)) {
+        atomicOr(&g_umma_error, 2u);
+        sm.abort = 1;
+        break;
+      }
+      // every thread of the team has arrived (the MMAs ran): the stage is free
+      fetch(tile_of(m + UM_WG));
+      tc_fence_after();
+      // level sums: TMEM lane r, columns t * UM_COLS + 32 l + o (o < 16: real part of
+      // amplitude o, o >= 16: imaginary part of amplitude o - 16)
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * UM_COLS);
+#pragma unroll
+      for (int c4 = 0; c4 < 2; ++c4) {
+        const int a0 = 8 * h + 4 * c4;
+        uint32_t re[oz::NL][4], im[oz::NL][4];
+#pragma unroll
+        for (int l = 0; l < oz::NL; ++l) {
+          tmem_ld4(tbase + (uint32_t)(32 * l + a0), re[l]);
+          tmem_ld4(tbase + (uint32_t)(32 * l + 16 + a0), im[l]);
+        }
+        tmem_wait_ld();
+        if (ok) {
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const uint32_t K20 = (emax << 20) + sm.krow[a0 + a];
+            float lr[oz::NL], li[oz::NL];
+#pragma unroll
+            for (int l = 0; l < oz::NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
+            psi[gbase + (IT)p.off[a0 + a]] = make_double2(oz::combine(lr, K20), oz::combine(li, K20));
+          }
+        }
+      }
+      tc_fence_before();
+    }
+    cp_async_wait_all();
+  } else {
+    // ---- MMA warp: one elected thread issues each tile's 42 MMAs ----
+    const uint32_t bbase = smem_u32(&sm.bdig[0][0][0]);
+    for (uint64_t m = 0; tile_of(m) < ntiles; ++m) {
+      const int w = (int)(m % UM_WG);
+      const uint32_t it = (uint32_t)(m / UM_WG);
+      if (!mbar_wait_warp(&sm.full[w], it & 1u, &sm.abort)) {
+        atomicOr(&g_umma_error, 1u);
+        sm.abort = 1;
+        break;
+      }
+      tc_fence_after();
+      if (lane == 0) {
+        const uint32_t abase = smem_u32(&sm.adig[w][0][0][0]);
+        const uint32_t dcol = tmem + (uint32_t)(w * UM_COLS);
+#pragma unroll
+        for (int l = 0; l < oz::NL; ++l) {
+          uint32_t acc = 0;
+#pragma unroll
+          for (int i = 0; i < oz::NS; ++i) {
+            const int j = l - i;
+            if (j < 0 || j >= oz::NS) continue;
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+              const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
+              const uint64_t bd = smem_desc(bbase + (uint32_t)((i * 2 + ks) * UM_N * 32));
+              umma_bf16(dcol + (uint32_t)(l * UM_N), ad, bd, acc);
+              acc = 1;
+            }
+          }
+        }
+        umma_commit(&sm.done[w]);
+      }
+      __syncwarp();
+    }
+  }
+
+  // ---- teardown: all tensor-memory reads are done; free it ----
+  tc_fence_before();
+  __syncthreads();
+  if (warp == UM_WG * 8) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+  }
+}
+
+template <typename IT>
+void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
+  const size_t smem = sizeof(UmSmem);
+  check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+             "gate_pair_umma_kernel shared memory");
+  const uint64_t ntiles = p.ngroups / UM_M;
+  const int grid = (int)std::min<uint64_t>(ntiles, (uint64_t)sm_count());
+  gate_pair_umma_kernel<IT><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p);
+}
+
+}  // namespace
+
+bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
+  if (p.ngroups < (uint64_t)UM_M || p.ngroups % UM_M) return false;
+  if (p.ngroups * 16 <= (1ull << 32))
+    launch_umma<uint32_t>(psi, ga, gb, p, s);
+  else
+    launch_umma<uint64_t>(psi, ga, gb, p, s);
+  return true;
+}
+
+uint32_t take_umma_error() {
+  uint32_t v = 0;
+  check_cuda(cudaMemcpyFromSymbol(&v, g_umma_error, sizeof(v)), "read device error flags");
+  const uint32_t zero = 0;
+  check_cuda(cudaMemcpyToSymbol(g_umma_error, &zero, sizeof(zero)), "clear device error flags");
+  return v;
+}
+
+}  // namespace qtnh_impl
+
+using namespace qtnh_impl;
+
+extern "C" int qtnh_take_device_errors(uint32_t* flags) {
+  return guarded([&]() -> int {
+    if (!flags) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null flags pointer");
+    check_cuda(cudaDeviceSynchronize(), "device synchronize");
+    *flags = take_umma_error();
+    return QTNH_OK;
+  });
+}

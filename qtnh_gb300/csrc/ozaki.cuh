@@ -6,18 +6,20 @@
 // A real x of a group whose largest biased exponent is E is written with six balanced
 // base-256 digits:
 //     x ~= sum_{j<6} d_j * 2^(-8 j) * 2^(E - 1030),   |d_j| <= 128 (|d_0| <= 256),
-// i.e. its 53-bit significand is aligned to the group's scale, rounded to 48 bits, and
-// cut into digits. Every digit is an integer of at most 8 significant bits, so it is
-// exact in bf16, and a product of two digits is exact in FP32. With K = 32 terms a level
-// l = i + j (at most 6 digit pairs) sums to at most 2^22 in magnitude: the tensor core's
-// FP32 accumulator holds every level sum exactly. The levels are then combined with
-// compensated additions into a float pair carrying ~48 bits, and turned into a double
-// with integer instructions and one FP64 add.
+// i.e. its 53-bit significand is aligned to the group's scale and rounded to 48 bits
+// (M48 = round(|x| 2^(1070 - E)) <= 2^48), and cut into digits. Every digit is an integer
+// of at most 8 significant bits, so it is exact in bf16, and a product of two digits is
+// exact in FP32. With K = 32 terms a level l = i + j (at most 6 digit pairs) sums to at
+// most 2 * 32 * 256 * 128 + 4 * 32 * 128 * 128 = 2^22 in magnitude: the tensor core's
+// FP32 accumulator holds every level sum exactly. The levels are then combined with compensated additions into a
+// float pair carrying ~48 bits, and turned into a double with integer instructions and
+// one FP64 add.
 //
-// The digit extraction runs on the FP32 pipe: the aligned significand is split into
-// three 16-bit pieces (exact floats through the 2^23 magic number), and each piece into
-// two balanced digits by rounding to a multiple of 256 (magic number 1.5 * 2^23), the
-// carries rippling from the low piece upwards.
+// Digit extraction: M48 + B, B = 0x808080808080, has bytes b_j (b_0 = bits 40..49, up
+// to 384) with M48 = sum (b_j - 128) 256^(5-j) (the carries of the addition do the
+// balancing); b_j - 128 comes out of one byte permute (the byte under the 2^23 magic
+// exponent) and one FMA that also applies the sign. The rounding rides on the same
+// addition: (floor(m / 2^(s-1)) + 2B + 1) >> 1 = round(m / 2^s) + B.
 #pragma once
 
 #include "df32.cuh"
@@ -27,8 +29,6 @@ namespace oz {
 
 constexpr int NS = 6;  // digits per operand
 constexpr int NL = 6;  // levels kept: pairs (i, j) with i + j <= 5 (21 digit products)
-
-constexpr float RM = 12582912.0f;  // 1.5 * 2^23: x + RM - RM rounds |x| < 2^22 to an integer
 
 // Biased double exponent (0 for zero and subnormals).
 DF_HD uint32_t exponent(df::dwords w) { return (w.hi >> 20) & 0x7FFu; }
@@ -44,38 +44,36 @@ DF_HD uint32_t byte_perm(uint32_t a, uint32_t b, uint32_t sel) {
 #endif
 }
 
-// round(v / 256) for |v| < 2^30, exactly (one rounding of an exact quotient).
-DF_HD float rdiv256(float v) { return df::sub(df::fma(v, 0.00390625f, RM), RM); }
+// Largest biased exponent of a set of doubles, from max(hi << 1) (the sign shifted out,
+// the exponent on top): group_key() per element, then key_exponent() of the maximum.
+DF_HD uint32_t group_key(df::dwords w) { return w.hi << 1; }
+DF_HD uint32_t key_exponent(uint32_t key) { return key >> 21; }
 
-// The six balanced digits of x at group exponent E (E >= exponent(x)), as floats
-// (exact integers). x == 0 or a subnormal x gives zeros.
-DF_HD void digits(df::dwords w, uint32_t E, float d[NS]) {
+// Group scale for digits(): E, or (for an all-zero group, E == 0) a scale at which every
+// element's digits are 0.
+DF_HD uint32_t digit_scale(uint32_t E) { return E ? E : 0x7FFu; }
+
+// The six balanced digits of x at group scale Es = digit_scale(E) (E >= exponent(x),
+// Es >= 58), as floats (exact integers, |d_0| <= 256, |d_j| <= 128). Zeros and
+// subnormals give zeros (their alignment shift is clamped to 63 bits).
+DF_HD void digits(df::dwords w, uint32_t Es, float d[NS]) {
   const uint32_t e = exponent(w);
-  const uint32_t s = E + 5u - e;  // right shift aligning the 53-bit significand to 48 bits at E
+  // right shift aligning the 53-bit significand to 48 bits at Es, clamped: zeros and
+  // subnormals (e = 0) and elements below 2^-49 of the group fall to 0
+  uint32_t s = Es + 5u - e;
+  s = s < 63u ? s : 63u;
   const uint64_t mant = ((uint64_t)((w.hi & 0xFFFFFu) | 0x100000u) << 32) | w.lo;
-  // rounded to nearest (a truncation would bias every product of a dot product the same
-  // way); at most 2^48
-  const uint64_t m48 = (e != 0u && s <= 53u) ? ((mant + (1ull << (s - 1u))) >> s) : 0ull;
-  const uint32_t h = (uint32_t)(m48 >> 32), l = (uint32_t)m48;
-  // signed pieces: (2^23 + P) * sg - 2^23 * sg is exactly sg * P
+  const uint64_t mb = ((mant >> (s - 1u)) + 0x1010101010101ull) >> 1;  // M48 + B
+  const uint32_t h = (uint32_t)(mb >> 32), l = (uint32_t)mb;
+  // (2^23 + b) * sg - (2^23 + 128) * sg = sg * (b - 128)
   const float sg = df::u2f((w.hi & 0x80000000u) | 0x3F800000u);
-  const float msg = -8388608.0f * sg;
-  float p0 = df::fma(df::u2f(0x4B000000u | h), sg, msg);
-  float p1 = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7632u)), sg, msg);
-  const float p2 = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7610u)), sg, msg);
-  const float q2 = rdiv256(p2);
-  d[5] = df::fma(q2, -256.0f, p2);
-  const float c2 = rdiv256(q2);
-  d[4] = df::fma(c2, -256.0f, q2);
-  p1 = df::add(p1, c2);
-  const float q1 = rdiv256(p1);
-  d[3] = df::fma(q1, -256.0f, p1);
-  const float c1 = rdiv256(q1);
-  d[2] = df::fma(c1, -256.0f, q1);
-  p0 = df::add(p0, c1);
-  const float q0 = rdiv256(p0);
-  d[1] = df::fma(q0, -256.0f, p0);
-  d[0] = q0;
+  const float off = -8388736.0f * sg;
+  d[0] = df::fma(df::u2f(byte_perm(h, 0x4B000000u, 0x7621u)), sg, off);  // bits 40..49
+  d[1] = df::fma(df::u2f(byte_perm(h, 0x4B000000u, 0x7650u)), sg, off);
+  d[2] = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7653u)), sg, off);
+  d[3] = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7652u)), sg, off);
+  d[4] = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7651u)), sg, off);
+  d[5] = df::fma(df::u2f(byte_perm(l, 0x4B000000u, 0x7650u)), sg, off);
 }
 
 // Two digits as one bf16x2 register (lo in the low half). Exact: a digit has at most 8

@@ -47,9 +47,10 @@ static void real_form(const cd* U, double R[32][32]) {
     }
 }
 
-// digits of v at exponent E, checked: packing exact, reconstruction within half a unit
+// digits of v at group exponent E, checked: packing exact, digits in range,
+// reconstruction within half a unit of 2^(E - 1070)
 static void checked_digits(double v, uint32_t E, float d[oz::NS]) {
-  oz::digits(df::words(v), E, d);
+  oz::digits(df::words(v), oz::digit_scale(E), d);
   ld rec = 0;
   for (int j = 0; j < oz::NS; ++j) {
     const uint32_t p = oz::pack(d[j], -d[j]);
@@ -59,7 +60,10 @@ static void checked_digits(double v, uint32_t E, float d[oz::NS]) {
     }
     rec += std::ldexp((ld)d[j], 40 - 8 * j);
   }
-  if (oz::exponent(df::words(v)) == 0) return;
+  if (oz::exponent(df::words(v)) == 0) {
+    if (rec != 0) std::printf("zero/subnormal %a gives nonzero digits\n", v), ++fails;
+    return;
+  }
   const ld want = std::ldexp((ld)v, 1070 - (int)E);  // v in units of 2^(E - 1070)
   if (std::fabs(rec - want) > 0.5L + 1e-9L) {
     std::printf("digits of %a do not reconstruct it: %Lg vs %Lg\n", v, rec, want);
@@ -73,8 +77,9 @@ static float max_level = 0;
 // (per k-tile of 16, per digit pair), recombined with L levels
 template <int L>
 static void apply(const double R[32][32], const double X[32], double out[32]) {
-  uint32_t Ex = 0, Er[32] = {0};
-  for (int k = 0; k < 32; ++k) Ex = std::max(Ex, oz::exponent(df::words(X[k])));
+  uint32_t key = 0, Ex, Er[32] = {0};
+  for (int k = 0; k < 32; ++k) key = std::max(key, oz::group_key(df::words(X[k])));
+  Ex = oz::key_exponent(key);
   for (int r = 0; r < 32; ++r)
     for (int k = 0; k < 32; ++k) Er[r] = std::max(Er[r], oz::exponent(df::words(R[r][k])));
   static float B[32][oz::NS], A[32][32][oz::NS];
@@ -171,6 +176,15 @@ int main() {
   float d[oz::NS];
   for (double v : edge) checked_digits(v, oz::exponent(df::words(1.0)), d);
   checked_digits(1.0 - std::ldexp(1.0, -53), oz::exponent(df::words(0.75)), d);
+  checked_digits(0.0, 0, d);                      // all-zero group (E = 0)
+  checked_digits(4.9e-324, oz::exponent(df::words(1e-50)), d);  // subnormal in a group of the digit path
+  for (int k = 0; k < 200000; ++k) {              // random values and group scales
+    std::mt19937_64 r2(k);
+    const double v = std::ldexp(std::uniform_real_distribution<double>(-1, 1)(r2), (int)(r2() % 120) - 60);
+    const uint32_t e = oz::exponent(df::words(v));
+    checked_digits(v, e + (uint32_t)(r2() % 60), d);
+    checked_digits(v, e + 40 + (uint32_t)(r2() % 30), d);  // elements near or below 2^-48 of the group
+  }
   accuracy<oz::NL>("kernel's levels", 5e-14, 2e-14, 2e-12);
   accuracy<7>("7 levels (information)", 1.0, 1.0, 1.0);
   std::printf("largest level sum %.0f (< 2^24)\n", max_level);

@@ -354,8 +354,10 @@ def _oracle_layer(psi, n, gates):
 def bf16x6():
     old = q.get_arithmetic()
     q.set_arithmetic(q.ARITH_BF16X6)
+    q.take_device_errors()
     yield
     q.set_arithmetic(old)
+    assert q.take_device_errors() == 0  # no bounded wait of the tcgen05 kernel expired
 
 
 @pytest.mark.parametrize("seed", range(6))
@@ -372,6 +374,19 @@ def test_gate_pairs_tensor_core_match_oracle(seed, bf16x6):
     before = q.launches()
     q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
     assert q.launches() - before == 3  # six gates, three fused launches
+    assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
+
+
+@pytest.mark.parametrize("n", [8, 10, 18])
+def test_gate_pairs_tensor_core_sizes(n, bf16x6):
+    # n < 11: the mma.sync kernel (fewer than one 128-group tile); n = 18: the tcgen05
+    # kernel with several tiles per CTA, both warpgroups and barrier phases in use
+    nrng = np.random.default_rng(200 + n)
+    psi = crandn(nrng, [2] * n)
+    perm = [int(x) for x in nrng.permutation(n)]
+    gates = [(perm[2 * j:2 * j + 2], haar(nrng, 4).T.reshape(-1)) for j in range(4)]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
     assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
 
 
