@@ -488,7 +488,9 @@ static std::vector<qtnh::uint> qft(QTNHEnv& env, TensorNetwork& tn, qtnh::uint n
 }
 
 static void test_qft(QTNHEnv& env) {
-  const std::vector<std::pair<int, int>> cases = {{2, 0}, {3, 0}, {4, 0}, {5, 0}, {5, 2}, {6, 2}, {7, 3}, {8, 3}};
+  // up to the 16-qubit QFT of the reference's example, on 1 and 2 (dq = 1) "ranks"
+  const std::vector<std::pair<int, int>> cases = {{2, 0}, {3, 0}, {4, 0}, {5, 0}, {5, 2}, {6, 2},
+                                                  {7, 3}, {8, 3}, {16, 0}, {16, 1}};
   for (auto [nq, dq] : cases) {
     g_case = "qft-" + std::to_string(nq) + "-" + std::to_string(dq);
     TensorNetwork tn;
@@ -496,6 +498,7 @@ static void test_qft(QTNHEnv& env) {
     auto tp = tn.extract(tn.contractAll(order));
     REQUIRE(tp->totDims().size() == (std::size_t)nq);
     REQUIRE(utils::equal(tp->at(utils::i_to_idxs(0, tp->totDims())), 1.0, 1E-4));
+    REQUIRE(std::abs(tp->at(utils::i_to_idxs(0, tp->totDims())) - 1.0) < 1e-12);
     double rest = 0;
     for (std::size_t i = 1; i < tp->totSize(); ++i) rest += std::norm(tp->at(utils::i_to_idxs(i, tp->totDims())));
     REQUIRE(rest < 1e-20);
