@@ -291,7 +291,7 @@ def main():
     # gate-pair kernel, one launch per pair of gates)
     gate_ms = [s.elapsed_time(e) for s, e in events.get("gates", [])]
     gates_per_call = (a.n // 2 + 1) // 2 if a.arith == "bf16x6" else a.n // 2
-    kernel = {"f32x2": "gate_kernel_f32x2<4>", "fp64": "gate_kernel<4>", "bf16x6": "gate_pair_tc_kernel"}[a.arith]
+    kernel = {"f32x2": "gate_kernel_f32x2<4>", "fp64": "gate_kernel<4>", "bf16x6": "gate_pair_umma_kernel"}[a.arith]
     gate_launch_ms = (sum(gate_ms) / len(gate_ms)) / gates_per_call if gate_ms else None
     alg_bytes = 32.0 * N
     peak, peak_kind = _peaks()
