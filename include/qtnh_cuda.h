@@ -96,9 +96,10 @@ uint64_t qtnh_kernel_launch_count(void);
 
 /* Device-side error flags of the kernels whose waits are bounded (the tcgen05 gate-pair
  * kernel: bit 0 = a wait for converted digits expired, bit 1 = a wait for MMA completion
- * expired, bit 2 = a wait for the other half of a group expired; the kernel then stops
- * early and its output is incomplete). Synchronizes the device, returns the flags
- * raised since the previous call and clears them. */
+ * expired, bit 2 = a wait for the other half of a group expired; the tcgen05 GEMM:
+ * bits 8-10 = a producer / MMA / epilogue wait expired; the kernel then stops early and
+ * its output is incomplete). Synchronizes the device, returns the flags raised since the
+ * previous call and clears them. */
 int qtnh_take_device_errors(uint32_t* flags);
 
 /* Arithmetic of the complex128 gate and diagonal kernels (storage is always complex128).
@@ -118,6 +119,19 @@ int qtnh_take_device_errors(uint32_t* flags);
 enum { QTNH_ARITH_FP64 = 0, QTNH_ARITH_F32X2 = 1, QTNH_ARITH_BF16X6 = 2 };
 int qtnh_set_arithmetic(int mode);
 int qtnh_get_arithmetic(void);
+
+/* Precision of the complex GEMM inside dense contractions (_contract_dense,
+ * src/tensor/contract.cpp:12-201).
+ * QTNH_GEMM_FP64 (default): complex128 FP64 fused multiply-adds, the plain method
+ *   (reproduces the reference within 1e-12 relative L2).
+ * QTNH_GEMM_BF16X3: split precision on the tcgen05 tensor cores: every real split into
+ *   three bf16 pieces (24 bits), the six piece products with i + j <= 2 accumulated in
+ *   FP32 on the tensor cores; FP32-level error (~1e-6 relative L2 at K ~ 100, growing
+ *   with K; report it against QTNH_GEMM_FP64).
+ * The environment variable QTNH_GEMM=fp64|bf16x3 sets the initial mode. Process-wide. */
+enum { QTNH_GEMM_FP64 = 0, QTNH_GEMM_BF16X3 = 1 };
+int qtnh_set_gemm_precision(int mode);
+int qtnh_get_gemm_precision(void);
 
 /* ---- data movement: TIDense kernels ------------------------------------------------ */
 

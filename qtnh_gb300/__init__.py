@@ -252,3 +252,15 @@ def set_arithmetic(mode):
 
 def get_arithmetic():
     return int(lib().qtnh_get_arithmetic())
+
+
+GEMM_FP64, GEMM_BF16X3 = 0, 1
+
+
+def set_gemm_precision(mode):
+    """QTNH_GEMM_FP64 (0, plain) or QTNH_GEMM_BF16X3 (1, split precision on tcgen05)."""
+    check(lib().qtnh_set_gemm_precision(ctypes.c_int(mode)))
+
+
+def get_gemm_precision():
+    return int(lib().qtnh_get_gemm_precision())

@@ -215,7 +215,10 @@ void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, c
     }
     const bool direct = is_identity(pC);
     if (!direct) Cp = static_cast<c128*>(workspace_alloc(M * N * sizeof(c128), stream));
-    zgemm(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, s);
+    if (gemm_mode() == QTNH_GEMM_BF16X3)
+      gemm_bf16x3(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, stream);
+    else
+      zgemm(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, s);
     if (!direct) permute_device(Cp, c, dC, pC, stream);
   } catch (...) {
     workspace_free(Ap, stream);

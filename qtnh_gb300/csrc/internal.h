@@ -33,6 +33,7 @@ int guarded(F&& f) {
 
 extern std::atomic<uint64_t> g_launches;
 int arithmetic_mode();  // QTNH_ARITH_*
+int gemm_mode();        // QTNH_GEMM_*
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 inline uint64_t product(const dims_t& d) {
@@ -93,6 +94,9 @@ void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16
 // Gate list in order; consecutive disjoint two-qubit pairs fused onto the tensor cores.
 void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
                          const std::vector<const void*>& gates, void* stream);
+// C (M x N) = A (M x K) B (K x N), complex128 row-major, BF16x3 pieces on tcgen05.
+void gemm_bf16x3(const void* A, const void* B, void* C, uint64_t M, uint64_t N, uint64_t K, void* stream);
+uint32_t take_gemm_error();
 void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
                            const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,
                            const std::vector<uint16_t>& pos_b, void* c, void* stream);

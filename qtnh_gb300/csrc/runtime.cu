@@ -34,6 +34,18 @@ int arithmetic_mode() {
   return m;
 }
 
+static std::atomic<int> g_gemm{-1};
+
+int gemm_mode() {
+  int m = g_gemm.load(std::memory_order_relaxed);
+  if (m < 0) {
+    const char* e = std::getenv("QTNH_GEMM");
+    m = (e && std::strcmp(e, "bf16x3") == 0) ? QTNH_GEMM_BF16X3 : QTNH_GEMM_FP64;
+    g_gemm.store(m);
+  }
+  return m;
+}
+
 int status_from_current_exception() {
   try {
     throw;
@@ -119,6 +131,16 @@ int qtnh_set_arithmetic(int mode) {
 }
 
 int qtnh_get_arithmetic(void) { return arithmetic_mode(); }
+
+int qtnh_set_gemm_precision(int mode) {
+  return guarded([&]() -> int {
+    if (mode != QTNH_GEMM_FP64 && mode != QTNH_GEMM_BF16X3) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown GEMM precision");
+    g_gemm.store(mode);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_get_gemm_precision(void) { return gemm_mode(); }
 
 int qtnh_device_count(int* count) {
   return guarded([&]() -> int {
