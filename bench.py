@@ -60,6 +60,10 @@ def _args():
     p.add_argument("--arith", default="bf16x6", choices=["bf16x6", "f32x2", "fp64"],
                    help="arithmetic of the gate/diagonal kernels (storage is complex128 either way)")
     p.add_argument("--no-arith-check", action="store_true")
+    p.add_argument("--workload", default="circuit", choices=["circuit", "contract"],
+                   help="circuit: the n=28 random layered circuit (headline); contract: 64 seeded dense "
+                        "contraction pairs, split-precision BF16x3 GEMM vs FP64 plain (precision study)")
+    p.add_argument("--pairs", type=int, default=64)
     return p.parse_args()
 
 
@@ -77,13 +81,14 @@ def _config(a, cpu_cores=None):
     }
 
 
-def _peaks():
+def _peaks(key="hbm_gbs"):
+    """Measured peak (MEASURED_PEAKS.json: hbm_gbs or bf16_tflops), else the fallback."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+        return float(d[key]), "measured"
     except Exception:
-        return 6800.0, "fallback"
+        return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
 def _traffic(kernel, n):
@@ -205,8 +210,235 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# ---- dense contraction pairs: split-precision GEMM vs FP64 plain ---------------------
+
+CONTRACT_METRIC = "contraction TFLOP/s (BF16x3 split precision, FP32 accumulation) vs FP64 plain at stated error"
+CPU_GEMM_SAMPLE = (128, 128, 128)
+
+
+def _contract_config(a, pairs):
+    mnk = [(M, N, K) for _, _, _, M, N, K in pairs]
+    return {
+        "workload": "%d seeded DenseTensor pairs: ranks 4-6, dims from {2,4,16,32,64}, 2-3 shared indices at random "
+                    "positions, <= 2^26 elements per tensor, M,N,K in [256,16384]; entries complex Gaussian, A scaled "
+                    "1/sqrt(K)" % len(pairs),
+        "pairs": len(pairs),
+        "flop_per_step": float(sum(8.0 * M * N * K for M, N, K in mnk)),
+        "max_mnk": [int(x) for x in max(mnk, key=lambda t: t[0] * t[1] * t[2])],
+        "element": "complex128 in and out",
+        "l2_flush": "not needed: the operands of a step (GBs) are far larger than the 129 MB L2",
+        "parallelism": "replicas" if a.gpus > 1 else "single GPU",
+    }
+
+
+def _cpu_gemm_sample():
+    """Oracle port on one core: seconds for one complex contraction of CPU_GEMM_SAMPLE."""
+    import numpy as np
+    from oracle import oracle as orc
+    orc.build()
+    M, N, K = CPU_GEMM_SAMPLE
+    rng = np.random.default_rng(1)
+    t1 = orc.Tensor(orc.DENSE, [], [M, K], rng.standard_normal(M * K) + 1j * rng.standard_normal(M * K))
+    t2 = orc.Tensor(orc.DENSE, [], [K, N], rng.standard_normal(K * N) + 1j * rng.standard_normal(K * N))
+    t0 = time.perf_counter()
+    orc.contract(t1, t2, [(1, 0)])
+    return time.perf_counter() - t0
+
+
+def _gemm_worker(_):
+    return _cpu_gemm_sample()
+
+
+def run_reference_contract(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    M, N, K = CPU_GEMM_SAMPLE
+    times = []
+    with ctx.Pool(cores) as pool:
+        for step in range(a.warmup + a.steps):
+            t0 = time.perf_counter()
+            pool.map(_gemm_worker, range(cores))
+            if step >= a.warmup:
+                times.append(time.perf_counter() - t0)
+    value = cores * 8.0 * M * N * K / statistics.median(times) / 1e12
+    line = {
+        "metric": CONTRACT_METRIC, "value": value, "unit": "TFLOP/s", "impl": "reference", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": statistics.median(times) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+        "config": {"workload": "complex128 contraction %dx%dx%d, one per host core (the reference's triple loop, "
+                               "oracle port)" % (M, N, K)},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": "oracle port of _contract_dense, one %dx%dx%d contraction per core" % (M, N, K)},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main_contract(a):
+    import numpy as np
+    import torch
+    import qtnh_gb300 as q
+    from qtnh_gb300 import workload as wl
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        sec = min(_cpu_gemm_sample() for _ in range(2))
+        M, N, K = CPU_GEMM_SAMPLE
+        cpu = {"value": 8.0 * M * N * K / sec / 1e12, "unit": "TFLOP/s", "cores": 1, "kind": "port",
+               "sample": "oracle port of _contract_dense, one %dx%dx%d complex contraction on one core" % (M, N, K)}
+
+    rng = np.random.default_rng(a.seed)
+    pairs = [wl.dense_pair(rng) for _ in range(a.pairs)]
+    g = torch.Generator(device=dev)
+    g.manual_seed(a.seed + 1)
+    tens = []
+    max_out = 0
+    for d1, d2, wires, M, N, K in pairs:
+        A = torch.randn(int(np.prod(d1)), dtype=torch.complex128, device=dev, generator=g) / math.sqrt(K)
+        B = torch.randn(int(np.prod(d2)), dtype=torch.complex128, device=dev, generator=g)
+        tens.append((q.Tensor(q.DENSE, [], d1, A), q.Tensor(q.DENSE, [], d2, B), wires))
+        max_out = max(max_out, M * N)
+    out = torch.empty(max_out, dtype=torch.complex128, device=dev)
+    ref = torch.empty(max_out, dtype=torch.complex128, device=dev)
+    flops = sum(8.0 * M * N * K for _, _, _, M, N, K in pairs)
+    tensor_flops = sum(48.0 * M * N * K for _, _, _, M, N, K in pairs)  # 6 piece pairs x real form
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def step(buf):
+        for (t1, t2, wires), (_, _, _, M, N, _) in zip(tens, pairs):
+            q.contract(t1, t2, wires, out=buf[:M * N])
+
+    # FP64 plain: one timed pass (the reference numbers of the study) and the errors
+    q.set_gemm_precision(q.GEMM_FP64)
+    step(out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step(out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    q.set_gemm_precision(q.GEMM_BF16X3)
+    q.take_device_errors()
+    rels, maxs = [], []
+    for (t1, t2, wires), (_, _, _, M, N, _) in zip(tens, pairs):
+        q.set_gemm_precision(q.GEMM_FP64)
+        q.contract(t1, t2, wires, out=ref[:M * N])
+        q.set_gemm_precision(q.GEMM_BF16X3)
+        q.contract(t1, t2, wires, out=out[:M * N])
+        d = out[:M * N] - ref[:M * N]
+        rels.append((torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref[:M * N])).item())
+        maxs.append((d.abs().max() / ref[:M * N].abs().max()).item())
+
+    # split precision: warm-up, then the timed steps
+    for _ in range(a.warmup):
+        step(out)
+    torch.cuda.synchronize()
+    clocks = _Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    q.gemm_timing(True)
+    l0 = q.launches()
+    e0.record(stream)
+    for _ in range(a.steps):
+        step(out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ck = clocks.stop()
+    gemm_ms, gemm_launches = q.gemm_timing(False)
+    launches = q.launches() - l0
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * flops * a.steps / (ms * 1e-3) / 1e12
+    errors = q.take_device_errors()
+
+    # e2e: host operands copied in, results copied out, every contraction
+    hosts = [(t1.data.cpu().pin_memory(), t2.data.cpu().pin_memory()) for t1, t2, _ in tens]
+    host_out = torch.empty(max_out, dtype=torch.complex128, pin_memory=True)
+    h2d = sum(16 * (t1.data.numel() + t2.data.numel()) for t1, t2, _ in tens)
+    d2h = sum(16 * M * N for _, _, _, M, N, _ in pairs)
+    barrier()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(a.steps):
+        for (t1, t2, wires), (ha, hb), (_, _, _, M, N, _) in zip(tens, hosts, pairs):
+            t1.data.copy_(ha, non_blocking=True)
+            t2.data.copy_(hb, non_blocking=True)
+            q.contract(t1, t2, wires, out=out[:M * N])
+            host_out[:M * N].copy_(out[:M * N], non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ems = f0.elapsed_time(f1)
+    if dist is not None:
+        t = torch.tensor([ems], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ems = float(t.item())
+    e2e = world * flops * a.steps / (ems * 1e-3) / 1e12
+
+    if rank == 0:
+        peak, peak_kind = _peaks("bf16_tflops")
+        achieved = tensor_flops * a.steps / (gemm_ms * 1e-3) / 1e12 if gemm_ms else None
+        line = {
+            "metric": CONTRACT_METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128 (bf16x3 pieces, fp32 accumulation)",
+            "data": "synthetic (seeded dense pairs, complex Gaussian entries)", "config": _contract_config(a, pairs),
+            "plain_fp64": {"tflops": flops / (plain_ms * 1e-3) / 1e12, "ms_per_step": plain_ms,
+                           "speedup_of_split": (flops / (ms / a.steps * 1e-3)) / (flops / (plain_ms * 1e-3))},
+            "error_vs_fp64": {"rel_l2_median": statistics.median(rels), "rel_l2_max": max(rels),
+                              "max_abs_over_max_median": statistics.median(maxs), "max_abs_over_max_max": max(maxs)},
+            "roofline": {"bound": "tensor", "kernel": "gemm_bf16x3_umma_kernel", "achieved": achieved, "peak": peak,
+                         "peak_source": peak_kind, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                         "alg_flop_per_step": tensor_flops, "kernel_ms_per_step": gemm_ms / a.steps,
+                         "kernel_launches_per_step": gemm_launches // max(1, a.steps),
+                         "kernel_share_of_step": gemm_ms / ms if ms else None},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "clocks": ck,
+            "gpu_launches": launches,
+            "device_errors": errors,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     a = _args()
+    if a.workload == "contract":
+        if a.impl == "reference":
+            run_reference_contract(a)
+        else:
+            main_contract(a)
+        return
     if a.impl == "reference":
         run_reference(a)
         return

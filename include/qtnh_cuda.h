@@ -133,6 +133,11 @@ enum { QTNH_GEMM_FP64 = 0, QTNH_GEMM_BF16X3 = 1 };
 int qtnh_set_gemm_precision(int mode);
 int qtnh_get_gemm_precision(void);
 
+/* CUDA-event timing of the tcgen05 GEMM kernel launches (measurement support): returns
+ * the summed duration (ms) and count of the launches recorded since the previous call
+ * (synchronizing on them), then enables (enable != 0) or disables recording. */
+int qtnh_gemm_timing(int enable, double* ms, uint64_t* launches);
+
 /* ---- data movement: TIDense kernels ------------------------------------------------ */
 
 /* Tensor::permute / TIDense::_permute_internal (src/tensor/dense.cpp:152-169, 354-488):

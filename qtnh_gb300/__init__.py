@@ -264,3 +264,10 @@ def set_gemm_precision(mode):
 
 def get_gemm_precision():
     return int(lib().qtnh_get_gemm_precision())
+
+
+def gemm_timing(enable):
+    """(ms, launches) of the tcgen05 GEMM kernel since the last call; then (dis)arm recording."""
+    ms, n = ctypes.c_double(), ctypes.c_uint64()
+    check(lib().qtnh_gemm_timing(ctypes.c_int(1 if enable else 0), ctypes.byref(ms), ctypes.byref(n)))
+    return ms.value, int(n.value)

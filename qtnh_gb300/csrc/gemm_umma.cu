@@ -31,6 +31,8 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include "cuda_common.cuh"
 #include "df32.cuh"
@@ -451,6 +453,11 @@ __global__ void reduce_partials_kernel(const float* __restrict__ P, uint32_t S, 
 
 }  // namespace
 
+// Optional CUDA-event timing of the GEMM kernel launches (qtnh_gemm_timing).
+static std::mutex g_timing_mu;
+static bool g_timing = false;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_timing_events;
+
 // C (M x N) = A (M x K) B (K x N), complex128 row-major, through BF16x3 pieces on tcgen05.
 void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t N, uint64_t K, void* stream) {
   if (M == 0 || N == 0) return;
@@ -488,7 +495,21 @@ void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t 
     check_cuda(cudaFuncSetAttribute(gemm_bf16x3_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "gemm_bf16x3_umma_kernel shared memory");
     const int grid = (int)std::min<uint64_t>((uint64_t)p.MT * p.NT * p.S, (uint64_t)sm_count());
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(g_timing_mu);
+      if (g_timing) {
+        check_cuda(cudaEventCreate(&e0), "event");
+        check_cuda(cudaEventCreate(&e1), "event");
+        check_cuda(cudaEventRecord(e0, s), "event record");
+      }
+    }
     gemm_bf16x3_umma_kernel<<<grid, GM_THREADS, smem, s>>>(p);
+    if (e0) {
+      check_cuda(cudaEventRecord(e1, s), "event record");
+      std::lock_guard<std::mutex> lk(g_timing_mu);
+      g_timing_events.emplace_back(e0, e1);
+    }
     count_launch(3);
     if (p.S > 1) {
       reduce_partials_kernel<<<grid_for((M * N + 255) / 256, 8), 256, 0, s>>>(
@@ -503,6 +524,25 @@ void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t 
   workspace_free(ws, stream);
 }
 
+// Sum of the recorded GEMM kernel durations (synchronizes on each event pair).
+static void take_gemm_times(double& ms, uint64_t& launches) {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+  {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    ev.swap(g_timing_events);
+  }
+  ms = 0;
+  launches = ev.size();
+  for (auto& e : ev) {
+    float t = 0;
+    check_cuda(cudaEventSynchronize(e.second), "event synchronize");
+    check_cuda(cudaEventElapsedTime(&t, e.first, e.second), "event elapsed");
+    ms += t;
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+}
+
 uint32_t take_gemm_error() {
   uint32_t v = 0;
   check_cuda(cudaMemcpyFromSymbol(&v, g_gemm_error, sizeof(v)), "read device error flags");
@@ -512,3 +552,18 @@ uint32_t take_gemm_error() {
 }
 
 }  // namespace qtnh_impl
+
+using namespace qtnh_impl;
+
+extern "C" int qtnh_gemm_timing(int enable, double* ms, uint64_t* launches) {
+  return guarded([&]() -> int {
+    double t = 0;
+    uint64_t n = 0;
+    take_gemm_times(t, n);
+    if (ms) *ms = t;
+    if (launches) *launches = n;
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timing = enable != 0;
+    return QTNH_OK;
+  });
+}

@@ -107,3 +107,34 @@ def random_state(n, seed=7):
     psi = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
     psi /= np.linalg.norm(psi)
     return psi
+
+
+# ---- dense contraction pairs (the precision study of the dense GEMM) ------------------
+
+DENSE_DIMS = (2, 4, 16, 32, 64)
+
+
+def dense_pair(rng, max_elems=2 ** 26, mnk_range=(256, 16384), max_mnk=None):
+    """One DenseTensor pair: ranks 4-6, dims from {2, 4, 16, 32, 64}, 2-3 shared indices at
+    random positions, at most max_elems elements per tensor, M, N, K within mnk_range
+    (and M*N*K <= max_mnk when given). Returns (dims1, dims2, wires, M, N, K)."""
+    lo, hi = mnk_range
+    while True:
+        r1, r2 = int(rng.integers(4, 7)), int(rng.integers(4, 7))
+        ns = int(rng.integers(2, 4))
+        shared = [int(rng.choice(DENSE_DIMS)) for _ in range(ns)]
+        o1 = [int(rng.choice(DENSE_DIMS)) for _ in range(r1 - ns)]
+        o2 = [int(rng.choice(DENSE_DIMS)) for _ in range(r2 - ns)]
+        M, N, K = int(np.prod(o1)), int(np.prod(o2)), int(np.prod(shared))
+        if not (lo <= M <= hi and lo <= N <= hi and lo <= K <= hi):
+            continue
+        if M * K > max_elems or K * N > max_elems or (max_mnk and M * N * K > max_mnk):
+            continue
+        p1, p2 = [int(x) for x in rng.permutation(r1)], [int(x) for x in rng.permutation(r2)]
+        d1, d2 = [0] * r1, [0] * r2
+        for i, dim in enumerate(o1 + shared):
+            d1[p1[i]] = dim
+        for i, dim in enumerate(shared + o2):
+            d2[p2[i]] = dim
+        wires = [(p1[len(o1) + j], p2[j]) for j in range(ns)]
+        return d1, d2, wires, M, N, K
