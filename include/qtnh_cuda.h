@@ -239,6 +239,38 @@ int qtnh_apply_diag_layer(void* state, int32_t rank, const uint64_t* dims, int32
 /* sum |x|^2 over n elements, computed in FP64 on the device; result to host. Synchronous. */
 int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream);
 
+/* ---- batched circuits in mixed precision ------------------------------------------- */
+
+/* Many independent circuits of uneven qubit counts and depths, complex64 states resident
+ * in HBM. Operations per circuit follow the layered-circuit contractions: two-qubit
+ * SymmTensor gates (els in SymmTensor layout, host pointer to 16 complex128; input 0 on
+ * qubit qa, input 1 on qb; include/tensor/symm.hpp:22-45), a phase layer (n host
+ * phases: DiagTensor (1, e^{i phase}) on every qubit) and SwapTensor qubit exchanges,
+ * applied per layer in that order; every `renorm_every` layers each state is
+ * renormalised with an FP64 norm; queries return amplitudes as complex128 (host index
+ * lists). Qubit q is bit n - 1 - q of the amplitude index (row-major dims [2]*n).
+ * qtnh_batch_compile groups the operations of all circuits into rounds of grouped
+ * persistent kernels, optionally autotunes the gate kernel, and captures the whole run
+ * (state reset from the initial states, every round, the queries) as one CUDA graph;
+ * qtnh_batch_run replays it ordered after and before work on `stream`. */
+typedef struct qtnh_batch qtnh_batch;
+int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits);
+int qtnh_batch_destroy(qtnh_batch* b);
+/* Initial state of circuit c from a device complex128 array (converted to complex64). */
+int qtnh_batch_set_state(qtnh_batch* b, int32_t c, const void* psi_c128, void* stream);
+int qtnh_batch_add_gate(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb, const void* els_c128);
+int qtnh_batch_add_phases(qtnh_batch* b, int32_t c, int32_t layer, const double* phases);
+int qtnh_batch_add_swap(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb);
+int qtnh_batch_add_queries(qtnh_batch* b, int32_t c, int32_t nq, const uint64_t* idx);
+int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune);
+int qtnh_batch_run(qtnh_batch* b, void* stream);
+/* All query results (registration order) into a device complex128 array. */
+int qtnh_batch_results(qtnh_batch* b, void* out_c128, uint64_t capacity, void* stream);
+/* Final state of circuit c as complex128 (device array of 2^n; synchronizes `stream`). */
+int qtnh_batch_state(qtnh_batch* b, int32_t c, void* out_c128, void* stream);
+int qtnh_batch_info(qtnh_batch* b, uint64_t* amplitudes, uint64_t* rounds, uint64_t* launches_per_run,
+                    int32_t* gate_threads, uint64_t* gate_chunk);
+
 #ifdef __cplusplus
 }
 #endif

@@ -271,3 +271,79 @@ def gemm_timing(enable):
     ms, n = ctypes.c_double(), ctypes.c_uint64()
     check(lib().qtnh_gemm_timing(ctypes.c_int(1 if enable else 0), ctypes.byref(ms), ctypes.byref(n)))
     return ms.value, int(n.value)
+
+
+class Batch:
+    """Batched circuits in mixed precision (complex64 states, FP64 renormalisation and
+    queries) on the C ABI's qtnh_batch_* entry points: add circuits, compile once (rounds
+    of grouped kernels, autotuning, CUDA graph capture), run and read the queries."""
+
+    def __init__(self, nqubits):
+        self._b = ctypes.c_void_p()
+        arr = (ctypes.c_int32 * len(nqubits))(*[int(x) for x in nqubits])
+        check(lib().qtnh_batch_create(ctypes.byref(self._b), ctypes.c_int32(len(nqubits)), arr))
+        self.nq = [int(x) for x in nqubits]
+        self.nqueries = 0
+
+    def __del__(self):
+        try:
+            if self._b:
+                lib().qtnh_batch_destroy(self._b)
+        except Exception:
+            pass
+
+    def set_state(self, c, psi, stream=None):
+        _check_c128(psi)
+        check(lib().qtnh_batch_set_state(self._b, ctypes.c_int32(c), _ptr(psi), _stream(stream)))
+
+    def add_circuit(self, c, circuit, queries=()):
+        """Registers a workload.Circuit (gates, phase layers, qubit-swap permutations)."""
+        import numpy as np
+        L = lib()
+        for li, layer in enumerate(circuit.layers):
+            for (qa, qb), els in zip(layer.pairs, layer.gates):
+                e = np.ascontiguousarray(els, dtype=np.complex128)
+                check(L.qtnh_batch_add_gate(self._b, ctypes.c_int32(c), ctypes.c_int32(li), ctypes.c_uint16(qa),
+                                            ctypes.c_uint16(qb), ctypes.c_void_p(e.ctypes.data)))
+            if layer.phases is not None:
+                ph = np.ascontiguousarray(layer.phases, dtype=np.float64)
+                check(L.qtnh_batch_add_phases(self._b, ctypes.c_int32(c), ctypes.c_int32(li),
+                                              ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+            if layer.ptup is not None:
+                moved = [i for i, p in enumerate(layer.ptup) if p != i]
+                if len(moved) != 2 or layer.ptup[moved[0]] != moved[1]:
+                    raise ValueError("only two-qubit swaps are supported as permutations")
+                check(L.qtnh_batch_add_swap(self._b, ctypes.c_int32(c), ctypes.c_int32(li), ctypes.c_uint16(moved[0]),
+                                            ctypes.c_uint16(moved[1])))
+        if len(queries):
+            idx = np.ascontiguousarray(queries, dtype=np.uint64)
+            check(L.qtnh_batch_add_queries(self._b, ctypes.c_int32(c), ctypes.c_int32(len(idx)),
+                                           idx.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+            self.nqueries += len(idx)
+
+    def compile(self, renorm_every=8, autotune=True):
+        check(lib().qtnh_batch_compile(self._b, ctypes.c_int32(renorm_every), ctypes.c_int32(1 if autotune else 0)))
+
+    def run(self, stream=None):
+        check(lib().qtnh_batch_run(self._b, _stream(stream)))
+
+    def results(self, out=None, stream=None):
+        import torch
+        if out is None:
+            out = torch.empty(max(1, self.nqueries), dtype=torch.complex128, device="cuda")
+        check(lib().qtnh_batch_results(self._b, _ptr(out), ctypes.c_uint64(out.numel()), _stream(stream)))
+        return out[:self.nqueries]
+
+    def state(self, c, stream=None):
+        import torch
+        out = torch.empty(2 ** self.nq[c], dtype=torch.complex128, device="cuda")
+        check(lib().qtnh_batch_state(self._b, ctypes.c_int32(c), _ptr(out), _stream(stream)))
+        return out
+
+    def info(self):
+        amps, rounds, lpr, chunk = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        th = ctypes.c_int32()
+        check(lib().qtnh_batch_info(self._b, ctypes.byref(amps), ctypes.byref(rounds), ctypes.byref(lpr),
+                                    ctypes.byref(th), ctypes.byref(chunk)))
+        return {"amplitudes": amps.value, "rounds": rounds.value, "launches_per_run": lpr.value,
+                "gate_threads": th.value, "gate_chunk": chunk.value}

@@ -1,0 +1,722 @@
+// Batched circuits in mixed precision: many independent circuits of uneven qubit counts
+// and depths, complex64 states resident in HBM, run as layer-synchronous rounds of
+// grouped persistent kernels under one captured CUDA graph.
+//
+// Per circuit the operations are the reference's contractions with a layered circuit:
+// two-qubit SymmTensor gates (include/tensor/symm.hpp:22-45 layout, applied in place as
+// by the Symm rule of src/tensor/contract.cpp:250-289), a layer of single-qubit phase
+// DiagTensors, and SwapTensor qubit exchanges; every `renorm` layers the state is
+// renormalised with an FP64 norm, and the circuit ends in amplitude queries returned in
+// complex128.
+//
+// Arithmetic: amplitudes complex64; a gate U is held as two complex64 matrices
+// U = U_hi + U_lo (the FP64 gate to ~48 bits), and each output sum_i (U_lo x_i) +
+// (U_hi x_i) is accumulated with FP32 fused multiply-adds, so the only rounding of note is
+// the store to complex64. Phase layers multiply by lo/hi tables of per-qubit phase
+// products (built in FP64, stored complex64). Norms: per-thread compensated FP32 sums
+// (TwoSum) reduced in FP64.
+//
+// Scheduling: `compile` groups the operations of all circuits into rounds (layer L: the
+// s-th gate of every circuit that has one, for each slot s; then the phase layers; then
+// the swaps; then the renormalisation), so every round is one launch over a task table
+// (circuit, operand) x chunks; a persistent grid walks the (task, chunk) work items,
+// finding its task by binary search over the tasks' chunk offsets. An autotuner times
+// the gate kernel's block size and chunk length on the largest gate round. The whole
+// schedule -- state reset from the initial states, norm reset, every round, the
+// queries -- is captured once as a CUDA graph and replayed by `run`.
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <memory>
+#include <vector>
+
+#include "cuda_common.cuh"
+#include "df32.cuh"
+
+struct qtnh_batch;
+
+namespace qtnh_impl {
+
+namespace {
+
+using c64 = float2;
+
+struct GateTask {
+  uint64_t base;  // first amplitude of the circuit's state
+  uint32_t n;     // qubits
+  uint32_t ba, bb;  // bit positions of gate inputs 0 and 1
+  uint32_t gate;    // index into the gate table (32 c64: U_hi[16], U_lo[16], U[out * 4 + in])
+};
+struct PhaseTask {
+  uint64_t base, table;  // state offset, offset of the lo table (hi table follows, 2^(n - split))
+  uint32_t n, split;
+};
+struct SwapTask {
+  uint64_t base;
+  uint32_t n, ba, bb;
+};
+struct NormTask {
+  uint64_t base;
+  uint32_t n, slot;  // slot into the norm array
+};
+
+enum RoundKind { R_GATE = 0, R_PHASE = 1, R_SWAP = 2, R_NORM = 3, R_SCALE = 4 };
+
+struct Round {
+  int kind;
+  uint32_t ntasks = 0;
+  uint64_t total = 0;       // work items (chunks)
+  void* tasks = nullptr;    // device task table
+  uint64_t* cbeg = nullptr; // device chunk offsets (ntasks)
+  uint64_t elems_per_chunk = 0;
+};
+
+__device__ __forceinline__ uint32_t find_task(const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t w) {
+  uint32_t lo = 0, hi = ntasks;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (cbeg[mid] <= w)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint64_t insert_zero(uint64_t x, uint32_t bit) {
+  return ((x >> bit) << (bit + 1)) | (x & ((1ull << bit) - 1));
+}
+
+__device__ __forceinline__ void cmac(float2 u, float2 x, float& re, float& im) {
+  re = fmaf(u.x, x.x, re);
+  re = fmaf(-u.y, x.y, re);
+  im = fmaf(u.x, x.y, im);
+  im = fmaf(u.y, x.x, im);
+}
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) b_gate_kernel(c64* __restrict__ psi, const GateTask* __restrict__ tasks,
+                                                         const uint64_t* __restrict__ cbeg, uint32_t ntasks,
+                                                         uint64_t total, const c64* __restrict__ gates,
+                                                         uint64_t chunk_groups) {
+  __shared__ c64 g[32];
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const GateTask t = tasks[s_task];
+    if (threadIdx.x < 32) g[threadIdx.x] = gates[(uint64_t)t.gate * 32 + threadIdx.x];
+    __syncthreads();
+    const uint64_t ngroups = 1ull << (t.n - 2);
+    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
+    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
+    const uint32_t lo = min(t.ba, t.bb), hi = max(t.ba, t.bb);
+    const uint64_t sa = 1ull << t.ba, sb = 1ull << t.bb;
+    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
+      const uint64_t x0 = t.base + insert_zero(insert_zero(grp, lo), hi);
+      const uint64_t off[4] = {0, sb, sa, sa + sb};  // (input 0, input 1) = (0,0), (0,1), (1,0), (1,1)
+      c64 x[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x[i] = psi[x0 + off[i]];
+#pragma unroll
+      for (int o = 0; o < 4; ++o) {
+        float re = 0.0f, im = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cmac(g[16 + o * 4 + i], x[i], re, im);  // U_lo first (smaller terms)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cmac(g[o * 4 + i], x[i], re, im);
+        psi[x0 + off[o]] = make_float2(re, im);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void b_phase_kernel(c64* __restrict__ psi, const PhaseTask* __restrict__ tasks,
+                               const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total,
+                               const c64* __restrict__ tables, uint64_t chunk) {
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const PhaseTask t = tasks[s_task];
+    const uint64_t nel = 1ull << t.n;
+    const uint64_t e0 = (w - cbeg[s_task]) * chunk, e1 = min(e0 + chunk, nel);
+    const c64* tlo = tables + t.table;
+    const c64* thi = tlo + (1ull << t.split);
+    const uint64_t mask = (1ull << t.split) - 1;
+    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const c64 a = tlo[e & mask], b = thi[e >> t.split];
+      const c64 f = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+      const c64 x = psi[t.base + e];
+      psi[t.base + e] = make_float2(f.x * x.x - f.y * x.y, f.x * x.y + f.y * x.x);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void b_swap_kernel(c64* __restrict__ psi, const SwapTask* __restrict__ tasks,
+                              const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total, uint64_t chunk) {
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const SwapTask t = tasks[s_task];
+    const uint64_t npairs = 1ull << (t.n - 2);
+    const uint64_t p0 = (w - cbeg[s_task]) * chunk, p1 = min(p0 + chunk, npairs);
+    const uint32_t lo = min(t.ba, t.bb), hi = max(t.ba, t.bb);
+    for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+      const uint64_t x = t.base + insert_zero(insert_zero(p, lo), hi);
+      const uint64_t xa = x + (1ull << t.ba), xb = x + (1ull << t.bb);
+      const c64 va = psi[xa], vb = psi[xb];
+      psi[xa] = vb;
+      psi[xb] = va;
+    }
+    __syncthreads();
+  }
+}
+
+// Sum of |psi|^2 per task into norms[slot]: compensated FP32 per thread, FP64 across.
+__global__ void b_norm_kernel(const c64* __restrict__ psi, const NormTask* __restrict__ tasks,
+                              const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total, uint64_t chunk,
+                              double* __restrict__ norms) {
+  __shared__ uint32_t s_task;
+  __shared__ double s_part[32];
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const NormTask t = tasks[s_task];
+    const uint64_t nel = 1ull << t.n;
+    const uint64_t e0 = (w - cbeg[s_task]) * chunk, e1 = min(e0 + chunk, nel);
+    float s = 0.0f, c = 0.0f;
+    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const c64 x = psi[t.base + e];
+      float ns, err;
+      df::two_sum(s, fmaf(x.x, x.x, x.y * x.y), ns, err);
+      s = ns;
+      c += err;
+    }
+    double v = (double)s + (double)c;
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) tot += s_part[i];
+      atomicAdd(&norms[t.slot], tot);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void b_scale_kernel(c64* __restrict__ psi, const NormTask* __restrict__ tasks,
+                               const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total, uint64_t chunk,
+                               const double* __restrict__ norms) {
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const NormTask t = tasks[s_task];
+    const double nrm = norms[t.slot];
+    const float f = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 1.0f;
+    const uint64_t nel = 1ull << t.n;
+    const uint64_t e0 = (w - cbeg[s_task]) * chunk, e1 = min(e0 + chunk, nel);
+    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const c64 x = psi[t.base + e];
+      psi[t.base + e] = make_float2(x.x * f, x.y * f);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void b_query_kernel(const c64* __restrict__ psi, const uint64_t* __restrict__ where, uint64_t nq,
+                               double2* __restrict__ out) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (uint64_t)gridDim.x * blockDim.x) {
+    const c64 x = psi[where[i]];
+    out[i] = make_double2((double)x.x, (double)x.y);
+  }
+}
+
+__global__ void b_to_c64_kernel(const double2* __restrict__ in, c64* __restrict__ out, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+struct Op {
+  int kind;  // R_GATE, R_PHASE, R_SWAP
+  int layer;
+  uint16_t qa = 0, qb = 0;
+  uint32_t index = 0;  // gate table index / phase entry
+};
+
+}  // namespace
+
+}  // namespace qtnh_impl
+
+using namespace qtnh_impl;
+
+struct qtnh_batch {
+  std::vector<uint32_t> nq;
+  std::vector<uint64_t> base;
+  uint64_t total_amps = 0;
+  c64* psi = nullptr;   // working states
+  c64* psi0 = nullptr;  // initial states
+  std::vector<std::vector<Op>> ops;
+  std::vector<c64> gate_host;                     // 32 c64 per gate
+  std::vector<std::vector<double>> phase_host;    // per phase op: n phases
+  std::vector<std::pair<uint64_t, uint64_t>> queries;  // (circuit, index)
+  // compiled
+  std::vector<Round> rounds;
+  std::vector<void*> allocations;
+  c64* gates = nullptr;
+  c64* tables = nullptr;
+  double* norms = nullptr;
+  uint64_t nnorms = 0;
+  uint64_t* query_where = nullptr;
+  double2* query_out = nullptr;
+  int gate_threads = 256;
+  uint64_t gate_chunk = 1024;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t launches_per_run = 0;
+  int max_layer = -1;
+
+  ~qtnh_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : allocations) cudaFree(p);
+    if (psi) cudaFree(psi);
+    if (psi0) cudaFree(psi0);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  T* upload(const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    void* p = nullptr;
+    check_cuda(cudaMalloc(&p, v.size() * sizeof(T)), "batch allocation");
+    allocations.push_back(p);
+    check_cuda(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "batch upload");
+    return static_cast<T*>(p);
+  }
+
+  uint32_t bit(uint32_t c, uint16_t q) const { return nq[c] - 1 - q; }
+
+  int grid(uint64_t total, int threads) const {
+    const int per_sm = std::max(1, 2048 / threads);
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(total, (uint64_t)sm_count() * per_sm));
+  }
+
+  template <typename Task>
+  Round make_round(int kind, const std::vector<Task>& tasks, const std::vector<uint64_t>& units, uint64_t chunk) {
+    Round r;
+    r.kind = kind;
+    r.ntasks = (uint32_t)tasks.size();
+    r.elems_per_chunk = chunk;
+    std::vector<uint64_t> cb(tasks.size());
+    uint64_t acc = 0;
+    for (size_t i = 0; i < tasks.size(); ++i) {
+      cb[i] = acc;
+      acc += (units[i] + chunk - 1) / chunk;
+    }
+    r.total = acc;
+    r.tasks = upload(tasks);
+    r.cbeg = upload(cb);
+    return r;
+  }
+
+  void launch(const Round& r, cudaStream_t s, int gthreads, uint64_t gchunk) {
+    switch (r.kind) {
+      case R_GATE: {
+        const auto* t = static_cast<const GateTask*>(r.tasks);
+        const int g = grid(r.total, gthreads);
+        if (gthreads == 128)
+          b_gate_kernel<128><<<g, 128, 0, s>>>(psi, t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+        else if (gthreads == 512)
+          b_gate_kernel<512><<<g, 512, 0, s>>>(psi, t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+        else
+          b_gate_kernel<256><<<g, 256, 0, s>>>(psi, t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+        break;
+      }
+      case R_PHASE:
+        b_phase_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const PhaseTask*>(r.tasks), r.cbeg,
+                                                          r.ntasks, r.total, tables, r.elems_per_chunk);
+        break;
+      case R_SWAP:
+        b_swap_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const SwapTask*>(r.tasks), r.cbeg, r.ntasks,
+                                                         r.total, r.elems_per_chunk);
+        break;
+      case R_NORM:
+        b_norm_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const NormTask*>(r.tasks), r.cbeg, r.ntasks,
+                                                         r.total, r.elems_per_chunk, norms);
+        break;
+      case R_SCALE:
+        b_scale_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const NormTask*>(r.tasks), r.cbeg,
+                                                          r.ntasks, r.total, r.elems_per_chunk, norms);
+        break;
+    }
+    count_launch();
+  }
+};
+
+namespace {
+constexpr uint64_t B_CHUNK = 4096;  // amplitudes (or pairs) per work item of the streaming rounds
+
+qtnh_batch* checked(qtnh_batch* b) {
+  if (!b) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null batch");
+  return b;
+}
+void check_circuit(qtnh_batch* b, int32_t c) {
+  if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
+  if (b->exec) throw Error(QTNH_ERR_RUNTIME, "batch already compiled");
+}
+}  // namespace
+
+extern "C" {
+
+int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits) {
+  return guarded([&]() -> int {
+    if (!out || ncircuits <= 0 || !nqubits) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid batch arguments");
+    std::unique_ptr<qtnh_batch> b(new qtnh_batch());
+    for (int32_t c = 0; c < ncircuits; ++c) {
+      if (nqubits[c] < 2 || nqubits[c] > 34) throw Error(QTNH_ERR_INVALID_ARGUMENT, "qubit count outside 2..34");
+      b->nq.push_back((uint32_t)nqubits[c]);
+      b->base.push_back(b->total_amps);
+      b->total_amps += 1ull << nqubits[c];
+    }
+    b->ops.resize(ncircuits);
+    check_cuda(cudaMalloc(&b->psi, b->total_amps * sizeof(c64)), "batch states");
+    check_cuda(cudaMalloc(&b->psi0, b->total_amps * sizeof(c64)), "batch initial states");
+    check_cuda(cudaMemset(b->psi0, 0, b->total_amps * sizeof(c64)), "batch initial states");
+    check_cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "batch stream");
+    *out = b.release();
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_destroy(qtnh_batch* b) {
+  return guarded([&]() -> int {
+    delete b;
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_set_state(qtnh_batch* b, int32_t c, const void* psi_c128, void* stream) {
+  return guarded([&]() -> int {
+    checked(b);
+    if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
+    const uint64_t n = 1ull << b->nq[c];
+    b_to_c64_kernel<<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(
+        static_cast<const double2*>(psi_c128), b->psi0 + b->base[c], n);
+    count_launch();
+    check_cuda(cudaGetLastError(), "batch state conversion");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_add_gate(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb, const void* els_c128) {
+  return guarded([&]() -> int {
+    checked(b);
+    check_circuit(b, c);
+    if (layer < 0 || qa >= b->nq[c] || qb >= b->nq[c] || qa == qb || !els_c128)
+      throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid gate");
+    // SymmTensor elements els[in * 4 + out] = U[out][in]; stored as U_hi / U_lo [out * 4 + in]
+    const std::complex<double>* e = static_cast<const std::complex<double>*>(els_c128);
+    const size_t g0 = b->gate_host.size();
+    b->gate_host.resize(g0 + 32);
+    for (int o = 0; o < 4; ++o)
+      for (int i = 0; i < 4; ++i) {
+        const std::complex<double> u = e[i * 4 + o];
+        const float hr = (float)u.real(), hi = (float)u.imag();
+        b->gate_host[g0 + o * 4 + i] = make_float2(hr, hi);
+        b->gate_host[g0 + 16 + o * 4 + i] = make_float2((float)(u.real() - hr), (float)(u.imag() - hi));
+      }
+    Op op;
+    op.kind = R_GATE;
+    op.layer = layer;
+    op.qa = qa;
+    op.qb = qb;
+    op.index = (uint32_t)(g0 / 32);
+    b->ops[c].push_back(op);
+    b->max_layer = std::max(b->max_layer, (int)layer);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_add_phases(qtnh_batch* b, int32_t c, int32_t layer, const double* phases) {
+  return guarded([&]() -> int {
+    checked(b);
+    check_circuit(b, c);
+    if (layer < 0 || !phases) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid phase layer");
+    Op op;
+    op.kind = R_PHASE;
+    op.layer = layer;
+    op.index = (uint32_t)b->phase_host.size();
+    b->phase_host.emplace_back(phases, phases + b->nq[c]);
+    b->ops[c].push_back(op);
+    b->max_layer = std::max(b->max_layer, (int)layer);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_add_swap(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb) {
+  return guarded([&]() -> int {
+    checked(b);
+    check_circuit(b, c);
+    if (layer < 0 || qa >= b->nq[c] || qb >= b->nq[c] || qa == qb) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid swap");
+    Op op;
+    op.kind = R_SWAP;
+    op.layer = layer;
+    op.qa = qa;
+    op.qb = qb;
+    b->ops[c].push_back(op);
+    b->max_layer = std::max(b->max_layer, (int)layer);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_add_queries(qtnh_batch* b, int32_t c, int32_t nq, const uint64_t* idx) {
+  return guarded([&]() -> int {
+    checked(b);
+    check_circuit(b, c);
+    if (nq < 0 || (nq && !idx)) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid queries");
+    for (int32_t i = 0; i < nq; ++i) {
+      if (idx[i] >= (1ull << b->nq[c])) throw Error(QTNH_ERR_OUT_OF_RANGE, "query index out of range");
+      b->queries.emplace_back((uint64_t)c, idx[i]);
+    }
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
+  return guarded([&]() -> int {
+    checked(b);
+    if (b->exec) throw Error(QTNH_ERR_RUNTIME, "batch already compiled");
+    const size_t nc = b->nq.size();
+    b->gates = b->upload(b->gate_host);
+    // phase tables: per phase op, lo table over the low `split` bits and hi table over the rest
+    std::vector<c64> tab;
+    std::vector<uint64_t> tab_off(b->phase_host.size()), tab_split(b->phase_host.size());
+    std::vector<int32_t> phase_circuit(b->phase_host.size(), -1);
+    for (size_t c = 0; c < nc; ++c)
+      for (auto& op : b->ops[c])
+        if (op.kind == R_PHASE) phase_circuit[op.index] = (int32_t)c;
+    for (size_t k = 0; k < b->phase_host.size(); ++k) {
+      const uint32_t n = b->nq[phase_circuit[k]];
+      const uint32_t split = std::min<uint32_t>(n, 11);
+      tab_off[k] = tab.size();
+      tab_split[k] = split;
+      // bit j of the index is qubit n - 1 - j
+      for (int part = 0; part < 2; ++part) {
+        const uint32_t nbits = part ? n - split : split, shift = part ? split : 0;
+        for (uint64_t v = 0; v < (1ull << nbits); ++v) {
+          double ph = 0;
+          for (uint32_t j = 0; j < nbits; ++j)
+            if ((v >> j) & 1) ph += b->phase_host[k][n - 1 - (j + shift)];
+          tab.push_back(make_float2((float)std::cos(ph), (float)std::sin(ph)));
+        }
+      }
+    }
+    b->tables = b->upload(tab);
+    // rounds
+    const int period = renorm_every > 0 ? renorm_every : 0;
+    std::vector<uint64_t> norm_slot_base;
+    for (int L = 0; L <= b->max_layer; ++L) {
+      for (int slot = 0;; ++slot) {
+        std::vector<GateTask> t;
+        std::vector<uint64_t> u;
+        for (size_t c = 0; c < nc; ++c) {
+          int seen = 0;
+          for (auto& op : b->ops[c])
+            if (op.kind == R_GATE && op.layer == L && seen++ == slot) {
+              t.push_back({b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb), op.index});
+              u.push_back(1ull << (b->nq[c] - 2));
+            }
+        }
+        if (t.empty()) break;
+        b->rounds.push_back(b->make_round(R_GATE, t, u, b->gate_chunk));
+      }
+      {
+        std::vector<PhaseTask> t;
+        std::vector<uint64_t> u;
+        for (size_t c = 0; c < nc; ++c)
+          for (auto& op : b->ops[c])
+            if (op.kind == R_PHASE && op.layer == L) {
+              t.push_back({b->base[c], tab_off[op.index], b->nq[c], (uint32_t)tab_split[op.index]});
+              u.push_back(1ull << b->nq[c]);
+            }
+        if (!t.empty()) b->rounds.push_back(b->make_round(R_PHASE, t, u, B_CHUNK));
+      }
+      for (int slot = 0;; ++slot) {
+        std::vector<SwapTask> t;
+        std::vector<uint64_t> u;
+        for (size_t c = 0; c < nc; ++c) {
+          int seen = 0;
+          for (auto& op : b->ops[c])
+            if (op.kind == R_SWAP && op.layer == L && seen++ == slot) {
+              t.push_back({b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb)});
+              u.push_back(1ull << (b->nq[c] - 2));
+            }
+        }
+        if (t.empty()) break;
+        b->rounds.push_back(b->make_round(R_SWAP, t, u, B_CHUNK));
+      }
+      if (period && (L + 1) % period == 0) {
+        std::vector<NormTask> t;
+        std::vector<uint64_t> u;
+        for (size_t c = 0; c < nc; ++c) {
+          int last = -1;
+          for (auto& op : b->ops[c]) last = std::max(last, op.layer);
+          if (last < L) continue;  // the circuit has ended
+          t.push_back({b->base[c], b->nq[c], (uint32_t)(b->nnorms++)});
+          u.push_back(1ull << b->nq[c]);
+        }
+        if (!t.empty()) {
+          b->rounds.push_back(b->make_round(R_NORM, t, u, B_CHUNK));
+          b->rounds.push_back(b->make_round(R_SCALE, t, u, B_CHUNK));
+        }
+      }
+    }
+    if (b->nnorms) {
+      void* p = nullptr;
+      check_cuda(cudaMalloc(&p, b->nnorms * sizeof(double)), "batch norms");
+      b->allocations.push_back(p);
+      b->norms = static_cast<double*>(p);
+    }
+    std::vector<uint64_t> where;
+    for (auto& qv : b->queries) where.push_back(b->base[qv.first] + qv.second);
+    b->query_where = b->upload(where);
+    if (!where.empty()) {
+      void* p = nullptr;
+      check_cuda(cudaMalloc(&p, where.size() * sizeof(double2)), "batch query results");
+      b->allocations.push_back(p);
+      b->query_out = static_cast<double2*>(p);
+    }
+    // autotune the gate kernel on the largest gate round (block size x chunk length)
+    cudaStream_t s = b->stream;
+    if (autotune) {
+      const Round* big = nullptr;
+      for (auto& r : b->rounds)
+        if (r.kind == R_GATE && (!big || r.ntasks > big->ntasks)) big = &r;
+      if (big) {
+        float best = 1e30f;
+        cudaEvent_t e0, e1;
+        check_cuda(cudaEventCreate(&e0), "event");
+        check_cuda(cudaEventCreate(&e1), "event");
+        for (int th : {128, 256, 512})
+          for (uint64_t ch : {256ull, 1024ull, 4096ull}) {
+            // the chunk offsets depend on the chunk length: a probe round per candidate
+            std::vector<GateTask> t(big->ntasks);
+            check_cuda(cudaMemcpy(t.data(), big->tasks, t.size() * sizeof(GateTask), cudaMemcpyDeviceToHost), "tune");
+            std::vector<uint64_t> u;
+            for (auto& x : t) u.push_back(1ull << (x.n - 2));
+            Round probe = b->make_round(R_GATE, t, u, ch);
+            b->launch(probe, s, th, ch);  // warm-up
+            check_cuda(cudaEventRecord(e0, s), "event");
+            for (int rep = 0; rep < 3; ++rep) b->launch(probe, s, th, ch);
+            check_cuda(cudaEventRecord(e1, s), "event");
+            check_cuda(cudaEventSynchronize(e1), "event");
+            float ms = 0;
+            check_cuda(cudaEventElapsedTime(&ms, e0, e1), "event");
+            if (ms < best) best = ms, b->gate_threads = th, b->gate_chunk = ch;
+          }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        // rebuild the gate rounds' chunk offsets for the chosen chunk length
+        for (auto& r : b->rounds)
+          if (r.kind == R_GATE) {
+            std::vector<GateTask> t(r.ntasks);
+            check_cuda(cudaMemcpy(t.data(), r.tasks, t.size() * sizeof(GateTask), cudaMemcpyDeviceToHost), "tune");
+            std::vector<uint64_t> u;
+            for (auto& x : t) u.push_back(1ull << (x.n - 2));
+            r = b->make_round(R_GATE, t, u, b->gate_chunk);
+          }
+      }
+    }
+    // capture the whole run as one graph
+    check_cuda(cudaStreamSynchronize(s), "batch synchronize");
+    check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    uint64_t n0 = g_launches.load();
+    check_cuda(cudaMemcpyAsync(b->psi, b->psi0, b->total_amps * sizeof(c64), cudaMemcpyDeviceToDevice, s), "reset");
+    if (b->nnorms) check_cuda(cudaMemsetAsync(b->norms, 0, b->nnorms * sizeof(double), s), "norm reset");
+    for (auto& r : b->rounds) b->launch(r, s, b->gate_threads, b->gate_chunk);
+    if (!where.empty()) {
+      b_query_kernel<<<grid_for((where.size() + 255) / 256, 4), 256, 0, s>>>(b->psi, b->query_where, where.size(),
+                                                                            b->query_out);
+      count_launch();
+    }
+    b->launches_per_run = g_launches.load() - n0;
+    g_launches.fetch_sub(b->launches_per_run);  // counted when the graph runs
+    check_cuda(cudaStreamEndCapture(s, &b->graph), "end capture");
+    check_cuda(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_run(qtnh_batch* b, void* stream) {
+  return guarded([&]() -> int {
+    checked(b);
+    if (!b->exec) throw Error(QTNH_ERR_RUNTIME, "batch not compiled");
+    // order against the caller's stream: caller -> batch stream -> caller
+    cudaEvent_t e;
+    check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    check_cuda(cudaEventRecord(e, (cudaStream_t)stream), "event record");
+    check_cuda(cudaStreamWaitEvent(b->stream, e, 0), "stream wait");
+    check_cuda(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+    check_cuda(cudaEventRecord(e, b->stream), "event record");
+    check_cuda(cudaStreamWaitEvent((cudaStream_t)stream, e, 0), "stream wait");
+    check_cuda(cudaEventDestroy(e), "event");
+    count_launch(b->launches_per_run);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_results(qtnh_batch* b, void* out_c128, uint64_t capacity, void* stream) {
+  return guarded([&]() -> int {
+    checked(b);
+    if (capacity < b->queries.size()) throw Error(QTNH_ERR_CAPACITY, "result buffer too small");
+    if (!b->queries.empty())
+      check_cuda(cudaMemcpyAsync(out_c128, b->query_out, b->queries.size() * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                 (cudaStream_t)stream),
+                 "batch results");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_info(qtnh_batch* b, uint64_t* amplitudes, uint64_t* rounds, uint64_t* launches_per_run,
+                    int32_t* gate_threads, uint64_t* gate_chunk) {
+  return guarded([&]() -> int {
+    checked(b);
+    if (amplitudes) *amplitudes = b->total_amps;
+    if (rounds) *rounds = b->rounds.size();
+    if (launches_per_run) *launches_per_run = b->launches_per_run;
+    if (gate_threads) *gate_threads = b->gate_threads;
+    if (gate_chunk) *gate_chunk = b->gate_chunk;
+    return QTNH_OK;
+  });
+}
+
+int qtnh_batch_state(qtnh_batch* b, int32_t c, void* out_c128, void* stream) {
+  return guarded([&]() -> int {
+    checked(b);
+    if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
+    const uint64_t n = 1ull << b->nq[c];
+    // complex64 -> complex128 through the query kernel over consecutive positions
+    std::vector<uint64_t> where(n);
+    for (uint64_t i = 0; i < n; ++i) where[i] = b->base[c] + i;
+    uint64_t* w = nullptr;
+    check_cuda(cudaMallocAsync((void**)&w, n * sizeof(uint64_t), (cudaStream_t)stream), "batch state");
+    check_cuda(cudaMemcpyAsync(w, where.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, (cudaStream_t)stream),
+               "batch state");
+    b_query_kernel<<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(b->psi, w, n,
+                                                                                   static_cast<double2*>(out_c128));
+    count_launch();
+    check_cuda(cudaFreeAsync(w, (cudaStream_t)stream), "batch state");
+    check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch state");
+    return QTNH_OK;
+  });
+}
+
+}  // extern "C"

@@ -138,3 +138,44 @@ def dense_pair(rng, max_elems=2 ** 26, mnk_range=(256, 16384), max_mnk=None):
             d2[p2[i]] = dim
         wires = [(p1[len(o1) + j], p2[j]) for j in range(ns)]
         return d1, d2, wires, M, N, K
+
+
+# ---- batched uneven circuits (many independent circuits, mixed precision) -------------
+
+def haar_unitaries(rng, count, d):
+    """`count` Haar-random d x d unitaries at once (stacked QR with the phase fix)."""
+    z = (rng.standard_normal((count, d, d)) + 1j * rng.standard_normal((count, d, d))) / math.sqrt(2.0)
+    qm, r = np.linalg.qr(z)
+    dr = np.diagonal(r, axis1=1, axis2=2)
+    return qm * (dr / np.abs(dr))[:, None, :]
+
+
+def batch_circuits(count, seed=2026, qubits=(10, 22), depth=(8, 32), diag_every=4, swap_prob=0.25, queries=64):
+    """`count` independent circuits: qubits uniform in [qubits], depth uniform in [depth];
+    every layer a seeded random pairing with one Haar two-qubit gate per pair, every
+    `diag_every`-th layer per-qubit phases, and with probability `swap_prob` a SwapTensor
+    exchange of two random qubits (as a permutation). Returns [(Circuit, query indices)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(qubits[0], qubits[1] + 1))
+        dep = int(rng.integers(depth[0], depth[1] + 1))
+        us = haar_unitaries(rng, dep * (n // 2), 4)
+        c = Circuit(n)
+        k = 0
+        for l in range(dep):
+            order = rng.permutation(n)
+            pairs = [(int(order[2 * j]), int(order[2 * j + 1])) for j in range(n // 2)]
+            gates = [np.ascontiguousarray(us[k + j].T).reshape(-1).astype(np.complex128) for j in range(len(pairs))]
+            k += len(pairs)
+            layer = Layer(pairs, gates)
+            if diag_every and (l + 1) % diag_every == 0:
+                layer.phases = rng.uniform(0.0, 2.0 * math.pi, n)
+            if rng.random() < swap_prob:
+                a, b = (int(x) for x in rng.choice(n, size=2, replace=False))
+                ptup = list(range(n))
+                ptup[a], ptup[b] = b, a
+                layer.ptup = ptup
+            c.layers.append(layer)
+        out.append((c, rng.integers(0, 2 ** n, size=queries, dtype=np.uint64)))
+    return out

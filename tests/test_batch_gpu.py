@@ -1,0 +1,117 @@
+"""Batched uneven circuits in mixed precision (qtnh_batch_*: complex64 states, grouped
+persistent kernels under one CUDA graph, FP64 renormalisation every 8 layers, complex128
+amplitude queries) against the oracle's complex128 circuit runner (the reference's
+contraction sequence) and against the GPU's plain FP64 path for a larger circuit.
+
+Error bar of the mixed-precision method: every pass over a state rounds each amplitude
+to complex64 once (~6e-8 relative), so a circuit of G passes drifts like sqrt(G) * 6e-8;
+asserted at 5e-6 relative L2 per circuit (queries and full states)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import qtnh_gb300 as q
+from oracle import oracle as orc
+from qtnh_gb300 import workload as wl
+
+pytestmark = pytest.mark.gpu
+BAR = 5e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _setup():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    orc.build()
+    q.lib()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128).reshape(-1)).cuda()
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.fixture(scope="module")
+def small_batch():
+    circuits = wl.batch_circuits(12, seed=77, qubits=(10, 14), depth=(8, 20))
+    b = q.Batch([c.n for c, _ in circuits])
+    states = []
+    for i, (c, qi) in enumerate(circuits):
+        psi = wl.random_state(c.n, seed=100 + i)
+        states.append(psi)
+        b.set_state(i, dev(psi))
+        b.add_circuit(i, c, qi)
+    b.compile(renorm_every=8, autotune=True)
+    b.run()
+    res = b.results().cpu().numpy()
+    refs = [orc.run_circuit(psi, c) for psi, (c, _) in zip(states, circuits)]
+    return circuits, b, res, refs
+
+
+def test_batch_queries_match_oracle(small_batch):
+    circuits, b, res, refs = small_batch
+    k = 0
+    for (c, qi), ref in zip(circuits, refs):
+        got = res[k:k + len(qi)]
+        k += len(qi)
+        assert rel(got, ref[qi.astype(np.int64)]) < BAR, c.n
+    info = b.info()
+    assert info["gate_threads"] in (128, 256, 512) and info["gate_chunk"] in (256, 1024, 4096)
+    assert info["launches_per_run"] >= info["rounds"]
+
+
+def test_batch_full_states_and_norm(small_batch):
+    circuits, b, _, refs = small_batch
+    for i in (0, 5, 11):
+        st = b.state(i).cpu().numpy()
+        assert rel(st, refs[i]) < BAR
+        assert abs(np.linalg.norm(st) - 1.0) < 1e-6
+
+
+def test_batch_graph_replay(small_batch):
+    circuits, b, res, _ = small_batch
+    b.run()  # the graph starts from the stored initial states every time
+    again = b.results().cpu().numpy()
+    assert rel(again, res) < 1e-12
+
+
+def test_batch_large_circuit_vs_fp64_engine():
+    from qtnh_gb300.circuit import DeviceCircuit
+    (c, qi), = wl.batch_circuits(1, seed=5, qubits=(20, 20), depth=(12, 12))
+    psi = wl.random_state(c.n, seed=6)
+    b = q.Batch([c.n])
+    b.set_state(0, dev(psi))
+    b.add_circuit(0, c, qi)
+    b.compile(renorm_every=8, autotune=False)
+    b.run()
+    got = b.state(0).cpu().numpy()
+    old = q.get_arithmetic()
+    q.set_arithmetic(q.ARITH_FP64)
+    try:
+        st = dev(psi)
+        out = DeviceCircuit(c).run(st, torch.empty_like(st))
+        torch.cuda.synchronize()
+        ref = out.cpu().numpy()
+    finally:
+        q.set_arithmetic(old)
+    assert rel(got, ref) < BAR
+    assert rel(b.results().cpu().numpy(), ref[qi.astype(np.int64)]) < BAR
+
+
+def test_batch_rejects_invalid_operations():
+    b = q.Batch([10, 12])
+    eye = np.eye(4, dtype=np.complex128).reshape(-1)
+    c = wl.Circuit(10)
+    c.layers.append(wl.Layer([(0, 1)], [eye]))
+    with pytest.raises(q.QtnhError):
+        b.add_circuit(2, c)  # no circuit 2
+    c = wl.Circuit(10)
+    c.layers.append(wl.Layer([(3, 3)], [eye]))
+    with pytest.raises(q.QtnhError):
+        b.add_circuit(0, c)  # a gate on one qubit twice
+    with pytest.raises(q.QtnhError):
+        b.add_circuit(1, wl.Circuit(12), queries=[2 ** 12])
