@@ -60,10 +60,12 @@ def _args():
     p.add_argument("--arith", default="bf16x6", choices=["bf16x6", "f32x2", "fp64"],
                    help="arithmetic of the gate/diagonal kernels (storage is complex128 either way)")
     p.add_argument("--no-arith-check", action="store_true")
-    p.add_argument("--workload", default="circuit", choices=["circuit", "contract", "batch"],
+    p.add_argument("--workload", default="circuit", choices=["circuit", "contract", "batch", "serve"],
                    help="circuit: the n=28 random layered circuit (headline); contract: 64 seeded dense "
                         "contraction pairs, split-precision BF16x3 GEMM vs FP64 plain (precision study); batch: "
-                        "2048 uneven circuits in mixed precision under one CUDA graph")
+                        "2048 uneven circuits in mixed precision under one CUDA graph; serve: a Poisson request "
+                        "stream through the request loop, plain complex128 vs mixed complex64")
+    p.add_argument("--requests", type=int, default=400)
     p.add_argument("--circuits", type=int, default=2048)
     p.add_argument("--pairs", type=int, default=64)
     return p.parse_args()
@@ -606,8 +608,78 @@ def main_batch(a):
         dist.destroy_process_group()
 
 
+# ---- request loop ---------------------------------------------------------------------
+
+SERVE_METRIC = "serving p99 latency (mixed complex64; p50, throughput and plain complex128 beside it)"
+
+
+def main_serve(a):
+    import numpy as np
+    import torch
+    import qtnh_gb300 as q
+    from qtnh_gb300 import serve
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        spl = _cpu_sample(CPU_SAMPLE_N, CPU_SAMPLE_LAYERS, a.seed)
+        cpu = {"value": 1.0 / _extrapolate(spl, CPU_SAMPLE_N, 16), "unit": "gate-layers/s", "cores": 1, "kind": "port",
+               "sample": "oracle port (scalar C++), %d layers of a random circuit at n=%d on one core, scaled to "
+                         "n=16" % (CPU_SAMPLE_LAYERS, CPU_SAMPLE_N)}
+    reqs = serve.request_stream(a.requests, rate=400.0, seed=a.seed)
+    warm = serve.request_stream(4, rate=4000.0, seed=a.seed + 99, qubits=(12, 16), depth=(10, 12))
+    out = {}
+    for name, prec in (("mixed", serve.C64), ("plain", serve.C128)):
+        ex = serve.GpuExecutor(prec)
+        serve.serve(warm, ex, renorm_every=8 if prec == serve.C64 else 0)
+        torch.cuda.synchronize()
+        clocks = _Clocks(local)
+        clocks.start()
+        l0 = q.launches()
+        lat, results, stats = serve.serve(reqs, ex, budget_bytes=150e9, renorm_every=8 if prec == serve.C64 else 0)
+        stats["clocks"] = clocks.stop()
+        stats["gpu_launches"] = q.launches() - l0
+        out[name] = (stats, results)
+    errs = []
+    for r in reqs:
+        a_, b_ = np.asarray(out["mixed"][1][r.rid]), np.asarray(out["plain"][1][r.rid])
+        errs.append(float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_)))
+    ms, ps = out["mixed"][0], out["plain"][0]
+    if rank == 0:
+        gate_bytes = sum(16 * 16 * len(layer.gates) for r in reqs for layer in r.circuit.layers)
+        answer_bytes = sum(16 * (256 if r.kind == "amps" else 256) for r in reqs)
+        line = {
+            "metric": SERVE_METRIC, "value": ms["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": ms["steps"],
+            "warmup": 1, "ms_per_step": ms["makespan_s"] * 1e3 / max(1, ms["steps"]), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 (mixed) vs c128 (plain)",
+            "data": "synthetic (seeded Poisson request stream, seeded circuits and states)",
+            "config": {"workload": "%d requests, Poisson arrivals at 400/s, qubits log-uniform 12..26, depth 10..60, "
+                                   "Haar two-qubit gates, phase layer every 4th, qubit exchange every 8th layer, "
+                                   "256 amplitudes or a 4-qubit reduced density matrix each; 150 GB admission budget; "
+                                   "all active requests advance one layer per grouped step" % len(reqs),
+                       "requests": len(reqs), "rate_per_s": 400.0, "budget_bytes": 150e9,
+                       "parallelism": "single GPU"},
+            "mixed": {k: ms[k] for k in ("p50_ms", "p99_ms", "mean_ms", "requests_per_s", "gate_layers_per_s",
+                                         "makespan_s", "steps")},
+            "plain": {k: ps[k] for k in ("p50_ms", "p99_ms", "mean_ms", "requests_per_s", "gate_layers_per_s",
+                                         "makespan_s", "steps")},
+            "error_mixed_vs_plain": {"rel_max": max(errs), "rel_median": statistics.median(errs)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": ms["p99_ms"], "unit": "ms", "h2d_bytes_per_step": gate_bytes / max(1, ms["steps"]),
+                    "d2h_bytes_per_step": answer_bytes / max(1, ms["steps"])},
+            "clocks": ms["clocks"],
+            "gpu_launches": ms["gpu_launches"],
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
+    if a.workload == "serve":
+        main_serve(a)
+        return
     if a.workload == "batch":
         if a.impl == "reference":
             a.n = 16

@@ -239,6 +239,35 @@ int qtnh_apply_diag_layer(void* state, int32_t rank, const uint64_t* dims, int32
 /* sum |x|^2 over n elements, computed in FP64 on the device; result to host. Synchronous. */
 int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream);
 
+/* ---- grouped operations on many resident states (request loops) ---------------------- */
+
+/* State precision: plain complex128 (FP64 arithmetic) or mixed complex64 (FP32
+ * arithmetic, gates held as complex64 hi + lo; FP64 norms and sums). */
+enum { QTNH_STATE_C128 = 0, QTNH_STATE_C64 = 1 };
+
+/* The next layer of each of `nstates` device states (states[i], nqubits[i] qubits,
+ * qubit q = bit n - 1 - q): ngates[i] two-qubit SymmTensor gates (pairs: concatenated
+ * (qa, qb) per gate, input 0 on qa; gates_c128: host, 16 complex128 per gate in
+ * SymmTensor layout, include/tensor/symm.hpp:22-45), then if has_phases[i] a phase
+ * DiagTensor on every qubit (phases: host, concatenated nqubits[i] per such state), then
+ * if swaps[2i] != 0xFFFF the exchange of qubits swaps[2i], swaps[2i+1]. Gates of one
+ * state must be disjoint. Grouped launches: one per gate slot, one for the phases, one
+ * for the swaps. has_phases, phases and swaps may be null. */
+int qtnh_group_layer(int32_t precision, int32_t nstates, void* const* states, const int32_t* nqubits,
+                     const int32_t* ngates, const uint16_t* pairs, const void* gates_c128, const uint8_t* has_phases,
+                     const double* phases, const uint16_t* swaps, void* stream);
+/* Renormalise each state to unit L2 norm (FP64 norm). */
+int qtnh_group_renorm(int32_t precision, int32_t nstates, void* const* states, const int32_t* nqubits, void* stream);
+/* out_c128[i] = state[idx[i]] (idx: host; out: device complex128). */
+int qtnh_gather(int32_t precision, const void* state, int32_t nqubits, int32_t nidx, const uint64_t* idx,
+                void* out_c128, void* stream);
+/* Reduced density matrix of qubits[0..3] (host): out_c128 (device, 16 x 16 complex128,
+ * row-major, index bits q0 q1 q2 q3) = sum over the other qubits of psi psi^*, in FP64. */
+int qtnh_rdm4(int32_t precision, const void* state, int32_t nqubits, const uint16_t* qubits, void* out_c128,
+              void* stream);
+/* n amplitudes complex128 -> complex64 (to_precision QTNH_STATE_C64) or back. */
+int qtnh_state_convert(int32_t to_precision, const void* in, void* out, uint64_t n, void* stream);
+
 /* ---- batched circuits in mixed precision ------------------------------------------- */
 
 /* Many independent circuits of uneven qubit counts and depths, complex64 states resident

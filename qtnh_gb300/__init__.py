@@ -347,3 +347,78 @@ class Batch:
                                     ctypes.byref(th), ctypes.byref(chunk)))
         return {"amplitudes": amps.value, "rounds": rounds.value, "launches_per_run": lpr.value,
                 "gate_threads": th.value, "gate_chunk": chunk.value}
+
+
+# ---- grouped operations on many resident states (request loops) ------------------------
+
+STATE_C128, STATE_C64 = 0, 1
+
+
+def _check_state(t, precision):
+    import torch
+    want = torch.complex128 if precision == STATE_C128 else torch.complex64
+    if t.dtype != want or not t.is_cuda or not t.is_contiguous():
+        raise TypeError("expected a contiguous %s CUDA tensor" % want)
+
+
+def state_convert(to_precision, src, dst, stream=None):
+    """complex128 -> complex64 (to_precision STATE_C64) or back, n = src.numel()."""
+    check(lib().qtnh_state_convert(ctypes.c_int32(to_precision), _ptr(src), _ptr(dst), ctypes.c_uint64(src.numel()),
+                                   _stream(stream)))
+    return dst
+
+
+def group_layer(precision, items, stream=None):
+    """items: [(state, n, pairs, gates, phases or None, swap (qa, qb) or None)] -> the layer
+    applied to every state in grouped launches (qtnh_group_layer)."""
+    import numpy as np
+    ns = len(items)
+    if ns == 0:
+        return
+    for it in items:
+        _check_state(it[0], precision)
+    states = (ctypes.c_void_p * ns)(*[it[0].data_ptr() for it in items])
+    nq = (ctypes.c_int32 * ns)(*[int(it[1]) for it in items])
+    ng = (ctypes.c_int32 * ns)(*[len(it[2]) for it in items])
+    pairs = _u16([x for it in items for p in it[2] for x in p])
+    gl = [np.asarray(g, dtype=np.complex128).reshape(16) for it in items for g in it[3]]
+    gates = np.ascontiguousarray(np.concatenate(gl) if gl else np.zeros(16, np.complex128))
+    hp = (ctypes.c_uint8 * ns)(*[0 if it[4] is None else 1 for it in items])
+    pl = [np.asarray(it[4], dtype=np.float64) for it in items if it[4] is not None]
+    phases = np.ascontiguousarray(np.concatenate(pl) if pl else np.zeros(1))
+    sw = _u16([x for it in items for x in (it[5] if it[5] is not None else (0xFFFF, 0xFFFF))])
+    check(lib().qtnh_group_layer(ctypes.c_int32(precision), ctypes.c_int32(ns), states, nq, ng, pairs,
+                                 ctypes.c_void_p(gates.ctypes.data), hp,
+                                 phases.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sw, _stream(stream)))
+
+
+def group_renorm(precision, items, stream=None):
+    """items: [(state, n)] -> every state scaled to unit L2 norm (FP64 norms)."""
+    ns = len(items)
+    if ns == 0:
+        return
+    states = (ctypes.c_void_p * ns)(*[it[0].data_ptr() for it in items])
+    nq = (ctypes.c_int32 * ns)(*[int(it[1]) for it in items])
+    check(lib().qtnh_group_renorm(ctypes.c_int32(precision), ctypes.c_int32(ns), states, nq, _stream(stream)))
+
+
+def gather(precision, state, n, idx, stream=None):
+    """Amplitudes state[idx] as a complex128 CUDA tensor."""
+    import numpy as np
+    import torch
+    _check_state(state, precision)
+    ix = np.ascontiguousarray(idx, dtype=np.uint64)
+    out = torch.empty(max(1, len(ix)), dtype=torch.complex128, device="cuda")
+    check(lib().qtnh_gather(ctypes.c_int32(precision), _ptr(state), ctypes.c_int32(n), ctypes.c_int32(len(ix)),
+                            ix.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _ptr(out), _stream(stream)))
+    return out[:len(ix)]
+
+
+def rdm4(precision, state, n, qubits, stream=None):
+    """16 x 16 reduced density matrix of 4 qubits (complex128 CUDA tensor, FP64 sums)."""
+    import torch
+    _check_state(state, precision)
+    out = torch.empty(256, dtype=torch.complex128, device="cuda")
+    check(lib().qtnh_rdm4(ctypes.c_int32(precision), _ptr(state), ctypes.c_int32(n), _u16(qubits), _ptr(out),
+                          _stream(stream)))
+    return out.reshape(16, 16)

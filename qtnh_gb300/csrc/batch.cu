@@ -31,8 +31,7 @@
 #include <memory>
 #include <vector>
 
-#include "cuda_common.cuh"
-#include "df32.cuh"
+#include "group_kernels.cuh"
 
 struct qtnh_batch;
 
@@ -41,27 +40,12 @@ namespace qtnh_impl {
 namespace {
 
 using c64 = float2;
+using grp::GateTask;
+using grp::NormTask;
+using grp::PhaseTask;
+using grp::SwapTask;
 
-struct GateTask {
-  uint64_t base;  // first amplitude of the circuit's state
-  uint32_t n;     // qubits
-  uint32_t ba, bb;  // bit positions of gate inputs 0 and 1
-  uint32_t gate;    // index into the gate table (32 c64: U_hi[16], U_lo[16], U[out * 4 + in])
-};
-struct PhaseTask {
-  uint64_t base, table;  // state offset, offset of the lo table (hi table follows, 2^(n - split))
-  uint32_t n, split;
-};
-struct SwapTask {
-  uint64_t base;
-  uint32_t n, ba, bb;
-};
-struct NormTask {
-  uint64_t base;
-  uint32_t n, slot;  // slot into the norm array
-};
-
-enum RoundKind { R_GATE = 0, R_PHASE = 1, R_SWAP = 2, R_NORM = 3, R_SCALE = 4 };
+enum RoundKind { R_GATE = grp::GATE, R_PHASE = grp::PHASE, R_SWAP = grp::SWAP, R_NORM = grp::NORM, R_SCALE = grp::SCALE };
 
 struct Round {
   int kind;
@@ -71,172 +55,6 @@ struct Round {
   uint64_t* cbeg = nullptr; // device chunk offsets (ntasks)
   uint64_t elems_per_chunk = 0;
 };
-
-__device__ __forceinline__ uint32_t find_task(const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t w) {
-  uint32_t lo = 0, hi = ntasks;
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (cbeg[mid] <= w)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
-
-__device__ __forceinline__ uint64_t insert_zero(uint64_t x, uint32_t bit) {
-  return ((x >> bit) << (bit + 1)) | (x & ((1ull << bit) - 1));
-}
-
-__device__ __forceinline__ void cmac(float2 u, float2 x, float& re, float& im) {
-  re = fmaf(u.x, x.x, re);
-  re = fmaf(-u.y, x.y, re);
-  im = fmaf(u.x, x.y, im);
-  im = fmaf(u.y, x.x, im);
-}
-
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) b_gate_kernel(c64* __restrict__ psi, const GateTask* __restrict__ tasks,
-                                                         const uint64_t* __restrict__ cbeg, uint32_t ntasks,
-                                                         uint64_t total, const c64* __restrict__ gates,
-                                                         uint64_t chunk_groups) {
-  __shared__ c64 g[32];
-  __shared__ uint32_t s_task;
-  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
-    __syncthreads();
-    const GateTask t = tasks[s_task];
-    if (threadIdx.x < 32) g[threadIdx.x] = gates[(uint64_t)t.gate * 32 + threadIdx.x];
-    __syncthreads();
-    const uint64_t ngroups = 1ull << (t.n - 2);
-    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
-    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
-    const uint32_t lo = min(t.ba, t.bb), hi = max(t.ba, t.bb);
-    const uint64_t sa = 1ull << t.ba, sb = 1ull << t.bb;
-    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
-      const uint64_t x0 = t.base + insert_zero(insert_zero(grp, lo), hi);
-      const uint64_t off[4] = {0, sb, sa, sa + sb};  // (input 0, input 1) = (0,0), (0,1), (1,0), (1,1)
-      c64 x[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) x[i] = psi[x0 + off[i]];
-#pragma unroll
-      for (int o = 0; o < 4; ++o) {
-        float re = 0.0f, im = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) cmac(g[16 + o * 4 + i], x[i], re, im);  // U_lo first (smaller terms)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) cmac(g[o * 4 + i], x[i], re, im);
-        psi[x0 + off[o]] = make_float2(re, im);
-      }
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void b_phase_kernel(c64* __restrict__ psi, const PhaseTask* __restrict__ tasks,
-                               const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total,
-                               const c64* __restrict__ tables, uint64_t chunk) {
-  __shared__ uint32_t s_task;
-  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
-    __syncthreads();
-    const PhaseTask t = tasks[s_task];
-    const uint64_t nel = 1ull << t.n;
-    const uint64_t e0 = (w - cbeg[s_task]) * chunk, e1 = min(e0 + chunk, nel);
-    const c64* tlo = tables + t.table;
-    const c64* thi = tlo + (1ull << t.split);
-    const uint64_t mask = (1ull << t.split) - 1;
-    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const c64 a = tlo[e & mask], b = thi[e >> t.split];
-      const c64 f = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-      const c64 x = psi[t.base + e];
-      psi[t.base + e] = make_float2(f.x * x.x - f.y * x.y, f.x * x.y + f.y * x.x);
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void b_swap_kernel(c64* __restrict__ psi, const SwapTask* __restrict__ tasks,
-                              const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total, uint64_t chunk) {
-  __shared__ uint32_t s_task;
-  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
-    __syncthreads();
-    const SwapTask t = tasks[s_task];
-    const uint64_t npairs = 1ull << (t.n - 2);
-    const uint64_t p0 = (w - cbeg[s_task]) * chunk, p1 = min(p0 + chunk, npairs);
-    const uint32_t lo = min(t.ba, t.bb), hi = max(t.ba, t.bb);
-    for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-      const uint64_t x = t.base + insert_zero(insert_zero(p, lo), hi);
-      const uint64_t xa = x + (1ull << t.ba), xb = x + (1ull << t.bb);
-      const c64 va = psi[xa], vb = psi[xb];
-      psi[xa] = vb;
-      psi[xb] = va;
-    }
-    __syncthreads();
-  }
-}
-
-// Sum of |psi|^2 per task into norms[slot]: compensated FP32 per thread, FP64 across.
-__global__ void b_norm_kernel(const c64* __restrict__ psi, const NormTask* __restrict__ tasks,
-                              const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total, uint64_t chunk,
-                              double* __restrict__ norms) {
-  __shared__ uint32_t s_task;
-  __shared__ double s_part[32];
-  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
-    __syncthreads();
-    const NormTask t = tasks[s_task];
-    const uint64_t nel = 1ull << t.n;
-    const uint64_t e0 = (w - cbeg[s_task]) * chunk, e1 = min(e0 + chunk, nel);
-    float s = 0.0f, c = 0.0f;
-    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const c64 x = psi[t.base + e];
-      float ns, err;
-      df::two_sum(s, fmaf(x.x, x.x, x.y * x.y), ns, err);
-      s = ns;
-      c += err;
-    }
-    double v = (double)s + (double)c;
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double tot = 0;
-      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) tot += s_part[i];
-      atomicAdd(&norms[t.slot], tot);
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void b_scale_kernel(c64* __restrict__ psi, const NormTask* __restrict__ tasks,
-                               const uint64_t* __restrict__ cbeg, uint32_t ntasks, uint64_t total, uint64_t chunk,
-                               const double* __restrict__ norms) {
-  __shared__ uint32_t s_task;
-  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
-    __syncthreads();
-    const NormTask t = tasks[s_task];
-    const double nrm = norms[t.slot];
-    const float f = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 1.0f;
-    const uint64_t nel = 1ull << t.n;
-    const uint64_t e0 = (w - cbeg[s_task]) * chunk, e1 = min(e0 + chunk, nel);
-    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const c64 x = psi[t.base + e];
-      psi[t.base + e] = make_float2(x.x * f, x.y * f);
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void b_query_kernel(const c64* __restrict__ psi, const uint64_t* __restrict__ where, uint64_t nq,
-                               double2* __restrict__ out) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (uint64_t)gridDim.x * blockDim.x) {
-    const c64 x = psi[where[i]];
-    out[i] = make_double2((double)x.x, (double)x.y);
-  }
-}
 
 __global__ void b_to_c64_kernel(const double2* __restrict__ in, c64* __restrict__ out, uint64_t n) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
@@ -333,28 +151,28 @@ struct qtnh_batch {
         const auto* t = static_cast<const GateTask*>(r.tasks);
         const int g = grid(r.total, gthreads);
         if (gthreads == 128)
-          b_gate_kernel<128><<<g, 128, 0, s>>>(psi, t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+          grp::gate_kernel<c64, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gates, gchunk);
         else if (gthreads == 512)
-          b_gate_kernel<512><<<g, 512, 0, s>>>(psi, t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+          grp::gate_kernel<c64, 512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gates, gchunk);
         else
-          b_gate_kernel<256><<<g, 256, 0, s>>>(psi, t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+          grp::gate_kernel<c64, 256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gates, gchunk);
         break;
       }
       case R_PHASE:
-        b_phase_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const PhaseTask*>(r.tasks), r.cbeg,
-                                                          r.ntasks, r.total, tables, r.elems_per_chunk);
+        grp::phase_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const PhaseTask*>(r.tasks), r.cbeg,
+                                                                  r.ntasks, r.total, tables, r.elems_per_chunk);
         break;
       case R_SWAP:
-        b_swap_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const SwapTask*>(r.tasks), r.cbeg, r.ntasks,
-                                                         r.total, r.elems_per_chunk);
+        grp::swap_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const SwapTask*>(r.tasks), r.cbeg,
+                                                                 r.ntasks, r.total, r.elems_per_chunk);
         break;
       case R_NORM:
-        b_norm_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const NormTask*>(r.tasks), r.cbeg, r.ntasks,
-                                                         r.total, r.elems_per_chunk, norms);
+        grp::norm_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const NormTask*>(r.tasks), r.cbeg,
+                                                                 r.ntasks, r.total, r.elems_per_chunk, norms);
         break;
       case R_SCALE:
-        b_scale_kernel<<<grid(r.total, 256), 256, 0, s>>>(psi, static_cast<const NormTask*>(r.tasks), r.cbeg,
-                                                          r.ntasks, r.total, r.elems_per_chunk, norms);
+        grp::scale_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const NormTask*>(r.tasks), r.cbeg,
+                                                                  r.ntasks, r.total, r.elems_per_chunk, norms);
         break;
     }
     count_launch();
@@ -531,7 +349,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           int seen = 0;
           for (auto& op : b->ops[c])
             if (op.kind == R_GATE && op.layer == L && seen++ == slot) {
-              t.push_back({b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb), op.index});
+              t.push_back({b->psi + b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb), op.index});
               u.push_back(1ull << (b->nq[c] - 2));
             }
         }
@@ -544,7 +362,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
         for (size_t c = 0; c < nc; ++c)
           for (auto& op : b->ops[c])
             if (op.kind == R_PHASE && op.layer == L) {
-              t.push_back({b->base[c], tab_off[op.index], b->nq[c], (uint32_t)tab_split[op.index]});
+              t.push_back({b->psi + b->base[c], tab_off[op.index], b->nq[c], (uint32_t)tab_split[op.index]});
               u.push_back(1ull << b->nq[c]);
             }
         if (!t.empty()) b->rounds.push_back(b->make_round(R_PHASE, t, u, B_CHUNK));
@@ -556,7 +374,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           int seen = 0;
           for (auto& op : b->ops[c])
             if (op.kind == R_SWAP && op.layer == L && seen++ == slot) {
-              t.push_back({b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb)});
+              t.push_back({b->psi + b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb)});
               u.push_back(1ull << (b->nq[c] - 2));
             }
         }
@@ -570,7 +388,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           int last = -1;
           for (auto& op : b->ops[c]) last = std::max(last, op.layer);
           if (last < L) continue;  // the circuit has ended
-          t.push_back({b->base[c], b->nq[c], (uint32_t)(b->nnorms++)});
+          t.push_back({b->psi + b->base[c], b->nq[c], (uint32_t)(b->nnorms++)});
           u.push_back(1ull << b->nq[c]);
         }
         if (!t.empty()) {
@@ -643,8 +461,8 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
     if (b->nnorms) check_cuda(cudaMemsetAsync(b->norms, 0, b->nnorms * sizeof(double), s), "norm reset");
     for (auto& r : b->rounds) b->launch(r, s, b->gate_threads, b->gate_chunk);
     if (!where.empty()) {
-      b_query_kernel<<<grid_for((where.size() + 255) / 256, 4), 256, 0, s>>>(b->psi, b->query_where, where.size(),
-                                                                            b->query_out);
+      grp::gather_kernel<c64><<<grid_for((where.size() + 255) / 256, 4), 256, 0, s>>>(b->psi, b->query_where,
+                                                                                     where.size(), b->query_out);
       count_launch();
     }
     b->launches_per_run = g_launches.load() - n0;
@@ -710,8 +528,8 @@ int qtnh_batch_state(qtnh_batch* b, int32_t c, void* out_c128, void* stream) {
     check_cuda(cudaMallocAsync((void**)&w, n * sizeof(uint64_t), (cudaStream_t)stream), "batch state");
     check_cuda(cudaMemcpyAsync(w, where.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, (cudaStream_t)stream),
                "batch state");
-    b_query_kernel<<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(b->psi, w, n,
-                                                                                   static_cast<double2*>(out_c128));
+    grp::gather_kernel<c64><<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(
+        b->psi, w, n, static_cast<double2*>(out_c128));
     count_launch();
     check_cuda(cudaFreeAsync(w, (cudaStream_t)stream), "batch state");
     check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch state");

@@ -1,0 +1,51 @@
+"""The request loop on the GPU (grouped layer steps over resident states, FP64
+renormalisation, amplitude and reduced-density-matrix answers) in plain complex128 and
+mixed complex64, against the oracle's complex128 contraction sequence of every
+request: plain within 1e-12 relative, mixed within the batched-circuit bar 5e-6."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import qtnh_gb300 as q
+from oracle import oracle as orc
+from qtnh_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _setup():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    orc.build()
+    q.lib()
+
+
+def reference(req):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(req.seed)
+    psi = torch.randn(2 ** req.circuit.n, dtype=torch.complex128, device="cuda", generator=g)
+    psi = (psi / torch.linalg.vector_norm(psi)).cpu().numpy()
+    fin = orc.run_circuit(psi, req.circuit)
+    n = req.circuit.n
+    if req.kind == "amps":
+        return fin[req.query.astype(np.int64)]
+    qs = [int(x) for x in req.query]
+    rest = [i for i in range(n) if i not in qs]
+    m = fin.reshape([2] * n).transpose(qs + rest).reshape(16, -1)
+    return m @ m.conj().T
+
+
+@pytest.mark.parametrize("precision,bar", [(serve.C128, 1e-12), (serve.C64, 5e-6)], ids=["plain", "mixed"])
+def test_serve_answers_match_oracle(precision, bar):
+    reqs = serve.request_stream(14, rate=4000.0, seed=11, qubits=(10, 14), depth=(10, 18))
+    ex = serve.GpuExecutor(precision)
+    lat, results, stats = serve.serve(reqs, ex, budget_bytes=4 * 2 ** 20,
+                                      renorm_every=8 if precision == serve.C64 else 0, realtime=False)
+    assert stats["requests"] == len(reqs)
+    for r in reqs:
+        got, ref = np.asarray(results[r.rid]), reference(r)
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err < bar, (r.rid, r.kind, r.circuit.n, err)
+    assert q.take_device_errors() == 0
