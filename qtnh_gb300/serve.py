@@ -5,10 +5,12 @@ the headline workload (Haar two-qubit SymmTensor gates on a random pairing per l
 phase DiagTensor layer every 4th layer, every 8th layer an exchange of a top qubit with a
 random other one) and asks for 256 amplitudes or the reduced density matrix of 4 qubits.
 The loop admits arrived requests in order while their states fit an HBM budget, keeps
-every admitted state resident, and advances all of them together: one step applies the
-next layer of every active request through one grouped call (qtnh_group_layer), complex64
-states are renormalised in FP64 every 8 layers, and finished requests are answered
-(qtnh_gather / qtnh_rdm4, FP64 sums) and freed. Latency is arrival to completion on the
+every admitted state resident, and advances all of them together in work-balanced steps:
+the largest active request advances one layer per step, and every other one as many
+layers as fit in the same amplitude-pass budget (2^n x gates per layer), each round of
+layers one grouped call (qtnh_group_layer) over the requests still taking layers;
+complex64 states are renormalised in FP64 every 8 layers, and finished requests are
+answered (qtnh_gather / qtnh_rdm4, FP64 sums) and freed. Latency is arrival to completion on the
 wall clock, the GPU work of a step synchronised before completions are stamped.
 
 The executor is a parameter (GpuExecutor drives the C ABI), so the scheduling logic can
@@ -151,15 +153,21 @@ def serve(requests, executor, budget_bytes=150e9, renorm_every=8, realtime=True,
             else:
                 vclock = pending[0].arrival
             continue
-        executor.step([(st, r.circuit, li) for r, st, li in active])
-        layers_done += len(active)
+        # layers per request this step: the largest per-layer work sets the step's budget
+        work = [2 ** r.circuit.n * max(1, r.circuit.n // 2) for r, _, _ in active]
+        budget = max(work)
+        take = [max(1, min(budget // w, len(a[0].circuit.layers) - a[2])) for a, w in zip(active, work)]
+        for j in range(max(take)):
+            part = [a for a, k in zip(active, take) if k > j]
+            executor.step([(st, r.circuit, li) for r, st, li in part])
+            layers_done += len(part)
+            for a in part:
+                a[2] += 1
+            if renorm_every:
+                due = [(st, r.circuit) for r, st, li in part if li % renorm_every == 0 and li < len(r.circuit.layers)]
+                if due:
+                    executor.renorm(due)
         steps += 1
-        for a in active:
-            a[2] += 1
-        if renorm_every:
-            due = [(st, r.circuit) for r, st, li in active if li % renorm_every == 0 and li < len(r.circuit.layers)]
-            if due:
-                executor.renorm(due)
         finished = [a for a in active if a[2] == len(a[0].circuit.layers)]
         outs = [(a[0], executor.answer(a[1], a[0])) for a in finished]
         executor.sync()
