@@ -47,6 +47,16 @@ CPU_SAMPLE_N = 20
 CPU_SAMPLE_LAYERS = 4
 
 
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time (every rank gets it); ms unchanged without a process group."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -765,11 +775,7 @@ def main():
     barrier()
     ck = clocks.stop()
     launches = q.launches() - l0
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     ms_per_step = ms / a.steps
     value = world * a.depth * a.steps / (ms / 1e3)
 
