@@ -70,11 +70,12 @@ def _args():
     p.add_argument("--arith", default="bf16x6", choices=["bf16x6", "f32x2", "fp64"],
                    help="arithmetic of the gate/diagonal kernels (storage is complex128 either way)")
     p.add_argument("--no-arith-check", action="store_true")
-    p.add_argument("--workload", default="circuit", choices=["circuit", "contract", "batch", "serve"],
+    p.add_argument("--workload", default="circuit", choices=["circuit", "contract", "batch", "serve", "kernels"],
                    help="circuit: the n=28 random layered circuit (headline); contract: 64 seeded dense "
                         "contraction pairs, split-precision BF16x3 GEMM vs FP64 plain (precision study); batch: "
                         "2048 uneven circuits in mixed precision under one CUDA graph; serve: a Poisson request "
-                        "stream through the request loop, plain complex128 vs mixed complex64")
+                        "stream through the request loop, plain complex128 vs mixed complex64; kernels: the "
+                        "plain path's permute, diag, gate and norm kernels one by one (HBM fractions)")
     p.add_argument("--requests", type=int, default=400)
     p.add_argument("--circuits", type=int, default=2048)
     p.add_argument("--pairs", type=int, default=64)
@@ -469,6 +470,24 @@ def _batch_bytes(circuits):
     return tot
 
 
+def _state_errors(got, ref):
+    """Relative L2, largest amplitude error (relative to the largest amplitude) and fidelity
+    |<ref|got>|^2 / (|ref|^2 |got|^2) of a state against its FP64 reference."""
+    import numpy as np
+    nr, ng = np.vdot(ref, ref).real, np.vdot(got, got).real
+    return {"rel_l2": float(np.linalg.norm(got - ref) / np.sqrt(nr)),
+            "max_abs": float(np.max(np.abs(got - ref)) / np.max(np.abs(ref))),
+            "fidelity": float(abs(np.vdot(ref, got)) ** 2 / (nr * ng))}
+
+
+def _worst_state_errors(errs):
+    if not errs:
+        return None
+    return {"rel_l2_max": max(e["rel_l2"] for e in errs), "max_abs_max": max(e["max_abs"] for e in errs),
+            "fidelity_min": min(e["fidelity"] for e in errs), "one_minus_fidelity_max":
+            max(1.0 - e["fidelity"] for e in errs)}
+
+
 def main_batch(a):
     import numpy as np
     import torch
@@ -538,7 +557,7 @@ def main_batch(a):
     res = b.results().cpu().numpy()
 
     # error against FP64 on the smaller circuits (oracle port, host)
-    errs = []
+    errs, state_errs = [], []
     if rank == 0:
         from oracle import oracle as orc
         orc.build()
@@ -553,9 +572,12 @@ def main_batch(a):
                 inits[i] = (psi / torch.linalg.vector_norm(psi)).cpu().numpy()
         for i in small:
             c, qi = circuits[i]
-            ref = orc.run_circuit(inits[i], c)[qi.astype(np.int64)]
+            full = orc.run_circuit(inits[i], c)
+            ref = full[qi.astype(np.int64)]
             got = res[off[i]:off[i + 1]]
             errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+            st = b.state(i).cpu().numpy()
+            state_errs.append(_state_errors(st, full))
 
     # e2e: initial states from pinned host memory (complex128), results back to the host
     host_init = []
@@ -583,6 +605,39 @@ def main_batch(a):
     e2e = world * layers / (ems / a.steps * 1e-3)
     h2d = sum(16 * h.numel() for h in host_init)
 
+    # the plain method on the same circuits and schedule (complex128 states, FP64 math, no
+    # renormalisation): the reference point of the mixed-precision speed-up, and the FP64
+    # states the mixed states are compared with (all queries; full states of the largest
+    # circuits). One warm-up and one timed run: it is several times slower.
+    bp = q.Batch([c.n for c, _ in circuits], precision=q.STATE_C128)
+    g4 = torch.Generator(device=dev)
+    g4.manual_seed(a.seed + 1)
+    for i, (c, qi) in enumerate(circuits):
+        psi = torch.randn(2 ** c.n, dtype=torch.complex128, device=dev, generator=g4)
+        bp.set_state(i, psi / torch.linalg.vector_norm(psi))
+        bp.add_circuit(i, c, qi)
+    bp.compile(renorm_every=0, autotune=True)
+    bp.run()
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    bp.run()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    if dist is not None:
+        t = torch.tensor([plain_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        plain_ms = float(t.item())
+    plain_value = world * layers / (plain_ms * 1e-3)
+    pres = bp.results().cpu().numpy()
+    offq = np.cumsum([0] + [len(qi) for _, qi in circuits])
+    q_vs_plain = [float(np.linalg.norm(res[offq[i]:offq[i + 1]] - pres[offq[i]:offq[i + 1]]) /
+                        np.linalg.norm(pres[offq[i]:offq[i + 1]])) for i in range(len(circuits))]
+    largest = sorted(range(len(circuits)), key=lambda i: -circuits[i][0].n)[:8]
+    s_vs_plain = [_state_errors(b.state(i).cpu().numpy(), bp.state(i).cpu().numpy()) for i in largest]
+    del bp
+
     if rank == 0:
         byts = _batch_bytes(circuits)
         peak, peak_kind = _peaks()
@@ -603,7 +658,15 @@ def main_batch(a):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "circuits_per_s": world * len(circuits) / sec,
             "error_vs_fp64": {"circuits_checked": len(errs), "queries_rel_l2_max": max(errs) if errs else None,
-                              "queries_rel_l2_median": statistics.median(errs) if errs else None},
+                              "queries_rel_l2_median": statistics.median(errs) if errs else None,
+                              "states": _worst_state_errors(state_errs)},
+            "plain_c128": {"value": plain_value, "unit": "gate-layers/s", "ms_per_step": plain_ms, "steps": 1,
+                           "dtype": "c128 (FP64 math, same rounds and graph)",
+                           "speedup_of_mixed": value / plain_value,
+                           "mixed_vs_plain": {"queries_rel_l2_max": max(q_vs_plain),
+                                              "queries_rel_l2_median": statistics.median(q_vs_plain),
+                                              "largest_states": _worst_state_errors(s_vs_plain),
+                                              "states_checked": len(s_vs_plain)}},
             "roofline": {"bound": "hbm", "kernel": "whole graph (b_gate_kernel dominant)", "achieved": achieved,
                          "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "alg_bytes_per_step": byts},
@@ -685,8 +748,156 @@ def main_serve(a):
         print(json.dumps(line), flush=True)
 
 
+KERNELS_METRIC = "plain complex128 kernels: achieved HBM GB/s per kernel (fraction of measured copy bandwidth)"
+
+
+def main_kernels(a):
+    """The plain path's data-movement and streaming kernels one by one on a 2^n-amplitude
+    complex128 state (n = 28: 4 GiB, far beyond L2): permutes (rescatter-style index
+    exchanges, a full reversal, Tensor::swap), DiagTensor contractions (the QFT's
+    controlled phase, a per-qubit phase layer), a two-qubit SymmTensor gate and the FP64
+    norm. Each case: 3 warm-up launches, then `steps` launches timed with CUDA events;
+    algorithmic bytes are the state read and written once (32 B per amplitude; the norm
+    reads it, 16 B)."""
+    import numpy as np
+    import torch
+    import qtnh_gb300 as q
+
+    n = a.n
+    N = 2 ** n
+    dims = [2] * n
+    reps = max(3, a.steps)
+    peak, peak_kind = _peaks()
+
+    cpu = None
+    if not a.no_cpu_baseline:
+        from oracle import oracle as orc
+        orc.build()
+        ns = 22
+        xh = (np.random.default_rng(1).standard_normal(2 ** ns) + 0j).reshape([2] * ns)
+        pt = list(range(ns))
+        pt[0:3], pt[ns - 3:ns] = pt[ns - 3:ns], pt[0:3]
+        t0 = time.perf_counter()
+        for _ in range(3):
+            orc.permute(xh, pt)
+        sec = (time.perf_counter() - t0) / 3
+        cpu = {"value": 32 * 2 ** ns / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+               "sample": "oracle port permute (scalar C++, one core) of a 2^22-element complex128 tensor, top 3 and "
+                         "bottom 3 axes exchanged, 3 repetitions"}
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(a.seed)
+    x = torch.randn(N, dtype=torch.complex128, device=dev, generator=g)
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(a.seed)
+    theta = float(rng.uniform(0, 2 * math.pi))
+    cphase = torch.tensor([1, 1, 1, complex(math.cos(theta), math.sin(theta))], dtype=torch.complex128, device=dev)
+    ph = rng.uniform(0, 2 * math.pi, n)
+    factors = torch.tensor(np.stack([np.ones(n), np.exp(1j * ph)], axis=1).reshape(-1), dtype=torch.complex128,
+                           device=dev)
+    m = rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))
+    u, _ = np.linalg.qr(m)
+    gate = torch.tensor(np.ascontiguousarray(u.T).reshape(-1), dtype=torch.complex128, device=dev)
+
+    def top3_with(lo):
+        pt = list(range(n))
+        for i in range(3):
+            pt[i], pt[lo + i] = lo + i, i
+        return pt
+
+    rev = [n - 1 - i for i in range(n)]
+    cases = [
+        ("permute: top 3 <-> axes %d..%d" % (n // 2, n // 2 + 2), "fp64", 32,
+         lambda: q.permute(x, dims, top3_with(n // 2), out=y)),
+        ("permute: top 3 <-> innermost 3", "fp64", 32, lambda: q.permute(x, dims, top3_with(n - 3), out=y)),
+        ("permute: full reversal", "fp64", 32, lambda: q.permute(x, dims, rev, out=y)),
+        ("swap: axes 0 <-> %d" % (n - 1), "fp64", 32, lambda: q.swap(x, dims, 0, n - 1, out=y)),
+        ("diag: controlled phase on (3, %d)" % (n - 5), "fp64", 32, lambda: q.apply_diag(x, dims, [3, n - 5], cphase)),
+        ("diag: controlled phase on (3, %d)" % (n - 5), "f32x2", 32,
+         lambda: q.apply_diag(x, dims, [3, n - 5], cphase)),
+        ("diag layer: %d per-qubit phases" % n, "fp64", 32,
+         lambda: q.apply_diag_layer(x, dims, list(range(n)), factors)),
+        ("diag layer: %d per-qubit phases" % n, "f32x2", 32,
+         lambda: q.apply_diag_layer(x, dims, list(range(n)), factors)),
+        ("gate: two-qubit SymmTensor on (4, %d)" % (n - 3), "fp64", 32, lambda: q.apply_gate(x, dims, [4, n - 3], gate)),
+        ("gate: two-qubit SymmTensor on (4, %d)" % (n - 3), "f32x2", 32,
+         lambda: q.apply_gate(x, dims, [4, n - 3], gate)),
+        ("norm: FP64 sum of squares", "fp64", 16, lambda: q.norm2(x)),
+    ]
+    old = q.get_arithmetic()
+    out = {}
+    clocks = _Clocks(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = q.launches()
+    for name, arith, bpe, fn in cases:
+        q.set_arithmetic(q.ARITH_NAMES[arith])
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        gbs = bpe * N / (ms * 1e-3) / 1e9
+        out["%s [%s]" % (name, arith)] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "bytes": bpe * N}
+    launches = q.launches() - l0
+    ck = clocks.stop()
+    q.set_arithmetic(old)
+    assert q.take_device_errors() == 0
+
+    # e2e: a permute through the C ABI with host buffers (pinned), copies inside the timed region
+    hx = x.cpu().pin_memory()
+    hy = torch.empty_like(hx).pin_memory()
+    pt = top3_with(n // 2)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(reps):
+        x.copy_(hx, non_blocking=True)
+        q.permute(x, dims, pt, out=y)
+        hy.copy_(y, non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = f0.elapsed_time(f1) / reps
+
+    hbm_cases = {k: v for k, v in out.items() if not k.startswith("gate")}  # gates: FP64 / FP32-issue bound
+    worst = min(hbm_cases, key=lambda k: hbm_cases[k]["frac"])
+    line = {
+        "metric": KERNELS_METRIC, "value": hbm_cases[worst]["frac"], "unit": "fraction of measured HBM (worst case)",
+        "n_gpus": 1, "steps": reps, "warmup": 3, "ms_per_step": sum(v["ms"] for v in out.values()),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded state, gates and phases)",
+        "config": {"workload": "plain-path kernels one by one on a 2^%d-amplitude complex128 state" % n,
+                   "qubits": n, "state_bytes": 16 * N,
+                   "l2_flush": "not needed: the %d MiB state is larger than the 129 MB L2" % (16 * N >> 20)},
+        "kernels": out,
+        "roofline": {"bound": "hbm", "kernel": worst, "achieved": hbm_cases[worst]["gbs"], "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": hbm_cases[worst]["frac"], "traffic": None},
+        "cpu_baseline": cpu,
+        "e2e": {"value": 32 * N / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s (permute with host copies)",
+                "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
+        "clocks": ck,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
+    if a.workload == "kernels":
+        if a.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the kernels workload has no reference arm: it "
+                              "times this engine's kernels one by one"}))
+        else:
+            main_kernels(a)
+        return
     if a.workload == "serve":
         main_serve(a)
         return

@@ -268,10 +268,11 @@ int qtnh_rdm4(int32_t precision, const void* state, int32_t nqubits, const uint1
 /* n amplitudes complex128 -> complex64 (to_precision QTNH_STATE_C64) or back. */
 int qtnh_state_convert(int32_t to_precision, const void* in, void* out, uint64_t n, void* stream);
 
-/* ---- batched circuits in mixed precision ------------------------------------------- */
+/* ---- batched circuits ---------------------------------------------------------------- */
 
-/* Many independent circuits of uneven qubit counts and depths, complex64 states resident
- * in HBM. Operations per circuit follow the layered-circuit contractions: two-qubit
+/* Many independent circuits of uneven qubit counts and depths, states resident in HBM:
+ * complex64 with FP32 math (mixed precision; qtnh_batch_create) or complex128 with FP64
+ * math (the plain method; qtnh_batch_create_typed with QTNH_STATE_C128). Operations per circuit follow the layered-circuit contractions: two-qubit
  * SymmTensor gates (els in SymmTensor layout, host pointer to 16 complex128; input 0 on
  * qubit qa, input 1 on qb; include/tensor/symm.hpp:22-45), a phase layer (n host
  * phases: DiagTensor (1, e^{i phase}) on every qubit) and SwapTensor qubit exchanges,
@@ -284,8 +285,11 @@ int qtnh_state_convert(int32_t to_precision, const void* in, void* out, uint64_t
  * qtnh_batch_run replays it ordered after and before work on `stream`. */
 typedef struct qtnh_batch qtnh_batch;
 int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits);
+/* precision: QTNH_STATE_C64 (as qtnh_batch_create) or QTNH_STATE_C128. */
+int qtnh_batch_create_typed(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits, int32_t precision);
 int qtnh_batch_destroy(qtnh_batch* b);
-/* Initial state of circuit c from a device complex128 array (converted to complex64). */
+/* Initial state of circuit c from a device complex128 array (converted to complex64 in a
+ * mixed-precision batch). */
 int qtnh_batch_set_state(qtnh_batch* b, int32_t c, const void* psi_c128, void* stream);
 int qtnh_batch_add_gate(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb, const void* els_c128);
 int qtnh_batch_add_phases(qtnh_batch* b, int32_t c, int32_t layer, const double* phases);

@@ -274,14 +274,18 @@ def gemm_timing(enable):
 
 
 class Batch:
-    """Batched circuits in mixed precision (complex64 states, FP64 renormalisation and
-    queries) on the C ABI's qtnh_batch_* entry points: add circuits, compile once (rounds
-    of grouped kernels, autotuning, CUDA graph capture), run and read the queries."""
+    """Batched circuits on the C ABI's qtnh_batch_* entry points: add circuits, compile
+    once (rounds of grouped kernels, autotuning, CUDA graph capture), run and read the
+    queries. precision STATE_C64 (default): mixed precision, complex64 states with FP64
+    renormalisation and complex128 queries; STATE_C128: the plain method, complex128
+    states and FP64 math on the same schedule."""
 
-    def __init__(self, nqubits):
+    def __init__(self, nqubits, precision=None):
         self._b = ctypes.c_void_p()
+        self.precision = STATE_C64 if precision is None else int(precision)
         arr = (ctypes.c_int32 * len(nqubits))(*[int(x) for x in nqubits])
-        check(lib().qtnh_batch_create(ctypes.byref(self._b), ctypes.c_int32(len(nqubits)), arr))
+        check(lib().qtnh_batch_create_typed(ctypes.byref(self._b), ctypes.c_int32(len(nqubits)), arr,
+                                            ctypes.c_int32(self.precision)))
         self.nq = [int(x) for x in nqubits]
         self.nqueries = 0
 

@@ -1,6 +1,7 @@
-// Batched circuits in mixed precision: many independent circuits of uneven qubit counts
-// and depths, complex64 states resident in HBM, run as layer-synchronous rounds of
-// grouped persistent kernels under one captured CUDA graph.
+// Batched circuits: many independent circuits of uneven qubit counts and depths, states
+// resident in HBM, run as layer-synchronous rounds of grouped persistent kernels under one
+// captured CUDA graph. States are complex64 (mixed precision, the default) or complex128
+// (the plain method: FP64 math throughout, the same schedule).
 //
 // Per circuit the operations are the reference's contractions with a layered circuit:
 // two-qubit SymmTensor gates (include/tensor/symm.hpp:22-45 layout, applied in place as
@@ -9,12 +10,13 @@
 // renormalised with an FP64 norm, and the circuit ends in amplitude queries returned in
 // complex128.
 //
-// Arithmetic: amplitudes complex64; a gate U is held as two complex64 matrices
+// Mixed-precision arithmetic: amplitudes complex64; a gate U is held as two complex64 matrices
 // U = U_hi + U_lo (the FP64 gate to ~48 bits), and each output sum_i (U_lo x_i) +
 // (U_hi x_i) is accumulated with FP32 fused multiply-adds, so the only rounding of note is
 // the store to complex64. Phase layers multiply by lo/hi tables of per-qubit phase
 // products (built in FP64, stored complex64). Norms: per-thread compensated FP32 sums
-// (TwoSum) reduced in FP64.
+// (TwoSum) reduced in FP64. Plain arithmetic: complex128 amplitudes, gates and phase
+// tables, FP64 fused multiply-adds.
 //
 // Scheduling: `compile` groups the operations of all circuits into rounds (layer L: the
 // s-th gate of every circuit that has one, for each slot s; then the phase layers; then
@@ -56,6 +58,8 @@ struct Round {
   uint64_t elems_per_chunk = 0;
 };
 
+using c128 = double2;
+
 __global__ void b_to_c64_kernel(const double2* __restrict__ in, c64* __restrict__ out, uint64_t n) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
     out[i] = make_float2((float)in[i].x, (float)in[i].y);
@@ -75,20 +79,21 @@ struct Op {
 using namespace qtnh_impl;
 
 struct qtnh_batch {
+  int32_t precision = QTNH_STATE_C64;  // QTNH_STATE_C64 (mixed) or QTNH_STATE_C128 (plain)
   std::vector<uint32_t> nq;
   std::vector<uint64_t> base;
   uint64_t total_amps = 0;
-  c64* psi = nullptr;   // working states
-  c64* psi0 = nullptr;  // initial states
+  void* psi = nullptr;   // working states
+  void* psi0 = nullptr;  // initial states
   std::vector<std::vector<Op>> ops;
-  std::vector<c64> gate_host;                     // 32 c64 per gate
+  std::vector<std::complex<double>> gate_host;    // 16 per gate: U[out * 4 + in]
   std::vector<std::vector<double>> phase_host;    // per phase op: n phases
   std::vector<std::pair<uint64_t, uint64_t>> queries;  // (circuit, index)
   // compiled
   std::vector<Round> rounds;
   std::vector<void*> allocations;
-  c64* gates = nullptr;
-  c64* tables = nullptr;
+  void* gates = nullptr;   // c64: U_hi[16], U_lo[16] per gate; c128: U[16]
+  void* tables = nullptr;  // phase tables in the state's type
   double* norms = nullptr;
   uint64_t nnorms = 0;
   uint64_t* query_where = nullptr;
@@ -121,6 +126,8 @@ struct qtnh_batch {
   }
 
   uint32_t bit(uint32_t c, uint16_t q) const { return nq[c] - 1 - q; }
+  size_t amp_bytes() const { return precision == QTNH_STATE_C128 ? sizeof(c128) : sizeof(c64); }
+  void* state_of(uint64_t c) const { return static_cast<char*>(psi) + base[c] * amp_bytes(); }
 
   int grid(uint64_t total, int threads) const {
     const int per_sm = std::max(1, 2048 / threads);
@@ -145,36 +152,56 @@ struct qtnh_batch {
     return r;
   }
 
-  void launch(const Round& r, cudaStream_t s, int gthreads, uint64_t gchunk) {
+  template <typename T>
+  void launch_as(const Round& r, cudaStream_t s, int gthreads, uint64_t gchunk) {
+    const T* g_tab = static_cast<const T*>(gates);
+    const T* p_tab = static_cast<const T*>(tables);
     switch (r.kind) {
       case R_GATE: {
         const auto* t = static_cast<const GateTask*>(r.tasks);
         const int g = grid(r.total, gthreads);
         if (gthreads == 128)
-          grp::gate_kernel<c64, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+          grp::gate_kernel<T, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, gchunk);
         else if (gthreads == 512)
-          grp::gate_kernel<c64, 512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+          grp::gate_kernel<T, 512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, gchunk);
         else
-          grp::gate_kernel<c64, 256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gates, gchunk);
+          grp::gate_kernel<T, 256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, gchunk);
         break;
       }
       case R_PHASE:
-        grp::phase_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const PhaseTask*>(r.tasks), r.cbeg,
-                                                                  r.ntasks, r.total, tables, r.elems_per_chunk);
+        grp::phase_kernel<T><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const PhaseTask*>(r.tasks), r.cbeg,
+                                                                r.ntasks, r.total, p_tab, r.elems_per_chunk);
         break;
       case R_SWAP:
-        grp::swap_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const SwapTask*>(r.tasks), r.cbeg,
-                                                                 r.ntasks, r.total, r.elems_per_chunk);
+        grp::swap_kernel<T><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const SwapTask*>(r.tasks), r.cbeg,
+                                                               r.ntasks, r.total, r.elems_per_chunk);
         break;
       case R_NORM:
-        grp::norm_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const NormTask*>(r.tasks), r.cbeg,
-                                                                 r.ntasks, r.total, r.elems_per_chunk, norms);
+        grp::norm_kernel<T><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const NormTask*>(r.tasks), r.cbeg,
+                                                               r.ntasks, r.total, r.elems_per_chunk, norms);
         break;
       case R_SCALE:
-        grp::scale_kernel<c64><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const NormTask*>(r.tasks), r.cbeg,
-                                                                  r.ntasks, r.total, r.elems_per_chunk, norms);
+        grp::scale_kernel<T><<<grid(r.total, 256), 256, 0, s>>>(static_cast<const NormTask*>(r.tasks), r.cbeg,
+                                                                r.ntasks, r.total, r.elems_per_chunk, norms);
         break;
     }
+    count_launch();
+  }
+
+  void launch(const Round& r, cudaStream_t s, int gthreads, uint64_t gchunk) {
+    if (precision == QTNH_STATE_C128)
+      launch_as<c128>(r, s, gthreads, gchunk);
+    else
+      launch_as<c64>(r, s, gthreads, gchunk);
+  }
+
+  // out[i] = psi[where[i]] as complex128
+  void gather(const uint64_t* where, uint64_t nq_, double2* out, cudaStream_t s) const {
+    const int g = grid_for((nq_ + 255) / 256, 4);
+    if (precision == QTNH_STATE_C128)
+      grp::gather_kernel<c128><<<g, 256, 0, s>>>(static_cast<const c128*>(psi), where, nq_, out);
+    else
+      grp::gather_kernel<c64><<<g, 256, 0, s>>>(static_cast<const c64*>(psi), where, nq_, out);
     count_launch();
   }
 };
@@ -194,10 +221,13 @@ void check_circuit(qtnh_batch* b, int32_t c) {
 
 extern "C" {
 
-int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits) {
+int qtnh_batch_create_typed(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits, int32_t precision) {
   return guarded([&]() -> int {
     if (!out || ncircuits <= 0 || !nqubits) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid batch arguments");
+    if (precision != QTNH_STATE_C64 && precision != QTNH_STATE_C128)
+      throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown state precision");
     std::unique_ptr<qtnh_batch> b(new qtnh_batch());
+    b->precision = precision;
     for (int32_t c = 0; c < ncircuits; ++c) {
       if (nqubits[c] < 2 || nqubits[c] > 34) throw Error(QTNH_ERR_INVALID_ARGUMENT, "qubit count outside 2..34");
       b->nq.push_back((uint32_t)nqubits[c]);
@@ -205,13 +235,17 @@ int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubit
       b->total_amps += 1ull << nqubits[c];
     }
     b->ops.resize(ncircuits);
-    check_cuda(cudaMalloc(&b->psi, b->total_amps * sizeof(c64)), "batch states");
-    check_cuda(cudaMalloc(&b->psi0, b->total_amps * sizeof(c64)), "batch initial states");
-    check_cuda(cudaMemset(b->psi0, 0, b->total_amps * sizeof(c64)), "batch initial states");
+    check_cuda(cudaMalloc(&b->psi, b->total_amps * b->amp_bytes()), "batch states");
+    check_cuda(cudaMalloc(&b->psi0, b->total_amps * b->amp_bytes()), "batch initial states");
+    check_cuda(cudaMemset(b->psi0, 0, b->total_amps * b->amp_bytes()), "batch initial states");
     check_cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "batch stream");
     *out = b.release();
     return QTNH_OK;
   });
+}
+
+int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits) {
+  return qtnh_batch_create_typed(out, ncircuits, nqubits, QTNH_STATE_C64);
 }
 
 int qtnh_batch_destroy(qtnh_batch* b) {
@@ -226,10 +260,17 @@ int qtnh_batch_set_state(qtnh_batch* b, int32_t c, const void* psi_c128, void* s
     checked(b);
     if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
     const uint64_t n = 1ull << b->nq[c];
-    b_to_c64_kernel<<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(
-        static_cast<const double2*>(psi_c128), b->psi0 + b->base[c], n);
-    count_launch();
-    check_cuda(cudaGetLastError(), "batch state conversion");
+    if (!psi_c128) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null state");
+    void* dst = static_cast<char*>(b->psi0) + b->base[c] * b->amp_bytes();
+    if (b->precision == QTNH_STATE_C128) {
+      check_cuda(cudaMemcpyAsync(dst, psi_c128, n * sizeof(c128), cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
+                 "batch state");
+    } else {
+      b_to_c64_kernel<<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(
+          static_cast<const double2*>(psi_c128), static_cast<c64*>(dst), n);
+      count_launch();
+      check_cuda(cudaGetLastError(), "batch state conversion");
+    }
     return QTNH_OK;
   });
 }
@@ -240,23 +281,18 @@ int qtnh_batch_add_gate(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, ui
     check_circuit(b, c);
     if (layer < 0 || qa >= b->nq[c] || qb >= b->nq[c] || qa == qb || !els_c128)
       throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid gate");
-    // SymmTensor elements els[in * 4 + out] = U[out][in]; stored as U_hi / U_lo [out * 4 + in]
+    // SymmTensor elements els[in * 4 + out] = U[out][in]; kept as U[out * 4 + in]
     const std::complex<double>* e = static_cast<const std::complex<double>*>(els_c128);
     const size_t g0 = b->gate_host.size();
-    b->gate_host.resize(g0 + 32);
+    b->gate_host.resize(g0 + 16);
     for (int o = 0; o < 4; ++o)
-      for (int i = 0; i < 4; ++i) {
-        const std::complex<double> u = e[i * 4 + o];
-        const float hr = (float)u.real(), hi = (float)u.imag();
-        b->gate_host[g0 + o * 4 + i] = make_float2(hr, hi);
-        b->gate_host[g0 + 16 + o * 4 + i] = make_float2((float)(u.real() - hr), (float)(u.imag() - hi));
-      }
+      for (int i = 0; i < 4; ++i) b->gate_host[g0 + o * 4 + i] = e[i * 4 + o];
     Op op;
     op.kind = R_GATE;
     op.layer = layer;
     op.qa = qa;
     op.qb = qb;
-    op.index = (uint32_t)(g0 / 32);
+    op.index = (uint32_t)(g0 / 16);
     b->ops[c].push_back(op);
     b->max_layer = std::max(b->max_layer, (int)layer);
     return QTNH_OK;
@@ -313,9 +349,27 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
     checked(b);
     if (b->exec) throw Error(QTNH_ERR_RUNTIME, "batch already compiled");
     const size_t nc = b->nq.size();
-    b->gates = b->upload(b->gate_host);
+    const bool plain = b->precision == QTNH_STATE_C128;
+    // gate table: complex128 U, or complex64 U_hi followed by U_lo = U - U_hi
+    if (plain) {
+      std::vector<c128> g;
+      for (auto& u : b->gate_host) g.push_back(make_double2(u.real(), u.imag()));
+      b->gates = b->upload(g);
+    } else {
+      std::vector<c64> g;
+      for (size_t g0 = 0; g0 < b->gate_host.size(); g0 += 16) {
+        for (int k = 0; k < 16; ++k)
+          g.push_back(make_float2((float)b->gate_host[g0 + k].real(), (float)b->gate_host[g0 + k].imag()));
+        for (int k = 0; k < 16; ++k) {
+          const std::complex<double> u = b->gate_host[g0 + k];
+          g.push_back(make_float2((float)(u.real() - (double)(float)u.real()),
+                                  (float)(u.imag() - (double)(float)u.imag())));
+        }
+      }
+      b->gates = b->upload(g);
+    }
     // phase tables: per phase op, lo table over the low `split` bits and hi table over the rest
-    std::vector<c64> tab;
+    std::vector<c128> tab;
     std::vector<uint64_t> tab_off(b->phase_host.size()), tab_split(b->phase_host.size());
     std::vector<int32_t> phase_circuit(b->phase_host.size(), -1);
     for (size_t c = 0; c < nc; ++c)
@@ -333,11 +387,17 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           double ph = 0;
           for (uint32_t j = 0; j < nbits; ++j)
             if ((v >> j) & 1) ph += b->phase_host[k][n - 1 - (j + shift)];
-          tab.push_back(make_float2((float)std::cos(ph), (float)std::sin(ph)));
+          tab.push_back(make_double2(std::cos(ph), std::sin(ph)));
         }
       }
     }
-    b->tables = b->upload(tab);
+    if (plain) {
+      b->tables = b->upload(tab);
+    } else {
+      std::vector<c64> t32;
+      for (auto& x : tab) t32.push_back(make_float2((float)x.x, (float)x.y));
+      b->tables = b->upload(t32);
+    }
     // rounds
     const int period = renorm_every > 0 ? renorm_every : 0;
     std::vector<uint64_t> norm_slot_base;
@@ -349,7 +409,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           int seen = 0;
           for (auto& op : b->ops[c])
             if (op.kind == R_GATE && op.layer == L && seen++ == slot) {
-              t.push_back({b->psi + b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb), op.index});
+              t.push_back({b->state_of(c), b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb), op.index});
               u.push_back(1ull << (b->nq[c] - 2));
             }
         }
@@ -362,7 +422,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
         for (size_t c = 0; c < nc; ++c)
           for (auto& op : b->ops[c])
             if (op.kind == R_PHASE && op.layer == L) {
-              t.push_back({b->psi + b->base[c], tab_off[op.index], b->nq[c], (uint32_t)tab_split[op.index]});
+              t.push_back({b->state_of(c), tab_off[op.index], b->nq[c], (uint32_t)tab_split[op.index]});
               u.push_back(1ull << b->nq[c]);
             }
         if (!t.empty()) b->rounds.push_back(b->make_round(R_PHASE, t, u, B_CHUNK));
@@ -374,7 +434,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           int seen = 0;
           for (auto& op : b->ops[c])
             if (op.kind == R_SWAP && op.layer == L && seen++ == slot) {
-              t.push_back({b->psi + b->base[c], b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb)});
+              t.push_back({b->state_of(c), b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb)});
               u.push_back(1ull << (b->nq[c] - 2));
             }
         }
@@ -388,7 +448,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
           int last = -1;
           for (auto& op : b->ops[c]) last = std::max(last, op.layer);
           if (last < L) continue;  // the circuit has ended
-          t.push_back({b->psi + b->base[c], b->nq[c], (uint32_t)(b->nnorms++)});
+          t.push_back({b->state_of(c), b->nq[c], (uint32_t)(b->nnorms++)});
           u.push_back(1ull << b->nq[c]);
         }
         if (!t.empty()) {
@@ -457,14 +517,11 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
     check_cuda(cudaStreamSynchronize(s), "batch synchronize");
     check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     uint64_t n0 = g_launches.load();
-    check_cuda(cudaMemcpyAsync(b->psi, b->psi0, b->total_amps * sizeof(c64), cudaMemcpyDeviceToDevice, s), "reset");
+    check_cuda(cudaMemcpyAsync(b->psi, b->psi0, b->total_amps * b->amp_bytes(), cudaMemcpyDeviceToDevice, s),
+               "reset");
     if (b->nnorms) check_cuda(cudaMemsetAsync(b->norms, 0, b->nnorms * sizeof(double), s), "norm reset");
     for (auto& r : b->rounds) b->launch(r, s, b->gate_threads, b->gate_chunk);
-    if (!where.empty()) {
-      grp::gather_kernel<c64><<<grid_for((where.size() + 255) / 256, 4), 256, 0, s>>>(b->psi, b->query_where,
-                                                                                     where.size(), b->query_out);
-      count_launch();
-    }
+    if (!where.empty()) b->gather(b->query_where, where.size(), b->query_out, s);
     b->launches_per_run = g_launches.load() - n0;
     g_launches.fetch_sub(b->launches_per_run);  // counted when the graph runs
     check_cuda(cudaStreamEndCapture(s, &b->graph), "end capture");
@@ -521,16 +578,14 @@ int qtnh_batch_state(qtnh_batch* b, int32_t c, void* out_c128, void* stream) {
     checked(b);
     if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
     const uint64_t n = 1ull << b->nq[c];
-    // complex64 -> complex128 through the query kernel over consecutive positions
+    // to complex128 through the query kernel over consecutive positions
     std::vector<uint64_t> where(n);
     for (uint64_t i = 0; i < n; ++i) where[i] = b->base[c] + i;
     uint64_t* w = nullptr;
     check_cuda(cudaMallocAsync((void**)&w, n * sizeof(uint64_t), (cudaStream_t)stream), "batch state");
     check_cuda(cudaMemcpyAsync(w, where.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, (cudaStream_t)stream),
                "batch state");
-    grp::gather_kernel<c64><<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(
-        b->psi, w, n, static_cast<double2*>(out_c128));
-    count_launch();
+    b->gather(w, n, static_cast<double2*>(out_c128), (cudaStream_t)stream);
     check_cuda(cudaFreeAsync(w, (cudaStream_t)stream), "batch state");
     check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch state");
     return QTNH_OK;

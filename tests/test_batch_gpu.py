@@ -5,7 +5,8 @@ contraction sequence) and against the GPU's plain FP64 path for a larger circuit
 
 Error bar of the mixed-precision method: every pass over a state rounds each amplitude
 to complex64 once (~6e-8 relative), so a circuit of G passes drifts like sqrt(G) * 6e-8;
-asserted at 5e-6 relative L2 per circuit (queries and full states)."""
+asserted at 5e-6 relative L2 per circuit (queries and full states). The plain form of the
+same schedule (complex128 states, FP64 math) is held to the contraction bar, 1e-12."""
 import numpy as np
 import pytest
 
@@ -102,6 +103,28 @@ def test_batch_large_circuit_vs_fp64_engine():
     assert rel(b.results().cpu().numpy(), ref[qi.astype(np.int64)]) < BAR
 
 
+def test_plain_batch_matches_oracle():
+    # the plain method on the same schedule: complex128 states, FP64 math, no renormalisation
+    circuits = wl.batch_circuits(10, seed=78, qubits=(10, 14), depth=(8, 20))
+    b = q.Batch([c.n for c, _ in circuits], precision=q.STATE_C128)
+    states = []
+    for i, (c, qi) in enumerate(circuits):
+        psi = wl.random_state(c.n, seed=300 + i)
+        states.append(psi)
+        b.set_state(i, dev(psi))
+        b.add_circuit(i, c, qi)
+    b.compile(renorm_every=0, autotune=True)
+    b.run()
+    res = b.results().cpu().numpy()
+    k = 0
+    for i, ((c, qi), psi) in enumerate(zip(circuits, states)):
+        ref = orc.run_circuit(psi, c)
+        assert rel(res[k:k + len(qi)], ref[qi.astype(np.int64)]) < 1e-12
+        k += len(qi)
+        if i % 3 == 0:
+            assert rel(b.state(i).cpu().numpy(), ref) < 1e-12
+
+
 def test_batch_rejects_invalid_operations():
     b = q.Batch([10, 12])
     eye = np.eye(4, dtype=np.complex128).reshape(-1)
@@ -115,3 +138,5 @@ def test_batch_rejects_invalid_operations():
         b.add_circuit(0, c)  # a gate on one qubit twice
     with pytest.raises(q.QtnhError):
         b.add_circuit(1, wl.Circuit(12), queries=[2 ** 12])
+    with pytest.raises(q.QtnhError):
+        q.Batch([10], precision=7)  # no such state precision

@@ -1,7 +1,8 @@
 """The request loop on the GPU (grouped layer steps over resident states, FP64
 renormalisation, amplitude and reduced-density-matrix answers) in plain complex128 and
 mixed complex64, against the oracle's complex128 contraction sequence of every
-request: plain within 1e-12 relative, mixed within the batched-circuit bar 5e-6."""
+request: plain within 1e-12 relative, mixed within the batched-circuit bar 5e-6; and a
+request's answer served alone against the same request served in a mix of others."""
 import numpy as np
 import pytest
 
@@ -48,4 +49,22 @@ def test_serve_answers_match_oracle(precision, bar):
         got, ref = np.asarray(results[r.rid]), reference(r)
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
         assert err < bar, (r.rid, r.kind, r.circuit.n, err)
+    assert q.take_device_errors() == 0
+
+
+@pytest.mark.parametrize("precision,bar", [(serve.C128, 1e-13), (serve.C64, 1e-6)], ids=["plain", "mixed"])
+def test_serve_result_same_alone_and_in_mix(precision, bar):
+    # a request's answer does not depend on what else is on the GPU: served in a mix of
+    # requests of other sizes and depths (grouped launches, work-balanced steps, several
+    # layers per step) and served alone, the answers agree within the stated tolerance
+    # (FP64 atomics in norms and RDM sums make the two runs differ in the last bits only)
+    reqs = serve.request_stream(12, rate=4000.0, seed=21, qubits=(10, 15), depth=(10, 24))
+    renorm = 8 if precision == serve.C64 else 0
+    _, mix, _ = serve.serve(reqs, serve.GpuExecutor(precision), budget_bytes=8 * 2 ** 20, renorm_every=renorm,
+                            realtime=False)
+    for r in reqs[::3]:
+        _, alone, _ = serve.serve([r], serve.GpuExecutor(precision), budget_bytes=8 * 2 ** 20, renorm_every=renorm,
+                                  realtime=False)
+        a, m = np.asarray(alone[r.rid]), np.asarray(mix[r.rid])
+        assert np.linalg.norm(a - m) / np.linalg.norm(a) < bar, (r.rid, r.kind, r.circuit.n)
     assert q.take_device_errors() == 0
