@@ -377,10 +377,11 @@ def test_gate_pairs_tensor_core_match_oracle(seed, bf16x6):
     assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
 
 
-@pytest.mark.parametrize("n", [8, 10, 18])
+@pytest.mark.parametrize("n", [8, 10, 18, 22])
 def test_gate_pairs_tensor_core_sizes(n, bf16x6):
     # n < 11: the mma.sync kernel (fewer than one 128-group tile); n = 18: the tcgen05
-    # kernel with several tiles per CTA, both warpgroups and barrier phases in use
+    # kernel with one tile per CTA; n = 22: 2048 tiles, 13-14 per CTA, so both pipeline
+    # buffers and both phases of every barrier are used several times
     nrng = np.random.default_rng(200 + n)
     psi = crandn(nrng, [2] * n)
     perm = [int(x) for x in nrng.permutation(n)]
@@ -388,6 +389,26 @@ def test_gate_pairs_tensor_core_sizes(n, bf16x6):
     st = dev(psi)
     q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
     assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
+
+
+def test_gate_pairs_tensor_core_fall_back_many_tiles(bf16x6):
+    # FP64 groups scattered through a state of many tiles per CTA: every 37th block of
+    # 4096 amplitudes is scaled to 1e-250 (the targets are bits 2, 5, 9, 11, so each group
+    # lies inside one block); each region is compared on its own scale
+    nrng = np.random.default_rng(15)
+    n = 21
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    blocks = psi.reshape(-1, 4096)
+    tiny = np.zeros(blocks.shape[0], dtype=bool)
+    tiny[::37] = True
+    blocks[tiny] *= 1e-250
+    gates = [([n - 1 - 2, n - 1 - 9], haar(nrng, 4).T.reshape(-1)),
+             ([n - 1 - 5, n - 1 - 11], haar(nrng, 4).T.reshape(-1))]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    out, ref = host(st).reshape(-1, 4096), _oracle_layer(psi, n, gates).reshape(-1, 4096)
+    assert rel_l2(out[tiny], ref[tiny]) < REL_TOL
+    assert rel_l2(out[~tiny], ref[~tiny]) < REL_TOL
 
 
 def test_gate_layer_tensor_core_mixed(bf16x6):
