@@ -380,8 +380,8 @@ def test_gate_pairs_tensor_core_match_oracle(seed, bf16x6):
 @pytest.mark.parametrize("n", [8, 10, 18, 22])
 def test_gate_pairs_tensor_core_sizes(n, bf16x6):
     # n < 11: the mma.sync kernel (fewer than one 128-group tile); n = 18: the tcgen05
-    # kernel with one tile per CTA; n = 22: 2048 tiles, 13-14 per CTA, so both pipeline
-    # buffers and both phases of every barrier are used several times
+    # kernel with one tile per CTA; n = 22: 2048 tiles, 13-14 per CTA, so both teams and
+    # both phases of every barrier are used several times
     nrng = np.random.default_rng(200 + n)
     psi = crandn(nrng, [2] * n)
     perm = [int(x) for x in nrng.permutation(n)]
