@@ -155,18 +155,22 @@ struct DiagParams {
   uint32_t dim_log2[8], stride_log2[8];
 };
 
-__device__ __forceinline__ uint64_t digit(uint64_t e, uint64_t stride, uint32_t stride_log2, uint64_t dim, uint32_t dim_log2) {
-  uint64_t q = (stride_log2 != 0xFFFFFFFFu) ? (e >> stride_log2) : (e / stride);
-  return (dim_log2 != 0xFFFFFFFFu) ? (q & (dim - 1)) : (q % dim);
-}
+// Streaming kernels move DU elements per thread per step, all loads issued before any
+// arithmetic, so that enough bytes are in flight per SM to keep HBM busy. IT is the index
+// type (32-bit when the state and the grid stride fit).
+constexpr int DU = 4;
 
-__global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const c128* __restrict__ d,
-                                                   const __grid_constant__ DiagParams p) {
-  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.n; e += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t idx = 0;
-    for (int j = 0; j < p.k; ++j) idx += digit(e, p.stride[j], p.stride_log2[j], p.dim[j], p.dim_log2[j]) * p.mult[j];
-    psi[e] = cmul(psi[e], __ldg(d + idx));
+template <typename IT>
+__device__ __forceinline__ IT diag_index(IT e, const DiagParams& p) {
+  IT idx = 0;
+  for (int j = 0; j < p.k; ++j) {
+    IT q;
+    if (p.stride_log2[j] != 0xFFFFFFFFu) q = e >> p.stride_log2[j];
+    else q = (IT)(e / (IT)p.stride[j]);
+    const IT dg = (p.dim_log2[j] != 0xFFFFFFFFu) ? (q & (IT)(p.dim[j] - 1)) : (IT)(q % (IT)p.dim[j]);
+    idx += dg * (IT)p.mult[j];
   }
+  return idx;
 }
 
 __device__ __noinline__ c128 cmul_fp64_outofline(c128 a, c128 b) { return cmul(a, b); }
@@ -182,12 +186,23 @@ __device__ __forceinline__ c128 cmul_f32x2(c128 a, c128 b) {
   return cmul_fp64_outofline(a, b);
 }
 
-__global__ void __launch_bounds__(256) diag_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ d,
-                                                         const __grid_constant__ DiagParams p) {
-  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.n; e += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t idx = 0;
-    for (int j = 0; j < p.k; ++j) idx += digit(e, p.stride[j], p.stride_log2[j], p.dim[j], p.dim_log2[j]) * p.mult[j];
-    psi[e] = cmul_f32x2(psi[e], __ldg(d + idx));
+// psi[e] *= d[index of e over the targets]; FF: float-float products (cmul_f32x2), else FP64.
+template <typename IT, bool FF>
+__global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const c128* __restrict__ d,
+                                                   const __grid_constant__ DiagParams p) {
+  const IT n = (IT)p.n, step = (IT)gridDim.x * blockDim.x * DU;
+  for (IT base = (IT)blockIdx.x * blockDim.x * DU + threadIdx.x; base < n; base += step) {
+    c128 x[DU], f[DU];
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e < n) x[u] = psi[e], f[u] = __ldg(d + diag_index<IT>(e, p));
+    }
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e < n) psi[e] = FF ? cmul_f32x2(x[u], f[u]) : cmul(x[u], f[u]);
+    }
   }
 }
 
@@ -216,16 +231,35 @@ __global__ void layer_table_kernel(const c128* __restrict__ factors, c128* __res
   }
 }
 
+template <typename IT>
+__device__ __forceinline__ void hi_lo(IT e, IT lo_size, uint32_t lo_log2, IT& h, IT& l) {
+  if (lo_log2 != 0xFFFFFFFFu) h = e >> lo_log2, l = e & (lo_size - 1);
+  else h = e / lo_size, l = e % lo_size;
+}
+
 // psi[e] *= hi[e / lo_size] * lo[e % lo_size]; lo_size is a power of two or general.
+template <typename IT>
 __global__ void __launch_bounds__(256) layer_apply_kernel(c128* __restrict__ psi, const c128* __restrict__ hi,
-                                                          const c128* __restrict__ lo, uint64_t n, uint64_t lo_size,
-                                                          uint32_t lo_log2) {
-  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t h, l;
-    if (lo_log2 != 0xFFFFFFFFu) h = e >> lo_log2, l = e & (lo_size - 1);
-    else h = e / lo_size, l = e % lo_size;
-    c128 ph = cmul(__ldg(hi + h), __ldg(lo + l));
-    psi[e] = cmul(psi[e], ph);
+                                                          const c128* __restrict__ lo, uint64_t n64,
+                                                          uint64_t lo_size64, uint32_t lo_log2) {
+  const IT n = (IT)n64, lo_size = (IT)lo_size64, step = (IT)gridDim.x * blockDim.x * DU;
+  for (IT base = (IT)blockIdx.x * blockDim.x * DU + threadIdx.x; base < n; base += step) {
+    c128 x[DU], ph[DU];
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e < n) {
+        IT h, l;
+        hi_lo<IT>(e, lo_size, lo_log2, h, l);
+        x[u] = psi[e];
+        ph[u] = cmul(__ldg(hi + h), __ldg(lo + l));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e < n) psi[e] = cmul(x[u], ph[u]);
+    }
   }
 }
 
@@ -239,30 +273,51 @@ __global__ void table_split_kernel(const c128* __restrict__ t, df::cf2* __restri
   }
 }
 
+template <typename IT>
 __global__ void __launch_bounds__(256) layer_apply_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ hi,
                                                                 const c128* __restrict__ lo,
                                                                 const df::cf2* __restrict__ his,
-                                                                const df::cf2* __restrict__ los, uint64_t n,
-                                                                uint64_t lo_size, uint32_t lo_log2) {
-  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t h, l;
-    if (lo_log2 != 0xFFFFFFFFu) h = e >> lo_log2, l = e & (lo_size - 1);
-    else h = e / lo_size, l = e % lo_size;
-    c128 x = psi[e];
-    df::cf2 a = his[h], b = los[l];
-    bool ok = a.re.h == a.re.h && b.re.h == b.re.h && df::in_range_state(x.x) && df::in_range_state(x.y);
-    if (__all_sync(__activemask(), ok)) {
-      df::acc pr, pi;
-      df::cmul_acc(a, b, pr, pi);
-      df::cf2 ph{df::renorm(pr), df::renorm(pi)};
-      df::acc re, im;
-      df::cmul_acc(df::csplit(x.x, x.y), ph, re, im);
-      psi[e] = make_double2(df::to_double(re), df::to_double(im));
-    } else {
-      psi[e] = cmul_fp64_outofline(x, cmul_fp64_outofline(__ldg(hi + h), __ldg(lo + l)));
+                                                                const df::cf2* __restrict__ los, uint64_t n64,
+                                                                uint64_t lo_size64, uint32_t lo_log2) {
+  const IT n = (IT)n64, lo_size = (IT)lo_size64, step = (IT)gridDim.x * blockDim.x * DU;
+  for (IT base = (IT)blockIdx.x * blockDim.x * DU + threadIdx.x; base < n; base += step) {
+    c128 x[DU];
+    df::cf2 a[DU], b[DU];
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e < n) {
+        IT h, l;
+        hi_lo<IT>(e, lo_size, lo_log2, h, l);
+        x[u] = psi[e];
+        a[u] = his[h];
+        b[u] = los[l];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e >= n) continue;
+      const bool ok = a[u].re.h == a[u].re.h && b[u].re.h == b[u].re.h && df::in_range_state(x[u].x) &&
+                      df::in_range_state(x[u].y);
+      if (__all_sync(__activemask(), ok)) {
+        df::acc pr, pi;
+        df::cmul_acc(a[u], b[u], pr, pi);
+        df::cf2 ph{df::renorm(pr), df::renorm(pi)};
+        df::acc re, im;
+        df::cmul_acc(df::csplit(x[u].x, x[u].y), ph, re, im);
+        psi[e] = make_double2(df::to_double(re), df::to_double(im));
+      } else {
+        IT h, l;
+        hi_lo<IT>(e, lo_size, lo_log2, h, l);
+        psi[e] = cmul_fp64_outofline(x[u], cmul_fp64_outofline(__ldg(hi + h), __ldg(lo + l)));
+      }
     }
   }
 }
+
+// 32-bit indices when n plus one grid stride of DU elements per thread fits.
+inline bool index32(uint64_t n, int grid) { return n + (uint64_t)grid * 256 * DU < (1ull << 32); }
 
 // Merge the non-target axes into runs and describe them (state strides in s_in).
 void other_axes(const dims_t& dims, const std::vector<uint16_t>& targets, RestDesc& out) {
@@ -373,11 +428,17 @@ void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16
     m *= p.dim[j];
   }
   cudaStream_t s = (cudaStream_t)stream;
-  int grid = grid_for((n + 255) / 256, 8);
-  if (arithmetic_mode() != QTNH_ARITH_FP64)
-    diag_kernel_f32x2<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
-  else
-    diag_kernel<<<grid, 256, 0, s>>>(static_cast<c128*>(state), static_cast<const c128*>(diag), p);
+  const int grid = grid_for((n + 256 * DU - 1) / (256 * DU), 8);
+  c128* st_ = static_cast<c128*>(state);
+  const c128* d_ = static_cast<const c128*>(diag);
+  const bool ff = arithmetic_mode() != QTNH_ARITH_FP64;
+  if (index32(n, grid)) {
+    if (ff) diag_kernel<uint32_t, true><<<grid, 256, 0, s>>>(st_, d_, p);
+    else diag_kernel<uint32_t, false><<<grid, 256, 0, s>>>(st_, d_, p);
+  } else {
+    if (ff) diag_kernel<uint64_t, true><<<grid, 256, 0, s>>>(st_, d_, p);
+    else diag_kernel<uint64_t, false><<<grid, 256, 0, s>>>(st_, d_, p);
+  }
   count_launch();
   check_cuda(cudaGetLastError(), "diag_kernel launch");
 }
@@ -419,16 +480,25 @@ void apply_diag_layer_device(void* state, const dims_t& dims, const std::vector<
   const c128* fac = static_cast<const c128*>(factors);
   layer_table_kernel<<<grid_for((lo_size + 255) / 256, 4), 256, 0, s>>>(fac, tables, *lo);
   layer_table_kernel<<<grid_for((hi_size + 255) / 256, 4), 256, 0, s>>>(fac, tables + lo_size, *hi);
+  const int grid = grid_for((n + 256 * DU - 1) / (256 * DU), 8);
+  const bool i32 = index32(n, grid);
+  c128* st_ = static_cast<c128*>(state);
+  const uint32_t lo_log2 = log2_or_none(lo_size);
   if (ff) {
     df::cf2* split_tab = reinterpret_cast<df::cf2*>(tables + tab);
     table_split_kernel<<<grid_for((tab + 255) / 256, 4), 256, 0, s>>>(tables, split_tab, tab);
-    layer_apply_kernel_f32x2<<<grid_for((n + 255) / 256, 8), 256, 0, s>>>(
-        static_cast<c128*>(state), tables + lo_size, tables, split_tab + lo_size, split_tab, n, lo_size,
-        log2_or_none(lo_size));
+    if (i32)
+      layer_apply_kernel_f32x2<uint32_t><<<grid, 256, 0, s>>>(st_, tables + lo_size, tables, split_tab + lo_size,
+                                                              split_tab, n, lo_size, lo_log2);
+    else
+      layer_apply_kernel_f32x2<uint64_t><<<grid, 256, 0, s>>>(st_, tables + lo_size, tables, split_tab + lo_size,
+                                                              split_tab, n, lo_size, lo_log2);
     count_launch(4);
   } else {
-    layer_apply_kernel<<<grid_for((n + 255) / 256, 8), 256, 0, s>>>(static_cast<c128*>(state), tables + lo_size, tables,
-                                                                    n, lo_size, log2_or_none(lo_size));
+    if (i32)
+      layer_apply_kernel<uint32_t><<<grid, 256, 0, s>>>(st_, tables + lo_size, tables, n, lo_size, lo_log2);
+    else
+      layer_apply_kernel<uint64_t><<<grid, 256, 0, s>>>(st_, tables + lo_size, tables, n, lo_size, lo_log2);
     count_launch(3);
   }
   cudaError_t e = cudaGetLastError();

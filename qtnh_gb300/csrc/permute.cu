@@ -12,9 +12,13 @@
 //     (each contiguous run of the input is one contiguous run of the output);
 //   * otherwise a tiled transpose: the tile spans the input's trailing axes (>= 32
 //     contiguous elements, coalesced 128-bit loads) and the output's trailing axes
-//     (>= 32 contiguous elements, coalesced 128-bit stores); the tile is staged in
-//     shared memory with one padding slot per row, and the per-element offsets of
-//     the tile come as tables in the kernel parameters (copied to shared memory);
+//     (>= 32 contiguous elements, coalesced 128-bit stores); a merged axis too large
+//     for the tile is split into (outer, inner) parts so the tile takes only the inner
+//     part it needs (e.g. an exchange of the top and bottom 3 axes of a 28-axis state:
+//     dims (8, 2^22, 8) become (8, 2^20, 4, 8) and the tile is 8 x 4 x 8). The tile is
+//     staged in shared memory with one padding slot per row; the per-element offsets of
+//     the tile come as tables in the kernel parameters (copied to shared memory), and
+//     small tiles are processed several per step so that enough loads are in flight;
 //   * a gather (coalesced stores, indexed loads) when no tile fits.
 
 #include <algorithm>
@@ -30,11 +34,14 @@ namespace {
 
 constexpr int TILE_MAX = 1024;   // elements per transpose tile
 constexpr int TILE_THREADS = 256;
+constexpr int STEP_ELEMS = 2048;  // elements of the tiles moved per step of a block (power-of-two tiles)
 
 
 struct TileParams {
   RestDesc rest;
-  int T;
+  int T;           // elements per tile
+  int G;           // tiles per step (T is a power of two when G > 1)
+  uint32_t T_log2;
   int tile_slots;
   int64_t rin[TILE_MAX];   // read order: input offset within the tile
   int64_t wout[TILE_MAX];  // write order: output offset within the tile
@@ -51,9 +58,11 @@ struct RunParams {
 __global__ void __launch_bounds__(TILE_THREADS) tiled_permute_kernel(const c128* __restrict__ in, c128* __restrict__ out,
                                                                      const __grid_constant__ TileParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int T = p.T;
-  c128* tile = reinterpret_cast<c128*>(smem_raw);
-  int64_t* s_rin = reinterpret_cast<int64_t*>(tile + p.tile_slots);
+  const int T = p.T, G = p.G, S = p.tile_slots;
+  c128* tile = reinterpret_cast<c128*>(smem_raw);  // G tiles of S slots
+  uint64_t* s_bin = reinterpret_cast<uint64_t*>(tile + (size_t)G * S);
+  uint64_t* s_bout = s_bin + G;
+  int64_t* s_rin = reinterpret_cast<int64_t*>(s_bout + G);
   int64_t* s_wout = s_rin + T;
   int32_t* s_rslot = reinterpret_cast<int32_t*>(s_wout + T);
   int32_t* s_wslot = s_rslot + T;
@@ -63,13 +72,26 @@ __global__ void __launch_bounds__(TILE_THREADS) tiled_permute_kernel(const c128*
     s_rslot[t] = p.rslot[t];
     s_wslot[t] = p.wslot[t];
   }
-  __syncthreads();
-  for (uint64_t r = blockIdx.x; r < p.rest.total; r += gridDim.x) {
-    uint64_t bin, bout;
-    decode(r, p.rest, bin, bout);
-    for (int t = threadIdx.x; t < T; t += blockDim.x) tile[s_rslot[t]] = __ldg(in + bin + s_rin[t]);
+  const uint64_t total = p.rest.total;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * G; r0 < total; r0 += (uint64_t)gridDim.x * G) {
+    for (int g = threadIdx.x; g < G && r0 + g < total; g += blockDim.x) {
+      uint64_t bin, bout;
+      decode(r0 + g, p.rest, bin, bout);
+      s_bin[g] = bin;
+      s_bout[g] = bout;
+    }
     __syncthreads();
-    for (int t = threadIdx.x; t < T; t += blockDim.x) out[bout + s_wout[t]] = tile[s_wslot[t]];
+    const uint64_t left = total - r0;
+    const int n = (left < (uint64_t)G ? (int)left : G) * T;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+      const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+      tile[g * S + s_rslot[t]] = __ldg(in + s_bin[g] + s_rin[t]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+      const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+      out[s_bout[g] + s_wout[t]] = tile[g * S + s_wslot[t]];
+    }
     __syncthreads();
   }
 }
@@ -155,6 +177,23 @@ Canon canonicalise(const dims_t& dims, const std::vector<uint16_t>& ptup) {
   return c;
 }
 
+// Splits merged axis i into (dims[i] / lo, lo); the two parts stay adjacent, in this
+// order, in the input and in the output.
+void split_axis(Canon& c, int i, uint64_t lo) {
+  const int P = c.ptup[i];
+  for (auto& x : c.ptup)
+    if (x > P) ++x;
+  c.dims[i] /= lo;
+  c.dims.insert(c.dims.begin() + i + 1, lo);
+  c.ptup.insert(c.ptup.begin() + i + 1, P + 1);
+}
+
+// Smallest divisor f of d with want <= f <= TILE_MAX and f < d, or 0.
+uint64_t inner_factor(uint64_t d, uint64_t want) {
+  for (uint64_t f = std::max<uint64_t>(want, 2); f <= (uint64_t)TILE_MAX && f < d; ++f)
+    if (d % f == 0) return f;
+  return 0;
+}
 
 }  // namespace
 
@@ -175,28 +214,24 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
   c128* out = static_cast<c128*>(out_v);
 
   Canon c = canonicalise(dims, ptup);
-  const int r = (int)c.dims.size();
-  if (r > KMAX) throw Error(QTNH_ERR_UNSUPPORTED, "too many non-trivial axes");
-  if (r <= 1) {
+  if ((int)c.dims.size() > KMAX) throw Error(QTNH_ERR_UNSUPPORTED, "too many non-trivial axes");
+  if (c.dims.size() <= 1) {
     check_cuda(cudaMemcpyAsync(out, in, N * sizeof(c128), cudaMemcpyDeviceToDevice, s), "permute copy");
     return;
   }
-  dims_t in_stride = row_strides(c.dims);
-  dims_t new_dims(r);
-  for (int i = 0; i < r; ++i) new_dims[c.ptup[i]] = c.dims[i];
-  dims_t ns = row_strides(new_dims);
-  dims_t out_stride(r);
-  std::vector<int> inv(r);
-  for (int i = 0; i < r; ++i) out_stride[i] = ns[c.ptup[i]], inv[c.ptup[i]] = i;
-
   // Run copy.
-  if (c.ptup[r - 1] == r - 1 && c.dims[r - 1] >= 32) {
+  if (c.ptup.back() == (int)c.dims.size() - 1 && c.dims.back() >= 32) {
+    const int r = (int)c.dims.size();
+    dims_t in_stride = row_strides(c.dims);
+    dims_t new_dims(r);
+    for (int i = 0; i < r; ++i) new_dims[c.ptup[i]] = c.dims[i];
+    dims_t ns = row_strides(new_dims);
     RunParams p;
     p.L = c.dims[r - 1];
     p.L_log2 = log2_or_none(p.L);
     p.rest.n = r - 1;
     p.rest.total = N / p.L;
-    for (int i = 0; i < r - 1; ++i) fill_axis(p.rest.ax[i], c.dims[i], in_stride[i], out_stride[i]);
+    for (int i = 0; i < r - 1; ++i) fill_axis(p.rest.ax[i], c.dims[i], in_stride[i], ns[c.ptup[i]]);
     int grid = grid_for((N + 1023) / 1024, 16);
     run_copy_kernel<<<grid, 256, 0, s>>>(in, out, p);
     count_launch();
@@ -204,23 +239,64 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
     return;
   }
 
-  // Tiled transpose.
-  std::vector<int> A, B;
-  std::vector<char> inA(r, 0), inB(r, 0);
+  // Tiled transpose: A = the input's trailing axes (>= 32 contiguous input elements), B =
+  // further axes completing the output's trailing run (>= 32 contiguous output elements).
+  // A merged axis that would overflow the tile is split and the plan restarts.
+  int r = 0;
+  dims_t in_stride, new_dims, out_stride;
+  std::vector<int> inv, A, B;
+  std::vector<char> inA, inB;
   uint64_t PA = 1, PB = 1;
-  for (int i = r - 1; i >= 0 && PA < 32; --i) A.push_back(i), PA *= c.dims[i], inA[i] = 1;
-  bool tiled = PA <= (uint64_t)TILE_MAX;
-  if (tiled) {
+  bool tiled = false;
+  for (int attempt = 0; attempt <= KMAX; ++attempt) {
+    r = (int)c.dims.size();
+    in_stride = row_strides(c.dims);
+    new_dims.assign(r, 0);
+    for (int i = 0; i < r; ++i) new_dims[c.ptup[i]] = c.dims[i];
+    dims_t ns = row_strides(new_dims);
+    out_stride.assign(r, 0);
+    inv.assign(r, 0);
+    for (int i = 0; i < r; ++i) out_stride[i] = ns[c.ptup[i]], inv[c.ptup[i]] = i;
+    A.clear();
+    B.clear();
+    inA.assign(r, 0);
+    inB.assign(r, 0);
+    PA = 1;
+    PB = 1;
+    const bool may_split = r < KMAX;
+    bool restart = false;
+    for (int i = r - 1; i >= 0 && PA < 32; --i) {
+      if (PA * c.dims[i] > 64 && may_split) {
+        const uint64_t f = inner_factor(c.dims[i], (32 + PA - 1) / PA);
+        if (f) {
+          split_axis(c, i, f);
+          restart = true;
+          break;
+        }
+      }
+      A.push_back(i), PA *= c.dims[i], inA[i] = 1;
+    }
+    if (restart) continue;
+    tiled = PA <= (uint64_t)TILE_MAX;
+    if (!tiled) break;
     uint64_t run = 1;
     for (int j = r - 1; j >= 0 && run < 32; --j) {
-      int i = inv[j];
+      const int i = inv[j];
       if (inA[i]) {
         run *= c.dims[i];
         continue;
       }
-      if (PA * PB * c.dims[i] > (uint64_t)TILE_MAX) break;
+      if (PA * PB * c.dims[i] > (uint64_t)TILE_MAX) {
+        const uint64_t f = may_split ? inner_factor(c.dims[i], (32 + run - 1) / run) : 0;
+        if (f && PA * PB * f <= (uint64_t)TILE_MAX) {
+          split_axis(c, i, f);
+          restart = true;
+        }
+        break;
+      }
       B.push_back(i), PB *= c.dims[i], inB[i] = 1, run *= c.dims[i];
     }
+    if (!restart) break;
   }
   if (tiled) {
     std::sort(A.begin(), A.end());
@@ -230,6 +306,9 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
     const int T = (int)(PA * PB);
     p.T = T;
     p.tile_slots = (int)(PB * (PA + 1));
+    const uint32_t tl = log2_or_none((uint64_t)T);
+    p.G = (tl != 0xFFFFFFFFu && T < STEP_ELEMS) ? std::min(STEP_ELEMS / T, 256) : 1;
+    p.T_log2 = tl == 0xFFFFFFFFu ? 0 : tl;
     // Row-major multipliers over A and B (input order).
     auto mults = [&](const std::vector<int>& axes) {
       std::vector<uint64_t> m(axes.size(), 1);
@@ -279,8 +358,12 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
       if (!inA[i] && !inB[i]) fill_axis(p.rest.ax[nr++], c.dims[i], in_stride[i], out_stride[i]);
     p.rest.n = nr;
     p.rest.total = N / (uint64_t)T;
-    size_t smem = (size_t)p.tile_slots * sizeof(c128) + (size_t)T * (2 * sizeof(int64_t) + 2 * sizeof(int32_t));
-    int grid = grid_for(p.rest.total, 5);
+    const size_t smem = (size_t)p.G * p.tile_slots * sizeof(c128) + 2 * (size_t)p.G * sizeof(uint64_t) +
+                        (size_t)T * (2 * sizeof(int64_t) + 2 * sizeof(int32_t));
+    if (smem > 48 * 1024)
+      check_cuda(cudaFuncSetAttribute(tiled_permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "tiled_permute_kernel shared memory");
+    int grid = grid_for((p.rest.total + p.G - 1) / p.G, 3);
     tiled_permute_kernel<<<grid, TILE_THREADS, smem, s>>>(in, out, p);
     count_launch();
     check_cuda(cudaGetLastError(), "tiled_permute_kernel launch");

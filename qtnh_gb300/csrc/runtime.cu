@@ -84,12 +84,23 @@ void workspace_free(void* p, void* stream) {
 
 // FP64 sum of |x|^2: grid-stride partial sums, one atomic per block.
 __global__ void norm2_kernel(const double2* __restrict__ x, uint64_t n, double* __restrict__ acc) {
-  double s = 0.0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    double2 v = x[i];
-    s = fma(v.x, v.x, s);
-    s = fma(v.y, v.y, s);
+  // four elements per thread per step, loads first, two independent accumulators
+  double s = 0.0, s2 = 0.0;
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x * 4;
+  for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x * 4 + threadIdx.x; b < n; b += step) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t i = b + (uint64_t)u * blockDim.x;
+      v[u] = i < n ? x[i] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      s = fma(v[u].x, v[u].x, s);
+      s2 = fma(v[u].y, v[u].y, s2);
+    }
   }
+  s += s2;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   __shared__ double ws[32];
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

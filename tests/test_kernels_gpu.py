@@ -88,7 +88,17 @@ def _perm_cases():
             p[k], p[n - 1 - 2 * k] = p[n - 1 - 2 * k], p[k]
         cases.append(([2] * n, p))
     cases.append(([2] * 20, [1, 0, 2] + list(range(3, 20))))  # run copy
-    cases.append(([4096, 3], [1, 0]))                           # gather fallback (huge inner axis)
+    cases.append(([4096, 3], [1, 0]))                           # huge axis split for the tile
+    # small innermost axes next to a large merged axis: the merged axis is split so the
+    # tile takes only its inner part (top 3 <-> bottom 3 axes, the Tensor::swap of the
+    # outermost and innermost axes, non-power-of-two splits, several tiles per step)
+    n = 20
+    cases.append(([2] * n, [n - 3, n - 2, n - 1] + list(range(3, n - 3)) + [0, 1, 2]))
+    cases.append(([2] * n, [n - 1] + list(range(1, n - 1)) + [0]))
+    cases.append(([3, 1000, 7], [2, 1, 0]))
+    cases.append(([5, 6000], [1, 0]))
+    cases.append(([7, 1009], [1, 0]))                           # prime axis: whole-axis tile
+    cases.append(([3, 4099], [1, 0]))                           # gather fallback (no tile fits)
     return cases
 
 
