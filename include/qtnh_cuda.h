@@ -280,7 +280,8 @@ int qtnh_state_convert(int32_t to_precision, const void* in, void* out, uint64_t
  * renormalised with an FP64 norm; queries return amplitudes as complex128 (host index
  * lists). Qubit q is bit n - 1 - q of the amplitude index (row-major dims [2]*n).
  * qtnh_batch_compile groups the operations of all circuits into rounds of grouped
- * persistent kernels, optionally autotunes the gate kernel, and captures the whole run
+ * persistent kernels (consecutive disjoint gates of a layer applied as one pass),
+ * optionally autotunes the gate kernels, and captures the whole run
  * (state reset from the initial states, every round, the queries) as one CUDA graph;
  * qtnh_batch_run replays it ordered after and before work on `stream`. */
 typedef struct qtnh_batch qtnh_batch;
@@ -301,6 +302,9 @@ int qtnh_batch_run(qtnh_batch* b, void* stream);
 int qtnh_batch_results(qtnh_batch* b, void* out_c128, uint64_t capacity, void* stream);
 /* Final state of circuit c as complex128 (device array of 2^n; synchronizes `stream`). */
 int qtnh_batch_state(qtnh_batch* b, int32_t c, void* out_c128, void* stream);
+/* gate_threads / gate_chunk: the autotuned block size and chunk length of the dominant
+ * gate kernel -- the two-gate pair kernel (chunk in 16-amplitude groups) when the batch
+ * has pair rounds, else the single-gate kernel (chunk in 4-amplitude groups). */
 int qtnh_batch_info(qtnh_batch* b, uint64_t* amplitudes, uint64_t* rounds, uint64_t* launches_per_run,
                     int32_t* gate_threads, uint64_t* gate_chunk);
 

@@ -19,11 +19,14 @@
 // tables, FP64 fused multiply-adds.
 //
 // Scheduling: `compile` groups the operations of all circuits into rounds (layer L: the
-// s-th gate of every circuit that has one, for each slot s; then the phase layers; then
-// the swaps; then the renormalisation), so every round is one launch over a task table
-// (circuit, operand) x chunks; a persistent grid walks the (task, chunk) work items,
-// finding its task by binary search over the tasks' chunk offsets. An autotuner times
-// the gate kernel's block size and chunk length on the largest gate round. The whole
+// gates of each circuit's layer in order, consecutive disjoint gates paired into one pass
+// over the state; the s-th gate item of every circuit for each slot s, pairs and single
+// gates in two launches; then the phase layers; then the swaps; then the
+// renormalisation), so every round is one launch over a task table (circuit, operand) x
+// chunks; a persistent grid walks the (task, chunk) work items, finding its task by
+// binary search over the tasks' chunk offsets. An autotuner times the block size and
+// chunk length of the pair kernel and of the single-gate kernel on their largest rounds.
+// The whole
 // schedule -- state reset from the initial states, norm reset, every round, the
 // queries -- is captured once as a CUDA graph and replayed by `run`.
 
@@ -44,10 +47,18 @@ namespace {
 using c64 = float2;
 using grp::GateTask;
 using grp::NormTask;
+using grp::PairTask;
 using grp::PhaseTask;
 using grp::SwapTask;
 
-enum RoundKind { R_GATE = grp::GATE, R_PHASE = grp::PHASE, R_SWAP = grp::SWAP, R_NORM = grp::NORM, R_SCALE = grp::SCALE };
+enum RoundKind {
+  R_GATE = grp::GATE,
+  R_PHASE = grp::PHASE,
+  R_SWAP = grp::SWAP,
+  R_NORM = grp::NORM,
+  R_SCALE = grp::SCALE,
+  R_PAIR = grp::PAIR
+};
 
 struct Round {
   int kind;
@@ -55,7 +66,8 @@ struct Round {
   uint64_t total = 0;       // work items (chunks)
   void* tasks = nullptr;    // device task table
   uint64_t* cbeg = nullptr; // device chunk offsets (ntasks)
-  uint64_t elems_per_chunk = 0;
+  uint64_t elems_per_chunk = 0;  // amplitudes, or groups (4 amplitudes a gate, 16 a pair)
+  int threads = 256;
 };
 
 using c128 = double2;
@@ -98,8 +110,10 @@ struct qtnh_batch {
   uint64_t nnorms = 0;
   uint64_t* query_where = nullptr;
   double2* query_out = nullptr;
-  int gate_threads = 256;
+  int gate_threads = 256;   // single-gate rounds (chunk in 4-amplitude groups)
   uint64_t gate_chunk = 1024;
+  int pair_threads = 256;   // pair rounds (chunk in 16-amplitude groups)
+  uint64_t pair_chunk = 256;
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -135,9 +149,11 @@ struct qtnh_batch {
   }
 
   template <typename Task>
-  Round make_round(int kind, const std::vector<Task>& tasks, const std::vector<uint64_t>& units, uint64_t chunk) {
+  Round make_round(int kind, const std::vector<Task>& tasks, const std::vector<uint64_t>& units, uint64_t chunk,
+                   int threads = 256) {
     Round r;
     r.kind = kind;
+    r.threads = threads;
     r.ntasks = (uint32_t)tasks.size();
     r.elems_per_chunk = chunk;
     std::vector<uint64_t> cb(tasks.size());
@@ -153,19 +169,31 @@ struct qtnh_batch {
   }
 
   template <typename T>
-  void launch_as(const Round& r, cudaStream_t s, int gthreads, uint64_t gchunk) {
+  void launch_as(const Round& r, cudaStream_t s) {
     const T* g_tab = static_cast<const T*>(gates);
     const T* p_tab = static_cast<const T*>(tables);
+    const uint64_t ch = r.elems_per_chunk;
     switch (r.kind) {
       case R_GATE: {
         const auto* t = static_cast<const GateTask*>(r.tasks);
-        const int g = grid(r.total, gthreads);
-        if (gthreads == 128)
-          grp::gate_kernel<T, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, gchunk);
-        else if (gthreads == 512)
-          grp::gate_kernel<T, 512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, gchunk);
+        const int g = grid(r.total, r.threads);
+        if (r.threads == 128)
+          grp::gate_kernel<T, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
+        else if (r.threads == 512)
+          grp::gate_kernel<T, 512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
         else
-          grp::gate_kernel<T, 256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, gchunk);
+          grp::gate_kernel<T, 256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
+        break;
+      }
+      case R_PAIR: {
+        const auto* t = static_cast<const PairTask*>(r.tasks);
+        const int g = grid(r.total, r.threads);
+        if (r.threads == 128)
+          grp::pair_kernel<T, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
+        else if (r.threads == 512)
+          grp::pair_kernel<T, 512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
+        else
+          grp::pair_kernel<T, 256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
         break;
       }
       case R_PHASE:
@@ -188,11 +216,27 @@ struct qtnh_batch {
     count_launch();
   }
 
-  void launch(const Round& r, cudaStream_t s, int gthreads, uint64_t gchunk) {
+  void launch(const Round& r, cudaStream_t s) {
     if (precision == QTNH_STATE_C128)
-      launch_as<c128>(r, s, gthreads, gchunk);
+      launch_as<c128>(r, s);
     else
-      launch_as<c64>(r, s, gthreads, gchunk);
+      launch_as<c64>(r, s);
+  }
+
+  // The same round with another block size and chunk length (chunk offsets rebuilt).
+  Round rechunk(const Round& r, int threads, uint64_t chunk) {
+    if (r.kind == R_PAIR) {
+      std::vector<PairTask> t(r.ntasks);
+      check_cuda(cudaMemcpy(t.data(), r.tasks, t.size() * sizeof(PairTask), cudaMemcpyDeviceToHost), "tune");
+      std::vector<uint64_t> u;
+      for (auto& x : t) u.push_back(1ull << (x.n - 4));
+      return make_round(R_PAIR, t, u, chunk, threads);
+    }
+    std::vector<GateTask> t(r.ntasks);
+    check_cuda(cudaMemcpy(t.data(), r.tasks, t.size() * sizeof(GateTask), cudaMemcpyDeviceToHost), "tune");
+    std::vector<uint64_t> u;
+    for (auto& x : t) u.push_back(1ull << (x.n - 2));
+    return make_round(R_GATE, t, u, chunk, threads);
   }
 
   // out[i] = psi[where[i]] as complex128
@@ -402,19 +446,45 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
     const int period = renorm_every > 0 ? renorm_every : 0;
     std::vector<uint64_t> norm_slot_base;
     for (int L = 0; L <= b->max_layer; ++L) {
-      for (int slot = 0;; ++slot) {
-        std::vector<GateTask> t;
-        std::vector<uint64_t> u;
-        for (size_t c = 0; c < nc; ++c) {
-          int seen = 0;
-          for (auto& op : b->ops[c])
-            if (op.kind == R_GATE && op.layer == L && seen++ == slot) {
-              t.push_back({b->state_of(c), b->nq[c], b->bit(c, op.qa), b->bit(c, op.qb), op.index});
-              u.push_back(1ull << (b->nq[c] - 2));
-            }
+      // gate items of each circuit's layer L: consecutive disjoint gates as pairs
+      std::vector<std::vector<std::pair<const Op*, const Op*>>> items(nc);
+      size_t nslots = 0;
+      for (size_t c = 0; c < nc; ++c) {
+        std::vector<const Op*> gl;
+        for (auto& op : b->ops[c])
+          if (op.kind == R_GATE && op.layer == L) gl.push_back(&op);
+        for (size_t k = 0; k < gl.size();) {
+          const Op* x = gl[k];
+          const Op* y = k + 1 < gl.size() ? gl[k + 1] : nullptr;
+          if (y && x->qa != y->qa && x->qa != y->qb && x->qb != y->qa && x->qb != y->qb) {
+            items[c].emplace_back(x, y);
+            k += 2;
+          } else {
+            items[c].emplace_back(x, nullptr);
+            k += 1;
+          }
         }
-        if (t.empty()) break;
-        b->rounds.push_back(b->make_round(R_GATE, t, u, b->gate_chunk));
+        nslots = std::max(nslots, items[c].size());
+      }
+      for (size_t slot = 0; slot < nslots; ++slot) {
+        std::vector<PairTask> tp;
+        std::vector<GateTask> tg;
+        std::vector<uint64_t> up, ug;
+        for (size_t c = 0; c < nc; ++c) {
+          if (slot >= items[c].size()) continue;
+          const Op* x = items[c][slot].first;
+          const Op* y = items[c][slot].second;
+          if (y) {
+            tp.push_back({b->state_of(c), b->nq[c], b->bit(c, x->qa), b->bit(c, x->qb), b->bit(c, y->qa),
+                          b->bit(c, y->qb), x->index, y->index});
+            up.push_back(1ull << (b->nq[c] - 4));
+          } else {
+            tg.push_back({b->state_of(c), b->nq[c], b->bit(c, x->qa), b->bit(c, x->qb), x->index});
+            ug.push_back(1ull << (b->nq[c] - 2));
+          }
+        }
+        if (!tp.empty()) b->rounds.push_back(b->make_round(R_PAIR, tp, up, b->pair_chunk, b->pair_threads));
+        if (!tg.empty()) b->rounds.push_back(b->make_round(R_GATE, tg, ug, b->gate_chunk, b->gate_threads));
       }
       {
         std::vector<PhaseTask> t;
@@ -472,46 +542,44 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
       b->allocations.push_back(p);
       b->query_out = static_cast<double2*>(p);
     }
-    // autotune the gate kernel on the largest gate round (block size x chunk length)
+    // autotune the pair and single-gate kernels on their largest rounds (block size x
+    // chunk length); the probes run on the working states, which every run resets
     cudaStream_t s = b->stream;
     if (autotune) {
-      const Round* big = nullptr;
-      for (auto& r : b->rounds)
-        if (r.kind == R_GATE && (!big || r.ntasks > big->ntasks)) big = &r;
-      if (big) {
+      cudaEvent_t e0, e1;
+      check_cuda(cudaEventCreate(&e0), "event");
+      check_cuda(cudaEventCreate(&e1), "event");
+      for (int kind : {R_PAIR, R_GATE}) {
+        const Round* big = nullptr;
+        for (auto& r : b->rounds)
+          if (r.kind == kind && (!big || r.ntasks > big->ntasks)) big = &r;
+        if (!big) continue;
         float best = 1e30f;
-        cudaEvent_t e0, e1;
-        check_cuda(cudaEventCreate(&e0), "event");
-        check_cuda(cudaEventCreate(&e1), "event");
+        int best_th = 256;
+        uint64_t best_ch = kind == R_PAIR ? 256 : 1024;
+        const std::vector<uint64_t> chunks =
+            kind == R_PAIR ? std::vector<uint64_t>{64, 256, 1024} : std::vector<uint64_t>{256, 1024, 4096};
         for (int th : {128, 256, 512})
-          for (uint64_t ch : {256ull, 1024ull, 4096ull}) {
-            // the chunk offsets depend on the chunk length: a probe round per candidate
-            std::vector<GateTask> t(big->ntasks);
-            check_cuda(cudaMemcpy(t.data(), big->tasks, t.size() * sizeof(GateTask), cudaMemcpyDeviceToHost), "tune");
-            std::vector<uint64_t> u;
-            for (auto& x : t) u.push_back(1ull << (x.n - 2));
-            Round probe = b->make_round(R_GATE, t, u, ch);
-            b->launch(probe, s, th, ch);  // warm-up
+          for (uint64_t ch : chunks) {
+            Round probe = b->rechunk(*big, th, ch);
+            b->launch(probe, s);  // warm-up
             check_cuda(cudaEventRecord(e0, s), "event");
-            for (int rep = 0; rep < 3; ++rep) b->launch(probe, s, th, ch);
+            for (int rep = 0; rep < 3; ++rep) b->launch(probe, s);
             check_cuda(cudaEventRecord(e1, s), "event");
             check_cuda(cudaEventSynchronize(e1), "event");
             float ms = 0;
             check_cuda(cudaEventElapsedTime(&ms, e0, e1), "event");
-            if (ms < best) best = ms, b->gate_threads = th, b->gate_chunk = ch;
+            if (ms < best) best = ms, best_th = th, best_ch = ch;
           }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        // rebuild the gate rounds' chunk offsets for the chosen chunk length
+        if (kind == R_PAIR)
+          b->pair_threads = best_th, b->pair_chunk = best_ch;
+        else
+          b->gate_threads = best_th, b->gate_chunk = best_ch;
         for (auto& r : b->rounds)
-          if (r.kind == R_GATE) {
-            std::vector<GateTask> t(r.ntasks);
-            check_cuda(cudaMemcpy(t.data(), r.tasks, t.size() * sizeof(GateTask), cudaMemcpyDeviceToHost), "tune");
-            std::vector<uint64_t> u;
-            for (auto& x : t) u.push_back(1ull << (x.n - 2));
-            r = b->make_round(R_GATE, t, u, b->gate_chunk);
-          }
+          if (r.kind == kind) r = b->rechunk(r, best_th, best_ch);
       }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
     }
     // capture the whole run as one graph
     check_cuda(cudaStreamSynchronize(s), "batch synchronize");
@@ -520,7 +588,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
     check_cuda(cudaMemcpyAsync(b->psi, b->psi0, b->total_amps * b->amp_bytes(), cudaMemcpyDeviceToDevice, s),
                "reset");
     if (b->nnorms) check_cuda(cudaMemsetAsync(b->norms, 0, b->nnorms * sizeof(double), s), "norm reset");
-    for (auto& r : b->rounds) b->launch(r, s, b->gate_threads, b->gate_chunk);
+    for (auto& r : b->rounds) b->launch(r, s);
     if (!where.empty()) b->gather(b->query_where, where.size(), b->query_out, s);
     b->launches_per_run = g_launches.load() - n0;
     g_launches.fetch_sub(b->launches_per_run);  // counted when the graph runs
@@ -567,8 +635,10 @@ int qtnh_batch_info(qtnh_batch* b, uint64_t* amplitudes, uint64_t* rounds, uint6
     if (amplitudes) *amplitudes = b->total_amps;
     if (rounds) *rounds = b->rounds.size();
     if (launches_per_run) *launches_per_run = b->launches_per_run;
-    if (gate_threads) *gate_threads = b->gate_threads;
-    if (gate_chunk) *gate_chunk = b->gate_chunk;
+    bool pairs = false;
+    for (auto& r : b->rounds) pairs = pairs || r.kind == R_PAIR;
+    if (gate_threads) *gate_threads = pairs ? b->pair_threads : b->gate_threads;
+    if (gate_chunk) *gate_chunk = pairs ? b->pair_chunk : b->gate_chunk;
     return QTNH_OK;
   });
 }

@@ -19,6 +19,14 @@ struct GateTask {
   uint32_t ba, bb;  // bit positions of gate inputs 0 and 1
   uint32_t gate;    // index into the gate table
 };
+// Two disjoint two-qubit gates applied in one pass: gate ga on bits (a0, a1), gate gb on
+// bits (b0, b1) (input 0, input 1 of each gate).
+struct PairTask {
+  void* psi;
+  uint32_t n;
+  uint32_t a0, a1, b0, b1;
+  uint32_t ga, gb;
+};
 struct PhaseTask {
   void* psi;
   uint64_t table;  // offset of the lo table (2^split entries); the hi table follows (2^(n - split))
@@ -33,7 +41,7 @@ struct NormTask {
   uint32_t n, slot;  // slot into the norm array
 };
 
-enum Kind { GATE = 0, PHASE = 1, SWAP = 2, NORM = 3, SCALE = 4 };
+enum Kind { GATE = 0, PHASE = 1, SWAP = 2, NORM = 3, SCALE = 4, PAIR = 5 };
 
 template <typename T>
 struct Cx;
@@ -112,6 +120,115 @@ __global__ void __launch_bounds__(THREADS) gate_kernel(const GateTask* __restric
 #pragma unroll
         for (int i = 0; i < 4; ++i) cmac(g[o * 4 + i], x[i], re, im);
         psi[x0 + off[o]] = Cx<T>::make(re, im);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One gate's table entries (GW amplitude-type words, 256 bytes) from shared memory into
+// registers with 128-bit loads that the compiler keeps where they are: each gate is held
+// in registers only while it is applied, so the pair kernel needs one gate's registers.
+template <typename T, int GW>
+union GateRegs {
+  uint4 v[16];
+  T u[GW];
+};
+template <typename T, int GW>
+__device__ __forceinline__ void load_gate(const T* g, GateRegs<T, GW>& r) {
+  static_assert(GW * sizeof(T) == 256, "a gate table entry is 256 bytes");
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(g);
+#pragma unroll
+  for (int k = 0; k < 16; ++k)
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.v[k].x), "=r"(r.v[k].y), "=r"(r.v[k].z), "=r"(r.v[k].w)
+                 : "r"(a + 16u * k));
+}
+
+// Two disjoint gates per task on groups of 16 amplitudes (index (ia, ib), ia the input pair
+// of gate a, ib that of gate b): gate b is applied to the 4 amplitudes of each ia, then
+// gate a to the 4 of each ib, both in registers, so the state is read and written once
+// for the two gates. Same arithmetic per gate as gate_kernel.
+template <typename T, int THREADS>
+__global__ void __launch_bounds__(THREADS) pair_kernel(const PairTask* __restrict__ tasks,
+                                                       const uint64_t* __restrict__ cbeg, uint32_t ntasks,
+                                                       uint64_t total, const T* __restrict__ gates,
+                                                       uint64_t chunk_groups) {
+  using R = typename Cx<T>::R;
+  constexpr int GW = Cx<T>::GATE_WORDS;
+  __shared__ __align__(16) T g[2][GW];
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const PairTask t = tasks[s_task];
+    if (threadIdx.x < 2 * GW) {
+      const int k = threadIdx.x / GW, j = threadIdx.x % GW;
+      g[k][j] = gates[(uint64_t)(k ? t.gb : t.ga) * GW + j];
+    }
+    __syncthreads();
+    T* psi = static_cast<T*>(t.psi);
+    const uint64_t ngroups = 1ull << (t.n - 4);
+    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
+    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
+    // zero bits inserted in increasing position order
+    uint32_t pos[4] = {t.a0, t.a1, t.b0, t.b1};
+#pragma unroll
+    for (int i = 1; i < 4; ++i)
+#pragma unroll
+      for (int j = 3; j >= i; --j)
+        if (pos[j - 1] > pos[j]) {
+          const uint32_t tmp = pos[j - 1];
+          pos[j - 1] = pos[j];
+          pos[j] = tmp;
+        }
+    uint64_t offa[4], offb[4];  // (input 0, input 1) = (0,0), (0,1), (1,0), (1,1)
+    offa[0] = 0, offa[1] = 1ull << t.a1, offa[2] = 1ull << t.a0, offa[3] = offa[1] + offa[2];
+    offb[0] = 0, offb[1] = 1ull << t.b1, offb[2] = 1ull << t.b0, offb[3] = offb[1] + offb[2];
+    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
+      uint64_t x0 = grp;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x0 = insert_zero(x0, pos[i]);
+      T x[16];
+#pragma unroll
+      for (int ia = 0; ia < 4; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < 4; ++ib) x[ia * 4 + ib] = psi[x0 + offa[ia] + offb[ib]];
+      GateRegs<T, GW> u;
+      // gate b on each quadruple of fixed ia
+      load_gate<T, GW>(g[1], u);
+#pragma unroll
+      for (int ia = 0; ia < 4; ++ia) {
+        T y[4];
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+          R re = 0, im = 0;
+          if (GW == 32) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cmac(u.u[16 + o * 4 + i], x[ia * 4 + i], re, im);
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cmac(u.u[o * 4 + i], x[ia * 4 + i], re, im);
+          y[o] = Cx<T>::make(re, im);
+        }
+#pragma unroll
+        for (int o = 0; o < 4; ++o) x[ia * 4 + o] = y[o];
+      }
+      // gate a on each quadruple of fixed ib, stored
+      load_gate<T, GW>(g[0], u);
+#pragma unroll
+      for (int ib = 0; ib < 4; ++ib) {
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+          R re = 0, im = 0;
+          if (GW == 32) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cmac(u.u[16 + o * 4 + i], x[i * 4 + ib], re, im);
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cmac(u.u[o * 4 + i], x[i * 4 + ib], re, im);
+          psi[x0 + offa[o] + offb[ib]] = Cx<T>::make(re, im);
+        }
       }
     }
     __syncthreads();

@@ -363,7 +363,9 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
     if (smem > 48 * 1024)
       check_cuda(cudaFuncSetAttribute(tiled_permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                  "tiled_permute_kernel shared memory");
-    int grid = grid_for((p.rest.total + p.G - 1) / p.G, 3);
+    // as many blocks per SM as shared memory allows (at most 8 blocks of 256 threads)
+    const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (220 * 1024) / (smem + 1024)));
+    int grid = grid_for((p.rest.total + p.G - 1) / p.G, per_sm);
     tiled_permute_kernel<<<grid, TILE_THREADS, smem, s>>>(in, out, p);
     count_launch();
     check_cuda(cudaGetLastError(), "tiled_permute_kernel launch");
