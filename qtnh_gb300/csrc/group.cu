@@ -1,6 +1,7 @@
 // Grouped operations on many independent resident states, for a request loop that
 // advances all admitted requests together: one call applies the next layer of every
-// given state (its two-qubit SymmTensor gates slot by slot, its phase DiagTensor layer,
+// given state (its two-qubit SymmTensor gates slot by slot -- consecutive disjoint gates
+// as one pass of the pair kernel --, its phase DiagTensor layer,
 // its SwapTensor exchange) as a few grouped launches (group_kernels.cuh), in plain
 // complex128 (FP64 arithmetic) or mixed complex64 (FP32 arithmetic with split gates);
 // plus FP64 renormalisation, amplitude gathers, and the 4-qubit reduced density matrix
@@ -18,6 +19,7 @@ namespace qtnh_impl {
 namespace {
 
 constexpr uint64_t G_GATE_CHUNK = 1024;  // groups per work item
+constexpr uint64_t G_PAIR_CHUNK = 256;   // 16-amplitude groups per work item of the pair kernel
 constexpr uint64_t G_CHUNK = 4096;       // amplitudes (pairs) per work item
 constexpr uint16_t NO_SWAP = 0xFFFF;
 
@@ -92,9 +94,8 @@ void group_layer(int32_t ns, void* const* states, const int32_t* nq, const int32
       }
   Upload up;
   const size_t gate_off = up.add(table.data(), table.size() * sizeof(T));
-  // gate rounds: slot k holds the k-th gate of every state that has one
-  int max_gates = 0;
-  for (int32_t i = 0; i < ns; ++i) max_gates = std::max(max_gates, (int)ngates[i]);
+  // gate items per state: consecutive disjoint gates paired; slot k holds the k-th item
+  // of every state that has one (pairs and single gates in two launches)
   struct RoundRef {
     int kind;
     size_t tasks, cbeg;
@@ -102,20 +103,58 @@ void group_layer(int32_t ns, void* const* states, const int32_t* nq, const int32
     uint64_t total;
   };
   std::vector<RoundRef> rounds;
-  for (int k = 0; k < max_gates; ++k) {
-    std::vector<grp::GateTask> t;
-    std::vector<uint64_t> u, cb;
-    for (int32_t i = 0; i < ns; ++i) {
-      if (k >= ngates[i]) continue;
+  std::vector<std::vector<std::pair<int, int>>> items(ns);  // (gate, second gate or -1)
+  size_t nslots = 0;
+  for (int32_t i = 0; i < ns; ++i) {
+    for (int k = 0; k < ngates[i]; ++k) {
       const uint16_t qa = pairs[2 * (first_gate[i] + k)], qb = pairs[2 * (first_gate[i] + k) + 1];
-      if (qa >= (uint32_t)nq[i] || qb >= (uint32_t)nq[i] || qa == qb) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid gate qubits");
-      t.push_back({states[i], (uint32_t)nq[i], (uint32_t)(nq[i] - 1 - qa), (uint32_t)(nq[i] - 1 - qb),
-                   (uint32_t)(first_gate[i] + k)});
-      u.push_back(1ull << (nq[i] - 2));
+      if (qa >= (uint32_t)nq[i] || qb >= (uint32_t)nq[i] || qa == qb)
+        throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid gate qubits");
     }
-    const uint64_t total = chunk_offsets(t, u, G_GATE_CHUNK, cb);
-    rounds.push_back({grp::GATE, up.add(t.data(), t.size() * sizeof(t[0])), up.add(cb.data(), cb.size() * 8),
-                      (uint32_t)t.size(), total});
+    for (int k = 0; k < ngates[i];) {
+      const uint16_t* x = pairs + 2 * (first_gate[i] + k);
+      if (k + 1 < ngates[i]) {
+        const uint16_t* y = x + 2;
+        if (x[0] != y[0] && x[0] != y[1] && x[1] != y[0] && x[1] != y[1]) {
+          items[i].emplace_back(k, k + 1);
+          k += 2;
+          continue;
+        }
+      }
+      items[i].emplace_back(k, -1);
+      k += 1;
+    }
+    nslots = std::max(nslots, items[i].size());
+  }
+  for (size_t k = 0; k < nslots; ++k) {
+    std::vector<grp::PairTask> tp;
+    std::vector<grp::GateTask> tg;
+    std::vector<uint64_t> up_, ug, cbp, cbg;
+    for (int32_t i = 0; i < ns; ++i) {
+      if (k >= items[i].size()) continue;
+      const int ga = items[i][k].first, gb = items[i][k].second;
+      const uint32_t n = (uint32_t)nq[i];
+      const uint16_t* x = pairs + 2 * (first_gate[i] + ga);
+      if (gb >= 0) {
+        const uint16_t* y = pairs + 2 * (first_gate[i] + gb);
+        tp.push_back({states[i], n, n - 1 - x[0], n - 1 - x[1], n - 1 - y[0], n - 1 - y[1],
+                      (uint32_t)(first_gate[i] + ga), (uint32_t)(first_gate[i] + gb)});
+        up_.push_back(1ull << (n - 4));
+      } else {
+        tg.push_back({states[i], n, n - 1 - x[0], n - 1 - x[1], (uint32_t)(first_gate[i] + ga)});
+        ug.push_back(1ull << (n - 2));
+      }
+    }
+    if (!tp.empty()) {
+      const uint64_t total = chunk_offsets(tp, up_, G_PAIR_CHUNK, cbp);
+      rounds.push_back({grp::PAIR, up.add(tp.data(), tp.size() * sizeof(tp[0])), up.add(cbp.data(), cbp.size() * 8),
+                        (uint32_t)tp.size(), total});
+    }
+    if (!tg.empty()) {
+      const uint64_t total = chunk_offsets(tg, ug, G_GATE_CHUNK, cbg);
+      rounds.push_back({grp::GATE, up.add(tg.data(), tg.size() * sizeof(tg[0])), up.add(cbg.data(), cbg.size() * 8),
+                        (uint32_t)tg.size(), total});
+    }
   }
   // phase round
   size_t tab_off = 0;
@@ -168,7 +207,11 @@ void group_layer(int32_t ns, void* const* states, const int32_t* nq, const int32
   try {
     for (auto& r : rounds) {
       const uint64_t* cb = reinterpret_cast<const uint64_t*>(up.dev + r.cbeg);
-      if (r.kind == grp::GATE)
+      if (r.kind == grp::PAIR)
+        grp::pair_kernel<T, 256><<<grid_items(r.total, 256), 256, 0, s>>>(
+            reinterpret_cast<const grp::PairTask*>(up.dev + r.tasks), cb, r.ntasks, r.total,
+            reinterpret_cast<const T*>(up.dev + gate_off), G_PAIR_CHUNK);
+      else if (r.kind == grp::GATE)
         grp::gate_kernel<T, 256><<<grid_items(r.total, 256), 256, 0, s>>>(
             reinterpret_cast<const grp::GateTask*>(up.dev + r.tasks), cb, r.ntasks, r.total,
             reinterpret_cast<const T*>(up.dev + gate_off), G_GATE_CHUNK);

@@ -35,6 +35,8 @@ namespace {
 constexpr int TILE_MAX = 1024;   // elements per transpose tile
 constexpr int TILE_THREADS = 256;
 constexpr int STEP_ELEMS = 2048;  // elements of the tiles moved per step of a block (power-of-two tiles)
+constexpr int TILE_PER_THREAD = STEP_ELEMS / TILE_THREADS;
+static_assert(TILE_MAX <= STEP_ELEMS, "one step holds at least one tile");
 
 
 struct TileParams {
@@ -55,7 +57,7 @@ struct RunParams {
   uint32_t L_log2;
 };
 
-__global__ void __launch_bounds__(TILE_THREADS) tiled_permute_kernel(const c128* __restrict__ in, c128* __restrict__ out,
+__global__ void __launch_bounds__(TILE_THREADS, 4) tiled_permute_kernel(const c128* __restrict__ in, c128* __restrict__ out,
                                                                      const __grid_constant__ TileParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = p.T, G = p.G, S = p.tile_slots;
@@ -82,15 +84,30 @@ __global__ void __launch_bounds__(TILE_THREADS) tiled_permute_kernel(const c128*
     }
     __syncthreads();
     const uint64_t left = total - r0;
-    const int n = (left < (uint64_t)G ? (int)left : G) * T;
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-      const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-      tile[g * S + s_rslot[t]] = __ldg(in + s_bin[g] + s_rin[t]);
+    const int n = (left < (uint64_t)G ? (int)left : G) * T;  // <= STEP_ELEMS
+    // all of this thread's loads are issued before any is stored to shared memory
+    c128 v[TILE_PER_THREAD];
+    int slot[TILE_PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < TILE_PER_THREAD; ++k) {
+      const int e = threadIdx.x + k * TILE_THREADS;
+      if (e < n) {
+        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+        slot[k] = g * S + s_rslot[t];
+        v[k] = __ldg(in + s_bin[g] + s_rin[t]);
+      }
     }
+#pragma unroll
+    for (int k = 0; k < TILE_PER_THREAD; ++k)
+      if (threadIdx.x + k * TILE_THREADS < n) tile[slot[k]] = v[k];
     __syncthreads();
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-      const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-      out[s_bout[g] + s_wout[t]] = tile[g * S + s_wslot[t]];
+#pragma unroll
+    for (int k = 0; k < TILE_PER_THREAD; ++k) {
+      const int e = threadIdx.x + k * TILE_THREADS;
+      if (e < n) {
+        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+        out[s_bout[g] + s_wout[t]] = tile[g * S + s_wslot[t]];
+      }
     }
     __syncthreads();
   }
@@ -363,8 +380,8 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
     if (smem > 48 * 1024)
       check_cuda(cudaFuncSetAttribute(tiled_permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                  "tiled_permute_kernel shared memory");
-    // as many blocks per SM as shared memory allows (at most 8 blocks of 256 threads)
-    const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (220 * 1024) / (smem + 1024)));
+    // as many blocks per SM as shared memory and registers allow (at most 4)
+    const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (smem + 1024)));
     int grid = grid_for((p.rest.total + p.G - 1) / p.G, per_sm);
     tiled_permute_kernel<<<grid, TILE_THREADS, smem, s>>>(in, out, p);
     count_launch();
