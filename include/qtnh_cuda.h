@@ -271,8 +271,9 @@ int qtnh_state_convert(int32_t to_precision, const void* in, void* out, uint64_t
 /* ---- batched circuits ---------------------------------------------------------------- */
 
 /* Many independent circuits of uneven qubit counts and depths, states resident in HBM:
- * complex64 with FP32 math (mixed precision; qtnh_batch_create) or complex128 with FP64
- * math (the plain method; qtnh_batch_create_typed with QTNH_STATE_C128). Operations per circuit follow the layered-circuit contractions: two-qubit
+ * complex64 (mixed precision; qtnh_batch_create: gates in exact 64-bit fixed-point sums
+ * with one rounding per output, phases in FP32) or complex128 with FP64 math (the plain
+ * method; qtnh_batch_create_typed with QTNH_STATE_C128). Operations per circuit follow the layered-circuit contractions: two-qubit
  * SymmTensor gates (els in SymmTensor layout, host pointer to 16 complex128; input 0 on
  * qubit qa, input 1 on qb; include/tensor/symm.hpp:22-45), a phase layer (n host
  * phases: DiagTensor (1, e^{i phase}) on every qubit) and SwapTensor qubit exchanges,

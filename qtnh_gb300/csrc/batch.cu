@@ -10,11 +10,13 @@
 // renormalised with an FP64 norm, and the circuit ends in amplitude queries returned in
 // complex128.
 //
-// Mixed-precision arithmetic: amplitudes complex64; a gate U is held as two complex64 matrices
-// U = U_hi + U_lo (the FP64 gate to ~48 bits), and each output sum_i (U_lo x_i) +
-// (U_hi x_i) is accumulated with FP32 fused multiply-adds, so the only rounding of note is
-// the store to complex64. Phase layers multiply by lo/hi tables of per-qubit phase
-// products (built in FP64, stored complex64). Norms: per-thread compensated FP32 sums
+// Mixed-precision arithmetic: amplitudes complex64; gates in exact fixed point
+// (group_kernels.cuh: each group of amplitudes scaled to 29-bit integers at its largest
+// exponent, the gate to 30-bit integers, products summed exactly in 64-bit integers,
+// one rounding per output when it is converted back to complex64; QTNH_BATCH_GATES=fp32
+// selects FP32 accumulation with the gate held as complex64 U_hi + U_lo instead). Phase
+// layers multiply by lo/hi tables of per-qubit phase products (built in FP64, stored
+// complex64). Norms: per-thread compensated FP32 sums
 // (TwoSum) reduced in FP64. Plain arithmetic: complex128 amplitudes, gates and phase
 // tables, FP64 fused multiply-adds.
 //
@@ -34,6 +36,7 @@
 #include <cmath>
 #include <complex>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "group_kernels.cuh"
@@ -105,6 +108,8 @@ struct qtnh_batch {
   std::vector<Round> rounds;
   std::vector<void*> allocations;
   void* gates = nullptr;   // c64: U_hi[16], U_lo[16] per gate; c128: U[16]
+  grp::FxGate* fx_gates = nullptr;  // c64: the exact fixed-point form (used unless fp32_gates)
+  bool fp32_gates = false;          // c64: FP32 gate arithmetic (QTNH_BATCH_GATES=fp32)
   void* tables = nullptr;  // phase tables in the state's type
   double* norms = nullptr;
   uint64_t nnorms = 0;
@@ -177,6 +182,15 @@ struct qtnh_batch {
       case R_GATE: {
         const auto* t = static_cast<const GateTask*>(r.tasks);
         const int g = grid(r.total, r.threads);
+        if (fx_gates && !fp32_gates) {
+          if (r.threads == 128)
+            grp::fx_gate_kernel<128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
+          else if (r.threads == 512)
+            grp::fx_gate_kernel<512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
+          else
+            grp::fx_gate_kernel<256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
+          break;
+        }
         if (r.threads == 128)
           grp::gate_kernel<T, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
         else if (r.threads == 512)
@@ -188,6 +202,15 @@ struct qtnh_batch {
       case R_PAIR: {
         const auto* t = static_cast<const PairTask*>(r.tasks);
         const int g = grid(r.total, r.threads);
+        if (fx_gates && !fp32_gates) {
+          if (r.threads == 128)
+            grp::fx_pair_kernel<128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
+          else if (r.threads == 512)
+            grp::fx_pair_kernel<512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
+          else
+            grp::fx_pair_kernel<256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
+          break;
+        }
         if (r.threads == 128)
           grp::pair_kernel<T, 128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, g_tab, ch);
         else if (r.threads == 512)
@@ -411,6 +434,11 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
         }
       }
       b->gates = b->upload(g);
+      std::vector<grp::FxGate> fx;
+      for (size_t g0 = 0; g0 < b->gate_host.size(); g0 += 16) fx.push_back(grp::make_fx_gate(&b->gate_host[g0]));
+      b->fx_gates = b->upload(fx);
+      const char* env = std::getenv("QTNH_BATCH_GATES");
+      b->fp32_gates = env && std::string(env) == "fp32";
     }
     // phase tables: per phase op, lo table over the low `split` bits and hi table over the rest
     std::vector<c128> tab;

@@ -3,7 +3,8 @@
 // given state (its two-qubit SymmTensor gates slot by slot -- consecutive disjoint gates
 // as one pass of the pair kernel --, its phase DiagTensor layer,
 // its SwapTensor exchange) as a few grouped launches (group_kernels.cuh), in plain
-// complex128 (FP64 arithmetic) or mixed complex64 (FP32 arithmetic with split gates);
+// complex128 (FP64 arithmetic) or mixed complex64 (gates in exact fixed point, phases in
+// FP32 with split tables);
 // plus FP64 renormalisation, amplitude gathers, and the 4-qubit reduced density matrix
 // as a contracted-index sum in FP64 (rho = sum over the other indices of psi psi^*, the
 // contraction of the state with its conjugate, src/tensor/contract.cpp:12-201).
@@ -94,6 +95,19 @@ void group_layer(int32_t ns, void* const* states, const int32_t* nq, const int32
       }
   Upload up;
   const size_t gate_off = up.add(table.data(), table.size() * sizeof(T));
+  // complex64: the exact fixed-point gate form (group_kernels.cuh)
+  constexpr bool fx = GW == 32;
+  size_t fx_off = 0;
+  if (fx) {
+    std::vector<grp::FxGate> fxt(ng);
+    for (size_t g = 0; g < ng; ++g) {
+      std::complex<double> U[16];
+      for (int o = 0; o < 4; ++o)
+        for (int in = 0; in < 4; ++in) U[o * 4 + in] = els[g * 16 + in * 4 + o];
+      fxt[g] = grp::make_fx_gate(U);
+    }
+    fx_off = up.add(fxt.data(), fxt.size() * sizeof(grp::FxGate));
+  }
   // gate items per state: consecutive disjoint gates paired; slot k holds the k-th item
   // of every state that has one (pairs and single gates in two launches)
   struct RoundRef {
@@ -207,7 +221,14 @@ void group_layer(int32_t ns, void* const* states, const int32_t* nq, const int32
   try {
     for (auto& r : rounds) {
       const uint64_t* cb = reinterpret_cast<const uint64_t*>(up.dev + r.cbeg);
-      if (r.kind == grp::PAIR)
+      const grp::FxGate* fxg = reinterpret_cast<const grp::FxGate*>(up.dev + fx_off);
+      if (fx && r.kind == grp::PAIR)
+        grp::fx_pair_kernel<256><<<grid_items(r.total, 256), 256, 0, s>>>(
+            reinterpret_cast<const grp::PairTask*>(up.dev + r.tasks), cb, r.ntasks, r.total, fxg, G_PAIR_CHUNK);
+      else if (fx && r.kind == grp::GATE)
+        grp::fx_gate_kernel<256><<<grid_items(r.total, 256), 256, 0, s>>>(
+            reinterpret_cast<const grp::GateTask*>(up.dev + r.tasks), cb, r.ntasks, r.total, fxg, G_GATE_CHUNK);
+      else if (r.kind == grp::PAIR)
         grp::pair_kernel<T, 256><<<grid_items(r.total, 256), 256, 0, s>>>(
             reinterpret_cast<const grp::PairTask*>(up.dev + r.tasks), cb, r.ntasks, r.total,
             reinterpret_cast<const T*>(up.dev + gate_off), G_PAIR_CHUNK);

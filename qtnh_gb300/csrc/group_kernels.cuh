@@ -7,6 +7,11 @@
 // (group.cu).
 #pragma once
 
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+
 #include "cuda_common.cuh"
 #include "df32.cuh"
 
@@ -228,6 +233,261 @@ __global__ void __launch_bounds__(THREADS) pair_kernel(const PairTask* __restric
 #pragma unroll
           for (int i = 0; i < 4; ++i) cmac(u.u[o * 4 + i], x[i * 4 + ib], re, im);
           psi[x0 + offa[o] + offb[ib]] = Cx<T>::make(re, im);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- exact fixed-point gates for complex64 states ----------------------------------
+//
+// Each group of amplitudes is scaled to integers at its largest exponent E:
+// x_int = round(x * 2^(155 - E)) (|x_int| < 2^29); a gate is held as integers
+// u_int = round(u * 2^s) (|u_int| < 2^30, s from the gate's largest entry). Products
+// accumulate exactly in 64-bit integers (IMAD.WIDE), so an output carries one rounding:
+// its conversion to float. Between the two gates of a pair the sums are brought back to
+// 32 bits (right shift by the gate's `shift`, |y| < 2^29 by the row bound of the gate).
+// Error per pass: the final rounding to complex64, plus 2^-28 of the group's largest
+// amplitude from the integer scaling.
+struct FxGate {
+  int2 u[16];      // (Re, Im) of U[out * 4 + in] as integers at scale 2^s
+  int32_t s;       // u = u_int * 2^-s
+  int32_t shift;   // requantisation of a first-stage sum: y32 = round(y64 / 2^shift)
+  int32_t pad[2];
+};
+static_assert(sizeof(FxGate) == 144, "FxGate layout");
+
+// Host: the fixed-point form of U[out * 4 + in] (complex128).
+inline FxGate make_fx_gate(const std::complex<double>* U) {
+  FxGate g{};
+  double mx = 0;
+  for (int k = 0; k < 16; ++k) mx = std::max(mx, std::max(std::fabs(U[k].real()), std::fabs(U[k].imag())));
+  const int eu = mx > 0 ? std::ilogb(mx) : 0;  // mx in [2^eu, 2^(eu + 1))
+  g.s = 29 - eu;                                // |u_int| <= 2^30
+  long long bound = 0;
+  for (int o = 0; o < 4; ++o) {
+    long long b = 0;
+    for (int i = 0; i < 4; ++i) {
+      const long long ur = std::llrint(std::ldexp(U[o * 4 + i].real(), g.s));
+      const long long ui = std::llrint(std::ldexp(U[o * 4 + i].imag(), g.s));
+      g.u[o * 4 + i] = make_int2((int)ur, (int)ui);
+      b += std::llabs(ur) + std::llabs(ui);
+    }
+    bound = std::max(bound, b);
+  }
+  // |x_int| <= 2^29, so |y64| <= bound 2^29; shift so that |y32| <= 2^29 (+ rounding)
+  int shift = 1;
+  while (shift < 62 && (1ll << shift) < bound) ++shift;
+  g.shift = shift;
+  return g;
+}
+
+// float bits of 2^k for k in [-126, 127]
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+
+// Scale exponent of a group whose largest |component| has float bits `m` (sign cleared):
+// x * 2^se puts the largest below 2^29 (and at or above 2^28 unless the group is tiny).
+__device__ __forceinline__ int fx_scale_exp(uint32_t m) {
+  const int E = (int)(m >> 23);
+  return max(-99, min(126, 155 - E));
+}
+
+__device__ __forceinline__ float fx_to_float(long long v, int k) { return ldexpf(__ll2float_rn(v), k); }
+
+// One complex output o of gate g over 4 integer inputs (re, im): 64-bit exact sums.
+__device__ __forceinline__ void fx_row(const FxGate& g, int o, const int (&xr)[4], const int (&xi)[4], long long& re,
+                                       long long& im) {
+  re = 0;
+  im = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int2 u = g.u[o * 4 + i];
+    re += (long long)u.x * xr[i] - (long long)u.y * xi[i];
+    im += (long long)u.x * xi[i] + (long long)u.y * xr[i];
+  }
+}
+
+// The 16 integer entries of a gate from shared memory into registers with loads the
+// compiler keeps in place (one gate in registers at a time in the pair kernel).
+struct FxRegs {
+  int2 u[16];
+};
+__device__ __forceinline__ void fx_load(const FxGate& g, FxRegs& r) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(&g.u[0]);
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.u[2 * k].x), "=r"(r.u[2 * k].y), "=r"(r.u[2 * k + 1].x), "=r"(r.u[2 * k + 1].y)
+                 : "r"(a + 16u * k));
+}
+
+// fx_row over register-held entries
+__device__ __forceinline__ void fx_row_r(const FxRegs& g, int o, const int (&xr)[4], const int (&xi)[4],
+                                         long long& re, long long& im) {
+  re = 0;
+  im = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int2 u = g.u[o * 4 + i];
+    re += (long long)u.x * xr[i] - (long long)u.y * xi[i];
+    im += (long long)u.x * xi[i] + (long long)u.y * xr[i];
+  }
+}
+
+__device__ __forceinline__ int fx_requant(long long y, int shift) {
+  return (int)((y + (1ll << (shift - 1))) >> shift);
+}
+
+// Single two-qubit gate per task, groups of 4 amplitudes (complex64).
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) fx_gate_kernel(const GateTask* __restrict__ tasks,
+                                                          const uint64_t* __restrict__ cbeg, uint32_t ntasks,
+                                                          uint64_t total, const FxGate* __restrict__ gates,
+                                                          uint64_t chunk_groups) {
+  __shared__ __align__(16) FxGate g;
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const GateTask t = tasks[s_task];
+    if (threadIdx.x < 36) reinterpret_cast<int*>(&g)[threadIdx.x] = reinterpret_cast<const int*>(gates + t.gate)[threadIdx.x];
+    __syncthreads();
+    float2* psi = static_cast<float2*>(t.psi);
+    const uint64_t ngroups = 1ull << (t.n - 2);
+    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
+    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
+    const uint32_t lo = min(t.ba, t.bb), hi = max(t.ba, t.bb);
+    const uint64_t off[4] = {0, 1ull << t.bb, 1ull << t.ba, (1ull << t.ba) + (1ull << t.bb)};
+    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
+      const uint64_t x0 = insert_zero(insert_zero(grp, lo), hi);
+      float2 x[4];
+      uint32_t m = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        x[i] = psi[x0 + off[i]];
+        m = max(m, max(__float_as_uint(x[i].x) & 0x7FFFFFFFu, __float_as_uint(x[i].y) & 0x7FFFFFFFu));
+      }
+      if (m >= 0x7F800000u) {  // an infinity or NaN: the group's outputs are NaN
+#pragma unroll
+        for (int o = 0; o < 4; ++o) psi[x0 + off[o]] = make_float2(__int_as_float(0x7FC00000), __int_as_float(0x7FC00000));
+        continue;
+      }
+      const int se = fx_scale_exp(m);
+      const float sc = pow2f(se);
+      int xr[4], xi[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) xr[i] = __float2int_rn(x[i].x * sc), xi[i] = __float2int_rn(x[i].y * sc);
+      const int k = -se - g.s;
+#pragma unroll
+      for (int o = 0; o < 4; ++o) {
+        long long re, im;
+        fx_row(g, o, xr, xi, re, im);
+        psi[x0 + off[o]] = make_float2(fx_to_float(re, k), fx_to_float(im, k));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Two disjoint gates per task (as pair_kernel) in exact fixed point: gate b on each
+// quadruple of fixed ia, requantised to 32 bits, then gate a on each quadruple of fixed ib.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS) fx_pair_kernel(const PairTask* __restrict__ tasks,
+                                                          const uint64_t* __restrict__ cbeg, uint32_t ntasks,
+                                                          uint64_t total, const FxGate* __restrict__ gates,
+                                                          uint64_t chunk_groups) {
+  __shared__ __align__(16) FxGate g[2];
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) s_task = find_task(cbeg, ntasks, w);
+    __syncthreads();
+    const PairTask t = tasks[s_task];
+    if (threadIdx.x < 72) {
+      const int k = threadIdx.x / 36, j = threadIdx.x % 36;
+      reinterpret_cast<int*>(&g[k])[j] = reinterpret_cast<const int*>(gates + (k ? t.gb : t.ga))[j];
+    }
+    __syncthreads();
+    float2* psi = static_cast<float2*>(t.psi);
+    const uint64_t ngroups = 1ull << (t.n - 4);
+    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
+    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
+    uint32_t pos[4] = {t.a0, t.a1, t.b0, t.b1};
+#pragma unroll
+    for (int i = 1; i < 4; ++i)
+#pragma unroll
+      for (int j = 3; j >= i; --j)
+        if (pos[j - 1] > pos[j]) {
+          const uint32_t tmp = pos[j - 1];
+          pos[j - 1] = pos[j];
+          pos[j] = tmp;
+        }
+    uint64_t offa[4], offb[4];
+    offa[0] = 0, offa[1] = 1ull << t.a1, offa[2] = 1ull << t.a0, offa[3] = offa[1] + offa[2];
+    offb[0] = 0, offb[1] = 1ull << t.b1, offb[2] = 1ull << t.b0, offb[3] = offb[1] + offb[2];
+    const int sa = g[0].s, sb = g[1].s, shb = g[1].shift;
+    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
+      uint64_t x0 = grp;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x0 = insert_zero(x0, pos[i]);
+      int xr[16], xi[16];
+      int k;  // output scale: value = sum * 2^k
+      {
+        float2 x[16];
+        uint32_t m = 0;
+#pragma unroll
+        for (int ia = 0; ia < 4; ++ia)
+#pragma unroll
+          for (int ib = 0; ib < 4; ++ib) {
+            const float2 v = psi[x0 + offa[ia] + offb[ib]];
+            x[ia * 4 + ib] = v;
+            m = max(m, max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu));
+          }
+        if (m >= 0x7F800000u) {  // an infinity or NaN: the group's outputs are NaN
+#pragma unroll
+          for (int ia = 0; ia < 4; ++ia)
+#pragma unroll
+            for (int ib = 0; ib < 4; ++ib) psi[x0 + offa[ia] + offb[ib]] = make_float2(__int_as_float(0x7FC00000), __int_as_float(0x7FC00000));
+          continue;
+        }
+        const int se = fx_scale_exp(m);
+        const float sc = pow2f(se);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) xr[i] = __float2int_rn(x[i].x * sc), xi[i] = __float2int_rn(x[i].y * sc);
+        k = -se - sb + shb - sa;
+      }
+      {
+        FxRegs u;
+        // gate b on each quadruple of fixed ia (requantised in place)
+        fx_load(g[1], u);
+#pragma unroll
+        for (int ia = 0; ia < 4; ++ia) {
+          int vr[4], vi[4], yr[4], yi[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) vr[i] = xr[ia * 4 + i], vi[i] = xi[ia * 4 + i];
+#pragma unroll
+          for (int o = 0; o < 4; ++o) {
+            long long re, im;
+            fx_row_r(u, o, vr, vi, re, im);
+            yr[o] = fx_requant(re, shb);
+            yi[o] = fx_requant(im, shb);
+          }
+#pragma unroll
+          for (int o = 0; o < 4; ++o) xr[ia * 4 + o] = yr[o], xi[ia * 4 + o] = yi[o];
+        }
+        // gate a on each quadruple of fixed ib, stored
+        fx_load(g[0], u);
+#pragma unroll
+        for (int ib = 0; ib < 4; ++ib) {
+          int vr[4], vi[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) vr[i] = xr[i * 4 + ib], vi[i] = xi[i * 4 + ib];
+#pragma unroll
+          for (int o = 0; o < 4; ++o) {
+            long long re, im;
+            fx_row_r(u, o, vr, vi, re, im);
+            psi[x0 + offa[o] + offb[ib]] = make_float2(fx_to_float(re, k), fx_to_float(im, k));
+          }
         }
       }
     }

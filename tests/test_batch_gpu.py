@@ -150,6 +150,28 @@ def test_batch_overlapping_gates_in_a_layer(precision, bar):
         assert rel(b.state(i).cpu().numpy(), orc.run_circuit(states[i], c)) < bar
 
 
+def test_batch_deep_circuits_within_1e6():
+    # the mixed-precision bar of the batched form: 1e-6 relative L2 against the FP64 oracle
+    # on circuits of ~320 gates per amplitude (depth 40 at 16 qubits): the gates sum their
+    # products exactly in 64-bit integers, so each pass over a state rounds once
+    circuits = wl.batch_circuits(3, seed=91, qubits=(15, 16), depth=(40, 40))
+    b = q.Batch([c.n for c, _ in circuits])
+    states = []
+    for i, (c, qi) in enumerate(circuits):
+        psi = wl.random_state(c.n, seed=500 + i)
+        states.append(psi)
+        b.set_state(i, dev(psi))
+        b.add_circuit(i, c, qi)
+    b.compile(renorm_every=8, autotune=False)
+    b.run()
+    for i, (c, _) in enumerate(circuits):
+        ref = orc.run_circuit(states[i], c)
+        got = b.state(i).cpu().numpy()
+        assert rel(got, ref) < 1e-6, (c.n, rel(got, ref))
+        fid = abs(np.vdot(ref, got)) ** 2 / (np.vdot(ref, ref).real * np.vdot(got, got).real)
+        assert fid > 1 - 1e-9
+
+
 def test_batch_rejects_invalid_operations():
     b = q.Batch([10, 12])
     eye = np.eye(4, dtype=np.complex128).reshape(-1)
