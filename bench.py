@@ -650,8 +650,35 @@ def main_batch(a):
     q_vs_plain = [float(np.linalg.norm(res[offq[i]:offq[i + 1]] - pres[offq[i]:offq[i + 1]]) /
                         np.linalg.norm(pres[offq[i]:offq[i + 1]])) for i in range(len(circuits))]
     largest = sorted(range(len(circuits)), key=lambda i: -circuits[i][0].n)[:8]
-    s_vs_plain = [_state_errors(b.state(i).cpu().numpy(), bp.state(i).cpu().numpy()) for i in largest]
+    plain_states = {i: bp.state(i).cpu().numpy() for i in largest}
+    s_vs_plain = [_state_errors(b.state(i).cpu().numpy(), plain_states[i]) for i in largest]
     del bp
+
+    # the same complex64 batch with FP32 gate sums (QTNH_BATCH_GATES=fp32): the faster,
+    # less accurate point of the trade-off
+    os.environ["QTNH_BATCH_GATES"] = "fp32"
+    bf = q.Batch([c.n for c, _ in circuits])
+    g5 = torch.Generator(device=dev)
+    g5.manual_seed(a.seed + 1)
+    for i, (c, qi) in enumerate(circuits):
+        psi = torch.randn(2 ** c.n, dtype=torch.complex128, device=dev, generator=g5)
+        bf.set_state(i, psi / torch.linalg.vector_norm(psi))
+        bf.add_circuit(i, c, qi)
+    bf.compile(renorm_every=8, autotune=True)
+    del os.environ["QTNH_BATCH_GATES"]
+    bf.run()
+    torch.cuda.synchronize()
+    p0.record(stream)
+    for _ in range(a.steps):
+        bf.run()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    fp32_ms = p0.elapsed_time(p1) / a.steps
+    fres = bf.results().cpu().numpy()
+    f_vs_plain = [float(np.linalg.norm(fres[offq[i]:offq[i + 1]] - pres[offq[i]:offq[i + 1]]) /
+                        np.linalg.norm(pres[offq[i]:offq[i + 1]])) for i in range(len(circuits))]
+    fs_vs_plain = [_state_errors(bf.state(i).cpu().numpy(), plain_states[i]) for i in largest]
+    del bf, plain_states
 
     if rank == 0:
         byts = _batch_bytes(circuits)
@@ -660,7 +687,8 @@ def main_batch(a):
         line = {
             "metric": BATCH_METRIC, "value": value, "unit": "gate-layers/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64 (FP64 renormalisation every 8 layers, complex128 queries)",
+            "vs_baseline": None, "dtype": "c64 (gates: exact 64-bit fixed-point sums; FP64 renormalisation every 8 "
+                                             "layers, complex128 queries)",
             "data": "synthetic (seeded circuits and states)",
             "config": {"workload": "%d independent circuits, qubits U{10..22}, depth U{8..32}, Haar two-qubit gates on "
                                    "random pairings, phase layer every 4th layer, a SwapTensor with probability 1/4 "
@@ -682,6 +710,11 @@ def main_batch(a):
                                               "queries_rel_l2_median": statistics.median(q_vs_plain),
                                               "largest_states": _worst_state_errors(s_vs_plain),
                                               "states_checked": len(s_vs_plain)}},
+            "fp32_gates": {"value": world * layers / (fp32_ms * 1e-3), "unit": "gate-layers/s", "ms_per_step": fp32_ms,
+                           "speedup_of_plain": (world * layers / (fp32_ms * 1e-3)) / plain_value,
+                           "vs_plain": {"queries_rel_l2_max": max(f_vs_plain),
+                                        "queries_rel_l2_median": statistics.median(f_vs_plain),
+                                        "largest_states": _worst_state_errors(fs_vs_plain)}},
             "roofline": {"bound": "hbm", "kernel": "whole graph (grouped pair kernel dominant)", "achieved": achieved,
                          "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "alg_bytes_per_step": byts["per_gate"],
