@@ -1,0 +1,83 @@
+// The three-piece bf16 form of complex128 operands for the split-precision GEMM
+// (gemm_umma.cu): every real x = h + m + l in bf16 (24 significant bits), written into
+// planes in the UMMA K-major core-matrix layout (8 rows x 16 bytes; per tile of `tile`
+// rows and K-step of 16 bf16 a contiguous block, LBO 128 B, SBO 256 B). Shared by the
+// split kernels of the GEMM and the fused permute-and-split kernels of permute.cu.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "cuda_common.cuh"
+#include "df32.cuh"
+
+namespace qtnh_impl {
+namespace bx3 {
+
+constexpr int K_STEP = 16;  // bf16 K per MMA
+constexpr int PIECES = 3;   // bf16 pieces per real
+
+// x = h + m + l in bf16 (24 significant bits), through the float-float split where x is
+// in its range, else through FP64 arithmetic.
+__device__ __forceinline__ void pieces(double x, uint16_t (&out)[PIECES]) {
+  const df::dwords w = df::words(x);
+  float hi, lo;
+  if (df::in_range_state(w)) {
+    const df::f2 f = df::split(w);
+    hi = f.h;
+    lo = f.l;
+  } else {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+  }
+  const __nv_bfloat16 h = __float2bfloat16_rn(hi);
+  const float r = __fadd_rn(__fsub_rn(hi, __bfloat162float(h)), lo);
+  const __nv_bfloat16 m = __float2bfloat16_rn(r);
+  const __nv_bfloat16 l = __float2bfloat16_rn(__fsub_rn(r, __bfloat162float(m)));
+  out[0] = __bfloat16_as_ushort(h);
+  out[1] = __bfloat16_as_ushort(m);
+  out[2] = __bfloat16_as_ushort(l);
+}
+
+// Byte offset of row `row`, K-core kc (8 reals) in a plane of tiles of `tile` rows and
+// KS K-steps per tile.
+__device__ __forceinline__ uint64_t plane_offset(uint64_t row, uint64_t kc, uint32_t tile, uint32_t KS) {
+  const uint64_t t = row / tile, rr = row % tile;
+  return (t * KS + kc / 2) * (uint64_t)(tile * K_STEP * 2) + (rr / 8) * 256 + (kc & 1) * 128 + (rr % 8) * 16;
+}
+
+// Where the pieces of an operand go.
+struct Planes {
+  uint8_t* base;         // PIECES planes, plane_bytes apart
+  uint64_t plane_bytes;
+  uint32_t tile;         // rows per tile (128 for A^, 256 for B^)
+  uint32_t KS;           // K-steps per tile
+  int two_rows;          // 1: A^ (complex row m -> real rows 2m, 2m+1), 0: B^ (one row per column n)
+};
+
+// The pieces of complex element v at (row, complex column k): A^ rows 2m = (Re, -Im),
+// 2m + 1 = (Im, Re) at reals 2k, 2k + 1; B^ row n = (Re, Im). One 4-byte store per piece
+// and row.
+__device__ __forceinline__ void write_pieces(const Planes& o, uint64_t row, uint64_t k, double2 v) {
+  uint16_t re[PIECES], im[PIECES];
+  pieces(v.x, re);
+  pieces(v.y, im);
+  const uint64_t kc = k >> 2, sub = (k & 3) * 4;
+  if (o.two_rows) {
+    const uint64_t off0 = plane_offset(2 * row, kc, o.tile, o.KS) + sub;
+    const uint64_t off1 = plane_offset(2 * row + 1, kc, o.tile, o.KS) + sub;
+#pragma unroll
+    for (int p = 0; p < PIECES; ++p) {
+      uint8_t* pl = o.base + p * o.plane_bytes;
+      *reinterpret_cast<uint32_t*>(pl + off0) = (uint32_t)re[p] | ((uint32_t)(im[p] ^ 0x8000u) << 16);
+      *reinterpret_cast<uint32_t*>(pl + off1) = (uint32_t)im[p] | ((uint32_t)re[p] << 16);
+    }
+  } else {
+    const uint64_t off = plane_offset(row, kc, o.tile, o.KS) + sub;
+#pragma unroll
+    for (int p = 0; p < PIECES; ++p)
+      *reinterpret_cast<uint32_t*>(o.base + p * o.plane_bytes + off) = (uint32_t)re[p] | ((uint32_t)im[p] << 16);
+  }
+}
+
+}  // namespace bx3
+}  // namespace qtnh_impl

@@ -204,6 +204,24 @@ void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, c
   c128* Ap = nullptr;
   c128* Bp = nullptr;
   c128* Cp = nullptr;
+  if (gemm_mode() == QTNH_GEMM_BF16X3) {
+    // split precision: the operand permutes are fused into the piece splits
+    std::vector<uint16_t> pBt(rb);
+    for (size_t y = 0; y < openB.size(); ++y) pBt[openB[y]] = (uint16_t)y;
+    for (size_t j = 0; j < wires.size(); ++j) pBt[wires[j].second] = (uint16_t)(openB.size() + j);
+    const bool direct = is_identity(pC);
+    try {
+      if (!direct) Cp = static_cast<c128*>(workspace_alloc(M * N * sizeof(c128), stream));
+      gemm_bf16x3_perm(A, dims_a, pA, (int)openA.size(), B, dims_b, pB, pBt, (int)openB.size(),
+                       direct ? static_cast<c128*>(c) : Cp, M, N, K, stream);
+      if (!direct) permute_device(Cp, c, dC, pC, stream);
+    } catch (...) {
+      workspace_free(Cp, stream);
+      throw;
+    }
+    workspace_free(Cp, stream);
+    return;
+  }
   try {
     if (!is_identity(pA)) {
       Ap = static_cast<c128*>(workspace_alloc(M * K * sizeof(c128), stream));
@@ -215,10 +233,7 @@ void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, c
     }
     const bool direct = is_identity(pC);
     if (!direct) Cp = static_cast<c128*>(workspace_alloc(M * N * sizeof(c128), stream));
-    if (gemm_mode() == QTNH_GEMM_BF16X3)
-      gemm_bf16x3(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, stream);
-    else
-      zgemm(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, s);
+    zgemm(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, s);
     if (!direct) permute_device(Cp, c, dC, pC, stream);
   } catch (...) {
     workspace_free(Ap, stream);

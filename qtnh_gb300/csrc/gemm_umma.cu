@@ -34,6 +34,7 @@
 #include <mutex>
 #include <vector>
 
+#include "bf16x3.cuh"
 #include "cuda_common.cuh"
 #include "df32.cuh"
 
@@ -46,8 +47,8 @@ namespace {
 
 constexpr int GM_M = 128;  // MMA M: rows of the real-form tile
 constexpr int GM_N = 256;  // MMA N: columns of C per tile
-constexpr int GM_K = 16;   // bf16 K per MMA
-constexpr int GM_P = 3;    // bf16 pieces per real
+constexpr int GM_K = bx3::K_STEP;  // bf16 K per MMA
+constexpr int GM_P = bx3::PIECES;  // bf16 pieces per real
 constexpr int GM_STAGES = 4;
 constexpr int GM_A_BLOCK = GM_M * GM_K * 2;  // 4096 bytes: one plane, one tile, one K-step
 constexpr int GM_B_BLOCK = GM_N * GM_K * 2;  // 8192 bytes
@@ -341,34 +342,8 @@ __global__ void __launch_bounds__(GM_THREADS, 1) gemm_bf16x3_umma_kernel(const _
   }
 }
 
-// x = h + m + l in bf16 (24 significant bits), through the float-float split where x is
-// in its range, else through FP64 arithmetic.
-__device__ __forceinline__ void pieces(double x, uint16_t (&out)[GM_P]) {
-  const df::dwords w = df::words(x);
-  float hi, lo;
-  if (df::in_range_state(w)) {
-    const df::f2 f = df::split(w);
-    hi = f.h;
-    lo = f.l;
-  } else {
-    hi = (float)x;
-    lo = (float)(x - (double)hi);
-  }
-  const __nv_bfloat16 h = __float2bfloat16_rn(hi);
-  const float r = __fadd_rn(__fsub_rn(hi, __bfloat162float(h)), lo);
-  const __nv_bfloat16 m = __float2bfloat16_rn(r);
-  const __nv_bfloat16 l = __float2bfloat16_rn(__fsub_rn(r, __bfloat162float(m)));
-  out[0] = __bfloat16_as_ushort(h);
-  out[1] = __bfloat16_as_ushort(m);
-  out[2] = __bfloat16_as_ushort(l);
-}
-
-// Byte offset of row `row` (0..tile-1), K-core kc (8 reals) in a plane of tiles of
-// `tile` rows and KS K-steps per tile.
-__device__ __forceinline__ uint64_t plane_offset(uint64_t row, uint64_t kc, uint32_t tile, uint32_t KS) {
-  const uint64_t t = row / tile, rr = row % tile;
-  return (t * KS + kc / 2) * (uint64_t)(tile * GM_K * 2) + (rr / 8) * 256 + (kc & 1) * 128 + (rr % 8) * 16;
-}
+using bx3::pieces;
+using bx3::plane_offset;
 
 // A^ pieces: thread per (complex row m, K-core kc = complex columns 4 kc .. 4 kc + 3);
 // rows 2m and 2m + 1 of A^. Out-of-range elements (padding) are zero.
@@ -458,11 +433,19 @@ static std::mutex g_timing_mu;
 static bool g_timing = false;
 static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_timing_events;
 
+// Operand preparation: fills the GM_P planes of one operand (pieces in the UMMA layout).
+struct Prep {
+  // A^ (two real rows per complex row) or B^ (one row per column)
+  bool is_a;
+  const c128* data;                 // the operand
+  const dims_t* dims = nullptr;     // non-null: permute (fused) with ptup to [rows | K]
+  const std::vector<uint16_t>* ptup = nullptr;
+  int nrow_axes = 0;
+};
+
 // C (M x N) = A (M x K) B (K x N), complex128 row-major, through BF16x3 pieces on tcgen05.
-void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t N, uint64_t K, void* stream) {
+static void gemm_core(const Prep& pa, const Prep& pb, void* Cv, uint64_t M, uint64_t N, uint64_t K, void* stream) {
   if (M == 0 || N == 0) return;
-  const c128* A = static_cast<const c128*>(Av);
-  const c128* B = static_cast<const c128*>(Bv);
   c128* C = static_cast<c128*>(Cv);
   cudaStream_t s = (cudaStream_t)stream;
   const uint64_t Kp = std::max<uint64_t>(8, (K + 7) / 8 * 8);  // complex K padded: 2 Kp reals = KS K-steps
@@ -487,10 +470,23 @@ void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t 
   p.b_planes = ws + GM_P * p.a_plane_bytes;
   p.partial = p.S > 1 ? reinterpret_cast<float*>(ws + planes) : nullptr;
   try {
-    const uint64_t na = Mpad * KS * 2, nb = Npad * KS * 2;
-    split_a_kernel<<<grid_for((na + 255) / 256, 8), 256, 0, s>>>(A, M, K, ws, p.a_plane_bytes, Mpad, KS);
-    split_b_kernel<<<grid_for((nb + 255) / 256, 8), 256, 0, s>>>(B, K, N, ws + GM_P * p.a_plane_bytes,
-                                                                 p.b_plane_bytes, Npad, KS);
+    if (pa.dims) {
+      permute_split_device(pa.data, *pa.dims, *pa.ptup, pa.nrow_axes, M, Mpad, K, 2 * (uint64_t)KS, ws,
+                           p.a_plane_bytes, GM_M, KS, true, stream);
+    } else {
+      const uint64_t na = Mpad * KS * 2;
+      split_a_kernel<<<grid_for((na + 255) / 256, 8), 256, 0, s>>>(pa.data, M, K, ws, p.a_plane_bytes, Mpad, KS);
+      count_launch();
+    }
+    uint8_t* bpl = ws + GM_P * p.a_plane_bytes;
+    if (pb.dims) {
+      permute_split_device(pb.data, *pb.dims, *pb.ptup, pb.nrow_axes, N, Npad, K, 2 * (uint64_t)KS, bpl,
+                           p.b_plane_bytes, GM_N, KS, false, stream);
+    } else {
+      const uint64_t nb = Npad * KS * 2;
+      split_b_kernel<<<grid_for((nb + 255) / 256, 8), 256, 0, s>>>(pb.data, K, N, bpl, p.b_plane_bytes, Npad, KS);
+      count_launch();
+    }
     const size_t smem = sizeof(GmSmem);
     check_cuda(cudaFuncSetAttribute(gemm_bf16x3_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "gemm_bf16x3_umma_kernel shared memory");
@@ -510,7 +506,7 @@ void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t 
       std::lock_guard<std::mutex> lk(g_timing_mu);
       g_timing_events.emplace_back(e0, e1);
     }
-    count_launch(3);
+    count_launch();
     if (p.S > 1) {
       reduce_partials_kernel<<<grid_for((M * N + 255) / 256, 8), 256, 0, s>>>(
           p.partial, p.S, (uint64_t)p.MT * GM_M, (uint64_t)p.NT * GM_N, C, M, N);
@@ -522,6 +518,30 @@ void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t 
     throw;
   }
   workspace_free(ws, stream);
+}
+
+void gemm_bf16x3(const void* Av, const void* Bv, void* Cv, uint64_t M, uint64_t N, uint64_t K, void* stream) {
+  Prep pa{true, static_cast<const c128*>(Av)}, pb{false, static_cast<const c128*>(Bv)};
+  gemm_core(pa, pb, Cv, M, N, K, stream);
+}
+
+// The contraction's GEMM with the operand permutes fused into the piece splits: A' = A
+// permuted by pA to [rows | K] (nrow_a row axes; identity: A is read directly), B' = B
+// permuted by pB to [K | columns] (identity: read directly), else B is permuted by pBt to
+// [columns | K] (ncol_b column axes) and written straight into the B^ planes.
+void gemm_bf16x3_perm(const void* A, const dims_t& dims_a, const std::vector<uint16_t>& pA, int nrow_a,
+                      const void* B, const dims_t& dims_b, const std::vector<uint16_t>& pB,
+                      const std::vector<uint16_t>& pBt, int ncol_b, void* C, uint64_t M, uint64_t N, uint64_t K,
+                      void* stream) {
+  auto identity = [](const std::vector<uint16_t>& p) {
+    for (size_t i = 0; i < p.size(); ++i)
+      if (p[i] != i) return false;
+    return true;
+  };
+  Prep pa{true, static_cast<const c128*>(A)}, pb{false, static_cast<const c128*>(B)};
+  if (!identity(pA)) pa.dims = &dims_a, pa.ptup = &pA, pa.nrow_axes = nrow_a;
+  if (!identity(pB)) pb.dims = &dims_b, pb.ptup = &pBt, pb.nrow_axes = ncol_b;
+  gemm_core(pa, pb, C, M, N, K, stream);
 }
 
 // Sum of the recorded GEMM kernel durations (synchronizes on each event pair).

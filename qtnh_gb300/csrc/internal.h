@@ -96,6 +96,15 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
                          const std::vector<const void*>& gates, void* stream);
 // C (M x N) = A (M x K) B (K x N), complex128 row-major, BF16x3 pieces on tcgen05.
 void gemm_bf16x3(const void* A, const void* B, void* C, uint64_t M, uint64_t N, uint64_t K, void* stream);
+// The same with the operand permutes fused into the piece splits (gemm_umma.cu).
+void gemm_bf16x3_perm(const void* A, const dims_t& dims_a, const std::vector<uint16_t>& pA, int nrow_a,
+                      const void* B, const dims_t& dims_b, const std::vector<uint16_t>& pB,
+                      const std::vector<uint16_t>& pBt, int ncol_b, void* C, uint64_t M, uint64_t N, uint64_t K,
+                      void* stream);
+// Permute `in` to [rows | K] and write its bf16 pieces into GEMM operand planes (permute.cu).
+void permute_split_device(const void* in, const dims_t& dims, const std::vector<uint16_t>& ptup, int nrow_axes,
+                          uint64_t rows, uint64_t rows_pad, uint64_t K, uint64_t kcs, uint8_t* planes,
+                          uint64_t plane_bytes, uint32_t tile_rows, uint32_t KS, bool two_rows, void* stream);
 uint32_t take_gemm_error();
 void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
                            const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,

@@ -26,6 +26,7 @@
 #include <memory>
 #include <numeric>
 
+#include "bf16x3.cuh"
 #include "cuda_common.cuh"
 
 namespace qtnh_impl {
@@ -160,12 +161,103 @@ __global__ void __launch_bounds__(256) gather_permute_kernel(const c128* __restr
   }
 }
 
+// Fused permute and split (the split-precision GEMM's operands): the same transpose, but
+// each element is written as its bf16 pieces into the GEMM's operand planes at (row, k).
+__global__ void __launch_bounds__(TILE_THREADS, 4) tiled_split_kernel(const c128* __restrict__ in,
+                                                                      const __grid_constant__ TileParams p,
+                                                                      const bx3::Planes o) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = p.T, G = p.G, S = p.tile_slots;
+  c128* tile = reinterpret_cast<c128*>(smem_raw);
+  uint64_t* s_bin = reinterpret_cast<uint64_t*>(tile + (size_t)G * S);
+  uint64_t* s_bout = s_bin + G;
+  int64_t* s_rin = reinterpret_cast<int64_t*>(s_bout + G);
+  int64_t* s_wout = s_rin + T;
+  int32_t* s_rslot = reinterpret_cast<int32_t*>(s_wout + T);
+  int32_t* s_wslot = s_rslot + T;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    s_rin[t] = p.rin[t];
+    s_wout[t] = p.wout[t];
+    s_rslot[t] = p.rslot[t];
+    s_wslot[t] = p.wslot[t];
+  }
+  const uint64_t total = p.rest.total;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * G; r0 < total; r0 += (uint64_t)gridDim.x * G) {
+    for (int g = threadIdx.x; g < G && r0 + g < total; g += blockDim.x) {
+      uint64_t bin, bout;
+      decode(r0 + g, p.rest, bin, bout);
+      s_bin[g] = bin;
+      s_bout[g] = bout;
+    }
+    __syncthreads();
+    const uint64_t left = total - r0;
+    const int n = (left < (uint64_t)G ? (int)left : G) * T;
+    c128 v[TILE_PER_THREAD];
+    int slot[TILE_PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < TILE_PER_THREAD; ++k) {
+      const int e = threadIdx.x + k * TILE_THREADS;
+      if (e < n) {
+        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+        slot[k] = g * S + s_rslot[t];
+        v[k] = __ldg(in + s_bin[g] + s_rin[t]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < TILE_PER_THREAD; ++k)
+      if (threadIdx.x + k * TILE_THREADS < n) tile[slot[k]] = v[k];
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += TILE_THREADS) {
+      const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+      const uint64_t rk = s_bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k
+      bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, tile[g * S + s_wslot[t]]);
+    }
+    __syncthreads();
+  }
+}
+
+// Fused fallback: one thread per element in output order.
+__global__ void __launch_bounds__(256) gather_split_kernel(const c128* __restrict__ in, const __grid_constant__ RestDesc p,
+                                                           const bx3::Planes o) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.total; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t src, rk;
+    decode(e, p, src, rk);
+    bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, __ldg(in + src));
+  }
+}
+
+// Zeros of the padding of an operand's planes: rows in [rows, rows_pad) and complex
+// columns in [K, Kp) (K-core granularity 4 columns, one 4-byte slot per column).
+__global__ void __launch_bounds__(256) pad_planes_kernel(bx3::Planes o, uint64_t rows, uint64_t rows_pad, uint64_t K,
+                                                         uint64_t kcs) {
+  // items: (row < rows, kc in [K / 4, kcs)) then (row in [rows, rows_pad), every kc)
+  const uint64_t kc0 = K / 4, n1 = rows * (kcs - kc0), n2 = (rows_pad - rows) * kcs;
+  const int prow = o.two_rows ? 2 : 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n1 + n2; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t row, kc;
+    if (i < n1) row = i / (kcs - kc0), kc = kc0 + i % (kcs - kc0);
+    else row = rows + (i - n1) / kcs, kc = (i - n1) % kcs;
+    for (int sub = 0; sub < 4; ++sub) {
+      const uint64_t k = kc * 4 + sub;
+      if (row < rows && k < K) continue;
+      for (int rr = 0; rr < prow; ++rr) {
+        const uint64_t off = bx3::plane_offset(prow * row + rr, kc, o.tile, o.KS) + 4 * sub;
+        for (int pc = 0; pc < bx3::PIECES; ++pc) *reinterpret_cast<uint32_t*>(o.base + pc * o.plane_bytes + off) = 0u;
+      }
+    }
+  }
+}
+
 struct Canon {
   dims_t dims;            // merged input dims
   std::vector<int> ptup;  // merged axis -> new position
+  std::vector<char> row;  // fused split: the axis is one of the output's row axes
 };
 
-Canon canonicalise(const dims_t& dims, const std::vector<uint16_t>& ptup) {
+// Drops size-1 axes and merges input-adjacent axes that stay adjacent in the output;
+// with boundary >= 0 (fused split), output positions below it are row axes and no merge
+// crosses from a row axis to a column axis.
+Canon canonicalise(const dims_t& dims, const std::vector<uint16_t>& ptup, int boundary) {
   std::vector<int> keep;
   for (size_t i = 0; i < dims.size(); ++i)
     if (dims[i] > 1) keep.push_back((int)i);
@@ -174,14 +266,17 @@ Canon canonicalise(const dims_t& dims, const std::vector<uint16_t>& ptup) {
   std::sort(order.begin(), order.end(), [&](int x, int y) { return ptup[keep[x]] < ptup[keep[y]]; });
   std::vector<int> kp(keep.size());
   for (size_t j = 0; j < order.size(); ++j) kp[order[j]] = (int)j;
+  auto is_row = [&](size_t x) { return boundary >= 0 && (int)ptup[keep[x]] < boundary; };
   dims_t gd;
   std::vector<int> gp;
+  std::vector<char> gr;
   for (size_t x = 0; x < keep.size(); ++x) {
-    if (x > 0 && kp[x] == kp[x - 1] + 1) {
+    if (x > 0 && kp[x] == kp[x - 1] + 1 && is_row(x) == is_row(x - 1)) {
       gd.back() *= dims[keep[x]];
     } else {
       gd.push_back(dims[keep[x]]);
       gp.push_back(kp[x]);
+      gr.push_back(is_row(x) ? 1 : 0);
     }
   }
   std::vector<int> go(gd.size());
@@ -189,6 +284,7 @@ Canon canonicalise(const dims_t& dims, const std::vector<uint16_t>& ptup) {
   std::sort(go.begin(), go.end(), [&](int x, int y) { return gp[x] < gp[y]; });
   Canon c;
   c.dims = gd;
+  c.row = gr;
   c.ptup.assign(gd.size(), 0);
   for (size_t j = 0; j < go.size(); ++j) c.ptup[go[j]] = (int)j;
   return c;
@@ -203,6 +299,7 @@ void split_axis(Canon& c, int i, uint64_t lo) {
   c.dims[i] /= lo;
   c.dims.insert(c.dims.begin() + i + 1, lo);
   c.ptup.insert(c.ptup.begin() + i + 1, P + 1);
+  c.row.insert(c.row.begin() + i + 1, c.row[i]);
 }
 
 // Smallest divisor f of d with want <= f <= TILE_MAX and f < d, or 0.
@@ -212,48 +309,65 @@ uint64_t inner_factor(uint64_t d, uint64_t want) {
   return 0;
 }
 
-}  // namespace
+struct Plan {
+  enum Kind { COPY, RUN, TILED, GATHER } kind = COPY;
+  std::unique_ptr<TileParams> tile;  // ~25 KB, passed by value to the launch
+  size_t smem = 0;
+  int grid = 0;
+  RunParams run;
+  RestDesc gather;
+};
 
-void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std::vector<uint16_t>& ptup, void* stream) {
-  const size_t r0 = dims.size();
-  if (ptup.size() != r0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple size differs from tensor rank");
-  {
-    std::vector<char> seen(r0, 0);
-    for (auto p : ptup) {
-      if (p >= r0 || seen[p]) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple is not a permutation");
-      seen[p] = 1;
-    }
-  }
+// The launch plan of a permutation. boundary < 0: plain permute (output offsets are
+// element offsets; copy and run-copy shortcuts). boundary >= 0: fused split (output
+// "offsets" are (row << 32) + k with rows over the output positions below the boundary
+// and k over the rest, each row-major; only the tiled and gather forms).
+Plan plan_permute(const dims_t& dims, const std::vector<uint16_t>& ptup, int boundary) {
   const uint64_t N = product(dims);
-  if (N == 0) return;
-  cudaStream_t s = (cudaStream_t)stream;
-  const c128* in = static_cast<const c128*>(in_v);
-  c128* out = static_cast<c128*>(out_v);
-
-  Canon c = canonicalise(dims, ptup);
+  Canon c = canonicalise(dims, ptup, boundary);
   if ((int)c.dims.size() > KMAX) throw Error(QTNH_ERR_UNSUPPORTED, "too many non-trivial axes");
-  if (c.dims.size() <= 1) {
-    check_cuda(cudaMemcpyAsync(out, in, N * sizeof(c128), cudaMemcpyDeviceToDevice, s), "permute copy");
-    return;
+  Plan plan;
+  if (boundary < 0 && c.dims.size() <= 1) {
+    plan.kind = Plan::COPY;
+    return plan;
   }
+  if (c.dims.empty()) {  // a single element (fused): one gather step
+    c.dims.push_back(1);
+    c.ptup.push_back(0);
+    c.row.push_back(boundary > 0 ? 1 : 0);
+  }
+  // output strides: plain, or packed (row << 32) + k
+  auto out_strides = [&](int r) {
+    dims_t nd(r), os(r);
+    for (int i = 0; i < r; ++i) nd[c.ptup[i]] = c.dims[i];
+    if (boundary < 0) {
+      dims_t ns = row_strides(nd);
+      for (int i = 0; i < r; ++i) os[i] = ns[c.ptup[i]];
+      return os;
+    }
+    std::vector<char> prow(r);
+    for (int i = 0; i < r; ++i) prow[c.ptup[i]] = c.row[i];
+    dims_t ns(r);
+    uint64_t rs = 1, ks = 1;
+    for (int j = r - 1; j >= 0; --j) {
+      if (prow[j]) ns[j] = rs << 32, rs *= nd[j];
+      else ns[j] = ks, ks *= nd[j];
+    }
+    for (int i = 0; i < r; ++i) os[i] = ns[c.ptup[i]];
+    return os;
+  };
   // Run copy.
-  if (c.ptup.back() == (int)c.dims.size() - 1 && c.dims.back() >= 32) {
+  if (boundary < 0 && c.ptup.back() == (int)c.dims.size() - 1 && c.dims.back() >= 32) {
     const int r = (int)c.dims.size();
-    dims_t in_stride = row_strides(c.dims);
-    dims_t new_dims(r);
-    for (int i = 0; i < r; ++i) new_dims[c.ptup[i]] = c.dims[i];
-    dims_t ns = row_strides(new_dims);
-    RunParams p;
-    p.L = c.dims[r - 1];
-    p.L_log2 = log2_or_none(p.L);
-    p.rest.n = r - 1;
-    p.rest.total = N / p.L;
-    for (int i = 0; i < r - 1; ++i) fill_axis(p.rest.ax[i], c.dims[i], in_stride[i], ns[c.ptup[i]]);
-    int grid = grid_for((N + 1023) / 1024, 16);
-    run_copy_kernel<<<grid, 256, 0, s>>>(in, out, p);
-    count_launch();
-    check_cuda(cudaGetLastError(), "run_copy_kernel launch");
-    return;
+    dims_t in_stride = row_strides(c.dims), os = out_strides(r);
+    plan.kind = Plan::RUN;
+    plan.run.L = c.dims[r - 1];
+    plan.run.L_log2 = log2_or_none(plan.run.L);
+    plan.run.rest.n = r - 1;
+    plan.run.rest.total = N / plan.run.L;
+    for (int i = 0; i < r - 1; ++i) fill_axis(plan.run.rest.ax[i], c.dims[i], in_stride[i], os[i]);
+    plan.grid = grid_for((N + 1023) / 1024, 16);
+    return plan;
   }
 
   // Tiled transpose: A = the input's trailing axes (>= 32 contiguous input elements), B =
@@ -270,10 +384,9 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
     in_stride = row_strides(c.dims);
     new_dims.assign(r, 0);
     for (int i = 0; i < r; ++i) new_dims[c.ptup[i]] = c.dims[i];
-    dims_t ns = row_strides(new_dims);
-    out_stride.assign(r, 0);
+    out_stride = out_strides(r);
     inv.assign(r, 0);
-    for (int i = 0; i < r; ++i) out_stride[i] = ns[c.ptup[i]], inv[c.ptup[i]] = i;
+    for (int i = 0; i < r; ++i) inv[c.ptup[i]] = i;
     A.clear();
     B.clear();
     inA.assign(r, 0);
@@ -318,8 +431,9 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
   if (tiled) {
     std::sort(A.begin(), A.end());
     std::sort(B.begin(), B.end());
-    std::unique_ptr<TileParams> pp(new TileParams());  // ~25 KB, passed by value to the launch
-    TileParams& p = *pp;
+    plan.kind = Plan::TILED;
+    plan.tile.reset(new TileParams());
+    TileParams& p = *plan.tile;
     const int T = (int)(PA * PB);
     p.T = T;
     p.tile_slots = (int)(PB * (PA + 1));
@@ -375,29 +489,93 @@ void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std
       if (!inA[i] && !inB[i]) fill_axis(p.rest.ax[nr++], c.dims[i], in_stride[i], out_stride[i]);
     p.rest.n = nr;
     p.rest.total = N / (uint64_t)T;
-    const size_t smem = (size_t)p.G * p.tile_slots * sizeof(c128) + 2 * (size_t)p.G * sizeof(uint64_t) +
-                        (size_t)T * (2 * sizeof(int64_t) + 2 * sizeof(int32_t));
-    if (smem > 48 * 1024)
-      check_cuda(cudaFuncSetAttribute(tiled_permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "tiled_permute_kernel shared memory");
+    plan.smem = (size_t)p.G * p.tile_slots * sizeof(c128) + 2 * (size_t)p.G * sizeof(uint64_t) +
+                (size_t)T * (2 * sizeof(int64_t) + 2 * sizeof(int32_t));
     // as many blocks per SM as shared memory and registers allow (at most 4)
-    const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (smem + 1024)));
-    int grid = grid_for((p.rest.total + p.G - 1) / p.G, per_sm);
-    tiled_permute_kernel<<<grid, TILE_THREADS, smem, s>>>(in, out, p);
-    count_launch();
-    check_cuda(cudaGetLastError(), "tiled_permute_kernel launch");
-    return;
+    const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (plan.smem + 1024)));
+    plan.grid = grid_for((p.rest.total + p.G - 1) / p.G, per_sm);
+    return plan;
   }
 
-  // Gather fallback: axes in output order, input strides.
-  RestDesc g;
-  g.n = r;
-  g.total = N;
-  for (int j = 0; j < r; ++j) fill_axis(g.ax[j], new_dims[j], in_stride[inv[j]], 0);
-  int grid = grid_for((N + 255) / 256, 16);
-  gather_permute_kernel<<<grid, 256, 0, s>>>(in, out, g);
+  // Gather fallback: axes in output order, input strides (and output strides).
+  plan.kind = Plan::GATHER;
+  plan.gather.n = r;
+  plan.gather.total = N;
+  for (int j = 0; j < r; ++j) fill_axis(plan.gather.ax[j], new_dims[j], in_stride[inv[j]], out_stride[inv[j]]);
+  plan.grid = grid_for((N + 255) / 256, 16);
+  return plan;
+}
+
+void check_permutation(const dims_t& dims, const std::vector<uint16_t>& ptup) {
+  const size_t r0 = dims.size();
+  if (ptup.size() != r0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple size differs from tensor rank");
+  std::vector<char> seen(r0, 0);
+  for (auto p : ptup) {
+    if (p >= r0 || seen[p]) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple is not a permutation");
+    seen[p] = 1;
+  }
+}
+
+}  // namespace
+
+void permute_device(const void* in_v, void* out_v, const dims_t& dims, const std::vector<uint16_t>& ptup, void* stream) {
+  check_permutation(dims, ptup);
+  const uint64_t N = product(dims);
+  if (N == 0) return;
+  cudaStream_t s = (cudaStream_t)stream;
+  const c128* in = static_cast<const c128*>(in_v);
+  c128* out = static_cast<c128*>(out_v);
+  Plan plan = plan_permute(dims, ptup, -1);
+  switch (plan.kind) {
+    case Plan::COPY:
+      check_cuda(cudaMemcpyAsync(out, in, N * sizeof(c128), cudaMemcpyDeviceToDevice, s), "permute copy");
+      return;
+    case Plan::RUN:
+      run_copy_kernel<<<plan.grid, 256, 0, s>>>(in, out, plan.run);
+      count_launch();
+      check_cuda(cudaGetLastError(), "run_copy_kernel launch");
+      return;
+    case Plan::TILED:
+      if (plan.smem > 48 * 1024)
+        check_cuda(cudaFuncSetAttribute(tiled_permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)plan.smem),
+                   "tiled_permute_kernel shared memory");
+      tiled_permute_kernel<<<plan.grid, TILE_THREADS, plan.smem, s>>>(in, out, *plan.tile);
+      count_launch();
+      check_cuda(cudaGetLastError(), "tiled_permute_kernel launch");
+      return;
+    case Plan::GATHER:
+      gather_permute_kernel<<<plan.grid, 256, 0, s>>>(in, out, plan.gather);
+      count_launch();
+      check_cuda(cudaGetLastError(), "gather_permute_kernel launch");
+      return;
+  }
+}
+
+void permute_split_device(const void* in_v, const dims_t& dims, const std::vector<uint16_t>& ptup, int nrow_axes,
+                          uint64_t rows, uint64_t rows_pad, uint64_t K, uint64_t kcs, uint8_t* planes,
+                          uint64_t plane_bytes, uint32_t tile_rows, uint32_t KS, bool two_rows, void* stream) {
+  check_permutation(dims, ptup);
+  cudaStream_t s = (cudaStream_t)stream;
+  const c128* in = static_cast<const c128*>(in_v);
+  bx3::Planes o{planes, plane_bytes, tile_rows, KS, two_rows ? 1 : 0};
+  if (rows_pad > rows || kcs * 4 > K) {
+    const uint64_t items = rows * (kcs - K / 4) + (rows_pad - rows) * kcs;
+    pad_planes_kernel<<<grid_for((items + 255) / 256, 8), 256, 0, s>>>(o, rows, rows_pad, K, kcs);
+    count_launch();
+  }
+  if (product(dims) == 0) return;
+  Plan plan = plan_permute(dims, ptup, nrow_axes);
+  if (plan.kind == Plan::TILED) {
+    if (plan.smem > 48 * 1024)
+      check_cuda(cudaFuncSetAttribute(tiled_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem),
+                 "tiled_split_kernel shared memory");
+    tiled_split_kernel<<<plan.grid, TILE_THREADS, plan.smem, s>>>(in, *plan.tile, o);
+  } else {
+    gather_split_kernel<<<plan.grid, 256, 0, s>>>(in, plan.gather, o);
+  }
   count_launch();
-  check_cuda(cudaGetLastError(), "gather_permute_kernel launch");
+  check_cuda(cudaGetLastError(), "permute-split launch");
 }
 
 }  // namespace qtnh_impl

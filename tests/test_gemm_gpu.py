@@ -121,3 +121,26 @@ def test_split_contraction_vs_fp64(seed, bf16x3):
     assert split.dis == plain.dis and split.loc == plain.loc
     rel, mx = errors(host(split.data), host(plain.data))
     assert rel < 2e-6 and mx < 2e-5, (d1, d2, wires, rel, mx)
+
+
+@pytest.mark.parametrize("d1,d2,wires", [
+    ([3, 5, 7], [2, 3, 4], [(0, 1)]),                  # small K, A permuted (tile)
+    ([4099, 3], [4099, 5], [(0, 0)]),                  # prime K: A through the gather form
+    ([6, 10], [7, 10, 3], [(1, 1)]),                   # B permuted, K = 10 (padding inside a K-core)
+    ([5, 9, 4, 7], [7, 3, 9, 2], [(1, 2), (3, 0)]),    # two wires, both operands permuted
+    ([64, 2, 33, 16], [16, 33, 5], [(3, 0), (2, 1)]),  # power-of-two and odd axes mixed
+])
+def test_split_fused_permutes(d1, d2, wires, bf16x3):
+    # operand permutes fused into the piece splits (tiled and gather forms, padding of
+    # rows and of K) against the FP64 plain path
+    rng = np.random.default_rng(sum(d1) + 3 * sum(d2))
+    ksize = int(np.prod([d1[a] for a, _ in wires]))
+    a = crandn(rng, d1, 1 / np.sqrt(ksize))
+    b = crandn(rng, d2)
+    t1, t2 = q.Tensor(q.DENSE, [], d1, dev(a)), q.Tensor(q.DENSE, [], d2, dev(b))
+    split, _, _, _ = q.contract(t1, t2, wires)
+    q.set_gemm_precision(q.GEMM_FP64)
+    plain, _, _, _ = q.contract(t1, t2, wires)
+    q.set_gemm_precision(q.GEMM_BF16X3)
+    rel, mx = errors(host(split.data), host(plain.data))
+    assert rel < 2e-6 and mx < 2e-5, (d1, d2, wires, rel, mx)
