@@ -952,7 +952,12 @@ def main():
             main_kernels(a)
         return
     if a.workload == "serve":
-        main_serve(a)
+        if a.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the serving workload has no reference arm: the "
+                              "reference has no request loop; its CPU gate-layer rate is the batch and circuit "
+                              "workloads' reference arm"}))
+        else:
+            main_serve(a)
         return
     if a.workload == "batch":
         if a.impl == "reference":
