@@ -186,8 +186,8 @@ __device__ __forceinline__ c128 cmul_f32x2(c128 a, c128 b) {
   return cmul_fp64_outofline(a, b);
 }
 
-// psi[e] *= d[index of e over the targets]; FF: float-float products (cmul_f32x2), else FP64.
-template <typename IT, bool FF>
+// psi[e] *= d[index of e over the targets] in FP64.
+template <typename IT>
 __global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const c128* __restrict__ d,
                                                    const __grid_constant__ DiagParams p) {
   const IT n = (IT)p.n, step = (IT)gridDim.x * blockDim.x * DU;
@@ -201,7 +201,39 @@ __global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const
 #pragma unroll
     for (int u = 0; u < DU; ++u) {
       const IT e = base + (IT)(u * blockDim.x);
-      if (e < n) psi[e] = FF ? cmul_f32x2(x[u], f[u]) : cmul(x[u], f[u]);
+      if (e < n) psi[e] = cmul(x[u], f[u]);
+    }
+  }
+}
+
+// The same in float-float: the diagonal comes pre-split (ds, table_split_kernel; a NaN hi
+// part flags an entry outside the float-float range), the amplitude is split per element.
+template <typename IT>
+__global__ void __launch_bounds__(256) diag_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ d,
+                                                         const df::cf2* __restrict__ ds,
+                                                         const __grid_constant__ DiagParams p) {
+  const IT n = (IT)p.n, step = (IT)gridDim.x * blockDim.x * DU;
+  for (IT base = (IT)blockIdx.x * blockDim.x * DU + threadIdx.x; base < n; base += step) {
+    c128 x[DU];
+    df::cf2 f[DU];
+    IT idx[DU];
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e < n) idx[u] = diag_index<IT>(e, p), x[u] = psi[e], f[u] = ds[idx[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < DU; ++u) {
+      const IT e = base + (IT)(u * blockDim.x);
+      if (e >= n) continue;
+      const bool ok = f[u].re.h == f[u].re.h && df::in_range_state(x[u].x) && df::in_range_state(x[u].y);
+      if (__all_sync(__activemask(), ok)) {
+        df::acc re, im;
+        df::cmul_acc(df::csplit(x[u].x, x[u].y), f[u], re, im);
+        psi[e] = make_double2(df::to_double(re), df::to_double(im));
+      } else {
+        psi[e] = cmul_fp64_outofline(x[u], __ldg(d + idx[u]));
+      }
     }
   }
 }
@@ -432,13 +464,20 @@ void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16
   c128* st_ = static_cast<c128*>(state);
   const c128* d_ = static_cast<const c128*>(diag);
   const bool ff = arithmetic_mode() != QTNH_ARITH_FP64;
-  if (index32(n, grid)) {
-    if (ff) diag_kernel<uint32_t, true><<<grid, 256, 0, s>>>(st_, d_, p);
-    else diag_kernel<uint32_t, false><<<grid, 256, 0, s>>>(st_, d_, p);
-  } else {
-    if (ff) diag_kernel<uint64_t, true><<<grid, 256, 0, s>>>(st_, d_, p);
-    else diag_kernel<uint64_t, false><<<grid, 256, 0, s>>>(st_, d_, p);
+  if (ff) {
+    // the diagonal's entries split once into float pairs
+    df::cf2* ds = static_cast<df::cf2*>(workspace_alloc(m * sizeof(df::cf2), stream));
+    table_split_kernel<<<grid_for((m + 255) / 256, 4), 256, 0, s>>>(d_, ds, m);
+    if (index32(n, grid)) diag_kernel_f32x2<uint32_t><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+    else diag_kernel_f32x2<uint64_t><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+    count_launch(2);
+    const cudaError_t e = cudaGetLastError();
+    workspace_free(ds, stream);
+    check_cuda(e, "diag_kernel launch");
+    return;
   }
+  if (index32(n, grid)) diag_kernel<uint32_t><<<grid, 256, 0, s>>>(st_, d_, p);
+  else diag_kernel<uint64_t><<<grid, 256, 0, s>>>(st_, d_, p);
   count_launch();
   check_cuda(cudaGetLastError(), "diag_kernel launch");
 }
