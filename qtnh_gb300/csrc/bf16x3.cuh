@@ -79,5 +79,42 @@ __device__ __forceinline__ void write_pieces(const Planes& o, uint64_t row, uint
   }
 }
 
+// Four consecutive complex columns k .. k + 3 (k % 4 == 0) of one row: whole 16-byte
+// chunks, one store per piece and row.
+__device__ __forceinline__ void write_pieces4(const Planes& o, uint64_t row, uint64_t k, const double2 (&v)[4]) {
+  uint16_t re[4][PIECES], im[4][PIECES];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    pieces(v[e].x, re[e]);
+    pieces(v[e].y, im[e]);
+  }
+  const uint64_t kc = k >> 2;
+  if (o.two_rows) {
+    const uint64_t off0 = plane_offset(2 * row, kc, o.tile, o.KS);
+    const uint64_t off1 = plane_offset(2 * row + 1, kc, o.tile, o.KS);
+#pragma unroll
+    for (int p = 0; p < PIECES; ++p) {
+      uint32_t r0[4], r1[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        r0[e] = (uint32_t)re[e][p] | ((uint32_t)(im[e][p] ^ 0x8000u) << 16);
+        r1[e] = (uint32_t)im[e][p] | ((uint32_t)re[e][p] << 16);
+      }
+      uint8_t* pl = o.base + p * o.plane_bytes;
+      *reinterpret_cast<uint4*>(pl + off0) = make_uint4(r0[0], r0[1], r0[2], r0[3]);
+      *reinterpret_cast<uint4*>(pl + off1) = make_uint4(r1[0], r1[1], r1[2], r1[3]);
+    }
+  } else {
+    const uint64_t off = plane_offset(row, kc, o.tile, o.KS);
+#pragma unroll
+    for (int p = 0; p < PIECES; ++p) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) w[e] = (uint32_t)re[e][p] | ((uint32_t)im[e][p] << 16);
+      *reinterpret_cast<uint4*>(o.base + p * o.plane_bytes + off) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
 }  // namespace bx3
 }  // namespace qtnh_impl

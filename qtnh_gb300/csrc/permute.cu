@@ -45,6 +45,7 @@ struct TileParams {
   int T;           // elements per tile
   int G;           // tiles per step (T is a power of two when G > 1)
   uint32_t T_log2;
+  int quad;        // fused split: write order runs in aligned quads of consecutive columns
   int tile_slots;
   int64_t rin[TILE_MAX];   // read order: input offset within the tile
   int64_t wout[TILE_MAX];  // write order: output offset within the tile
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(256) gather_permute_kernel(const c128* __restr
 
 // Fused permute and split (the split-precision GEMM's operands): the same transpose, but
 // each element is written as its bf16 pieces into the GEMM's operand planes at (row, k).
-__global__ void __launch_bounds__(TILE_THREADS, 4) tiled_split_kernel(const c128* __restrict__ in,
+__global__ void __launch_bounds__(TILE_THREADS, 3) tiled_split_kernel(const c128* __restrict__ in,
                                                                       const __grid_constant__ TileParams p,
                                                                       const bx3::Planes o) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -207,10 +208,22 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) tiled_split_kernel(const c128
     for (int k = 0; k < TILE_PER_THREAD; ++k)
       if (threadIdx.x + k * TILE_THREADS < n) tile[slot[k]] = v[k];
     __syncthreads();
-    for (int e = threadIdx.x; e < n; e += TILE_THREADS) {
-      const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-      const uint64_t rk = s_bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k
-      bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, tile[g * S + s_wslot[t]]);
+    if (p.quad) {
+      // four consecutive columns of one row per thread: whole 16-byte chunks
+      for (int e = 4 * threadIdx.x; e < n; e += 4 * TILE_THREADS) {
+        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+        const uint64_t rk = s_bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k, k % 4 == 0
+        double2 v[4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x) v[x] = tile[g * S + s_wslot[t + x]];
+        bx3::write_pieces4(o, rk >> 32, rk & 0xFFFFFFFFull, v);
+      }
+    } else {
+      for (int e = threadIdx.x; e < n; e += TILE_THREADS) {
+        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+        const uint64_t rk = s_bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k
+        bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, tile[g * S + s_wslot[t]]);
+      }
     }
     __syncthreads();
   }
@@ -440,6 +453,19 @@ Plan plan_permute(const dims_t& dims, const std::vector<uint16_t>& ptup, int bou
     const uint32_t tl = log2_or_none((uint64_t)T);
     p.G = (tl != 0xFFFFFFFFu && T < STEP_ELEMS) ? std::min(STEP_ELEMS / T, 256) : 1;
     p.T_log2 = tl == 0xFFFFFFFFu ? 0 : tl;
+    // fused split: the tile's trailing output positions that are column axes form a run
+    // of consecutive columns (stride 1 innermost); if its length is a multiple of 4,
+    // write order goes in aligned quads (every other axis strides by multiples of it)
+    p.quad = 0;
+    if (boundary >= 0) {
+      uint64_t run = 1;
+      for (int j = r - 1; j >= 0; --j) {
+        const int i = inv[j];
+        if (!(inA[i] || inB[i]) || c.row[i]) break;
+        run *= c.dims[i];
+      }
+      p.quad = (run % 4 == 0) ? 1 : 0;
+    }
     // Row-major multipliers over A and B (input order).
     auto mults = [&](const std::vector<int>& axes) {
       std::vector<uint64_t> m(axes.size(), 1);
