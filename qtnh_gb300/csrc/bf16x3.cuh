@@ -45,11 +45,17 @@ __device__ __forceinline__ uint64_t plane_offset(uint64_t row, uint64_t kc, uint
   return (t * KS + kc / 2) * (uint64_t)(tile * K_STEP * 2) + (rr / 8) * 256 + (kc & 1) * 128 + (rr % 8) * 16;
 }
 
+// The same with the tile height as a power of two (shifts instead of divisions).
+__device__ __forceinline__ uint64_t plane_offset_log2(uint64_t row, uint64_t kc, uint32_t tile_log2, uint32_t KS) {
+  const uint64_t t = row >> tile_log2, rr = row & ((1ull << tile_log2) - 1);
+  return ((t * KS + (kc >> 1)) << (tile_log2 + 5)) + ((rr >> 3) << 8) + ((kc & 1) << 7) + ((rr & 7) << 4);
+}
+
 // Where the pieces of an operand go.
 struct Planes {
   uint8_t* base;         // PIECES planes, plane_bytes apart
   uint64_t plane_bytes;
-  uint32_t tile;         // rows per tile (128 for A^, 256 for B^)
+  uint32_t tile_log2;    // rows per tile: 2^7 for A^, 2^8 for B^
   uint32_t KS;           // K-steps per tile
   int two_rows;          // 1: A^ (complex row m -> real rows 2m, 2m+1), 0: B^ (one row per column n)
 };
@@ -63,8 +69,8 @@ __device__ __forceinline__ void write_pieces(const Planes& o, uint64_t row, uint
   pieces(v.y, im);
   const uint64_t kc = k >> 2, sub = (k & 3) * 4;
   if (o.two_rows) {
-    const uint64_t off0 = plane_offset(2 * row, kc, o.tile, o.KS) + sub;
-    const uint64_t off1 = plane_offset(2 * row + 1, kc, o.tile, o.KS) + sub;
+    const uint64_t off0 = plane_offset_log2(2 * row, kc, o.tile_log2, o.KS) + sub;
+    const uint64_t off1 = plane_offset_log2(2 * row + 1, kc, o.tile_log2, o.KS) + sub;
 #pragma unroll
     for (int p = 0; p < PIECES; ++p) {
       uint8_t* pl = o.base + p * o.plane_bytes;
@@ -72,7 +78,7 @@ __device__ __forceinline__ void write_pieces(const Planes& o, uint64_t row, uint
       *reinterpret_cast<uint32_t*>(pl + off1) = (uint32_t)im[p] | ((uint32_t)re[p] << 16);
     }
   } else {
-    const uint64_t off = plane_offset(row, kc, o.tile, o.KS) + sub;
+    const uint64_t off = plane_offset_log2(row, kc, o.tile_log2, o.KS) + sub;
 #pragma unroll
     for (int p = 0; p < PIECES; ++p)
       *reinterpret_cast<uint32_t*>(o.base + p * o.plane_bytes + off) = (uint32_t)re[p] | ((uint32_t)im[p] << 16);
@@ -90,8 +96,8 @@ __device__ __forceinline__ void write_pieces4(const Planes& o, uint64_t row, uin
   }
   const uint64_t kc = k >> 2;
   if (o.two_rows) {
-    const uint64_t off0 = plane_offset(2 * row, kc, o.tile, o.KS);
-    const uint64_t off1 = plane_offset(2 * row + 1, kc, o.tile, o.KS);
+    const uint64_t off0 = plane_offset_log2(2 * row, kc, o.tile_log2, o.KS);
+    const uint64_t off1 = plane_offset_log2(2 * row + 1, kc, o.tile_log2, o.KS);
 #pragma unroll
     for (int p = 0; p < PIECES; ++p) {
       uint32_t r0[4], r1[4];
@@ -105,7 +111,7 @@ __device__ __forceinline__ void write_pieces4(const Planes& o, uint64_t row, uin
       *reinterpret_cast<uint4*>(pl + off1) = make_uint4(r1[0], r1[1], r1[2], r1[3]);
     }
   } else {
-    const uint64_t off = plane_offset(row, kc, o.tile, o.KS);
+    const uint64_t off = plane_offset_log2(row, kc, o.tile_log2, o.KS);
 #pragma unroll
     for (int p = 0; p < PIECES; ++p) {
       uint32_t w[4];

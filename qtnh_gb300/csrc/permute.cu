@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) pad_planes_kernel(bx3::Planes o, uint64_t
       const uint64_t k = kc * 4 + sub;
       if (row < rows && k < K) continue;
       for (int rr = 0; rr < prow; ++rr) {
-        const uint64_t off = bx3::plane_offset(prow * row + rr, kc, o.tile, o.KS) + 4 * sub;
+        const uint64_t off = bx3::plane_offset_log2(prow * row + rr, kc, o.tile_log2, o.KS) + 4 * sub;
         for (int pc = 0; pc < bx3::PIECES; ++pc) *reinterpret_cast<uint32_t*>(o.base + pc * o.plane_bytes + off) = 0u;
       }
     }
@@ -584,7 +584,8 @@ void permute_split_device(const void* in_v, const dims_t& dims, const std::vecto
   check_permutation(dims, ptup);
   cudaStream_t s = (cudaStream_t)stream;
   const c128* in = static_cast<const c128*>(in_v);
-  bx3::Planes o{planes, plane_bytes, tile_rows, KS, two_rows ? 1 : 0};
+  if (tile_rows != 128 && tile_rows != 256) throw Error(QTNH_ERR_UNSUPPORTED, "operand tile height");
+  bx3::Planes o{planes, plane_bytes, tile_rows == 128 ? 7u : 8u, KS, two_rows ? 1 : 0};
   if (rows_pad > rows || kcs * 4 > K) {
     const uint64_t items = rows * (kcs - K / 4) + (rows_pad - rows) * kcs;
     pad_planes_kernel<<<grid_for((items + 255) / 256, 8), 256, 0, s>>>(o, rows, rows_pad, K, kcs);
