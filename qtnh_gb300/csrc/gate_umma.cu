@@ -6,19 +6,22 @@
 // input reals) -- 21 digit pairs x 2 K-steps = 42 tcgen05.mma (kind::f16, bf16 operands,
 // FP32 accumulators) into six level column blocks of TMEM.
 //
-// CTA = two teams of eight warps + one MMA warp, one CTA per SM (persistent):
-//   * team t handles every other tile of the CTA; group r of its tile belongs to two
-//     threads (warp quarter q = r / 32 of the team's first and second four warps), each
+// CTA = a team of eight warps + one MMA warp; two CTAs per SM (persistent; each holds half
+// of the SM's tensor memory and ~97 KB of shared memory):
+//   * the team handles every tile of its CTA; group r of a tile belongs to two threads
+//     (warp quarter q = r / 32 of the team's first and second four warps), each
 //     owning 8 of the group's 16 amplitudes: it fetches them one tile ahead with
 //     cp.async, the two exchange their largest exponents through shared memory (an
 //     mbarrier), and each writes its 6 x 16 digits into shared memory in the UMMA
-//     K-major core-matrix layout (8 rows x 16 bytes) and arrives on full[t];
-//   * the MMA warp waits on full[t], issues the 42 MMAs into team t's TMEM columns and
-//     commits them to done[t];
-//   * team t waits on done[t], and each thread reads the level sums of its 8 amplitudes
+//     K-major core-matrix layout (8 rows x 16 bytes) and arrives on full;
+//   * the MMA warp waits on full, issues the 42 MMAs into the CTA's TMEM columns and
+//     commits them to done;
+//   * the team waits on done, and each thread reads the level sums of its 8 amplitudes
 //     from its TMEM lane with tcgen05.ld, recombines and stores them.
-// While one team converts, the other's MMAs run. Every wait is bounded by a clock limit;
-// on expiry the CTA records an error flag, stops and frees its tensor memory.
+// While one CTA's team waits for its MMAs, the other CTA on the SM converts (one CTA
+// with two teams, or 16 warps issuing their own MMAs, measured slower). Every wait is
+// bounded by a clock limit; on expiry the CTA records an error flag, stops and frees its
+// tensor memory.
 //
 // Groups with an infinity/NaN or a largest magnitude outside 2^-200..2^201, and all
 // groups when the gate has such entries, are computed in FP64 by their two threads.
@@ -35,13 +38,13 @@ __device__ unsigned int g_umma_error;
 
 namespace {
 
-constexpr int UM_WG = 2;                 // teams, one tile in flight each
+constexpr int UM_WG = 1;                 // teams per CTA, one tile in flight each
 constexpr int UM_TEAM = 256;             // threads of a team (two per group)
 constexpr int UM_THREADS = UM_WG * UM_TEAM + 32;
 constexpr int UM_M = 128;                // groups per tile (MMA M)
 constexpr int UM_N = 32;                 // output reals per group (MMA N)
 constexpr int UM_COLS = 256;             // TMEM column stride of a team (its level sums use 32 * NL)
-constexpr uint32_t UM_TMEM_COLS = 512;   // allocation (power of two >= UM_WG * UM_COLS)
+constexpr uint32_t UM_TMEM_COLS = 256;   // allocation (power of two >= UM_WG * UM_COLS): half of an SM's TMEM
 static_assert(oz::NL * UM_N <= UM_COLS, "level sums exceed a team's TMEM columns");
 constexpr long long UM_WAIT_CYCLES = 1ll << 31;  // ~1 s at 2 GHz
 
@@ -141,7 +144,7 @@ __device__ __noinline__ void half_group_fp64(double2* __restrict__ psi, IT gbase
 }
 
 template <typename IT>
-__global__ void __launch_bounds__(UM_THREADS, 1) gate_pair_umma_kernel(double2* __restrict__ psi,
+__global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* __restrict__ psi,
                                                                        const double2* __restrict__ ga,
                                                                        const double2* __restrict__ gb,
                                                                        const __grid_constant__ PairParams p) {
@@ -344,7 +347,7 @@ void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairP
   check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
              "gate_pair_umma_kernel shared memory");
   const uint64_t ntiles = p.ngroups / UM_M;
-  const int grid = (int)std::min<uint64_t>(ntiles, (uint64_t)sm_count());
+  const int grid = (int)std::min<uint64_t>(ntiles, 2 * (uint64_t)sm_count());  // two CTAs per SM
   gate_pair_umma_kernel<IT><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p);
 }
 
