@@ -11,7 +11,9 @@ L2 flush is needed between steps.
 
 value : gate-layers/s with the state resident in HBM (CUDA events on the launch stream).
 e2e   : the same through the C ABI with host buffers: every step copies the initial
-        state from pinned host memory to the device and the result back.
+        state from pinned host memory to the device and the result back, on two copy
+        streams with two device state buffers, so that the next step's input copy and
+        this step's result copy overlap the circuit.
 arith : default bf16x6: each layer's gates applied as fused pairs (two disjoint
         two-qubit gates = one 16x16 unitary) on the bf16 tensor cores with error-free
         8-bit digits (complex128 in and out, ~1e-14 relative error per pair);
@@ -1059,21 +1061,47 @@ def main():
     achieved = alg_bytes / (gate_launch_ms * 1e-3) / 1e9 if gate_launch_ms else None
     share = {k: sum(s.elapsed_time(e) for s, e in v) / ms for k, v in events.items()}
 
-    # e2e through the C ABI with host buffers
+    # e2e through the C ABI with host buffers: every step copies its input state from
+    # pinned host memory and its result back, on two copy streams, double-buffered so that
+    # step i+1's input copy and step i's result copy overlap the circuits
+    h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
+    bufs = [(cur, oth), (torch.empty_like(cur), torch.empty_like(cur))]
+    in_ev = [torch.cuda.Event(), torch.cuda.Event()]
+    free_ev = [torch.cuda.Event(), torch.cuda.Event()]
+    done_ev = torch.cuda.Event()
+
+    def h2d(i):
+        c = bufs[i % 2][0]
+        h2d_s.wait_event(free_ev[i % 2])  # that buffer's previous result has been copied out
+        q.check(q.lib().qtnh_memcpy_h2d(q._ptr(c), q._ptr(host_in), q.ctypes.c_size_t(16 * N), q._stream(h2d_s)))
+        in_ev[i % 2].record(h2d_s)
+
+    for e in free_ev:
+        e.record(stream)
     barrier()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
-    for _ in range(a.steps):
-        q.check(q.lib().qtnh_memcpy_h2d(q._ptr(cur), q._ptr(host_in), q.ctypes.c_size_t(16 * N), q._stream()))
-        res = dc.run(cur, oth)
-        if res is not cur:
-            cur, oth = oth, cur
-        q.check(q.lib().qtnh_memcpy_d2h(q._ptr(host_out), q._ptr(cur), q.ctypes.c_size_t(16 * N), q._stream()))
+    h2d_s.wait_event(f0)
+    h2d(0)
+    for i in range(a.steps):
+        c, o = bufs[i % 2]
+        stream.wait_event(in_ev[i % 2])
+        res = dc.run(c, o)
+        done_ev.record(stream)
+        if i + 1 < a.steps:
+            h2d(i + 1)
+        d2h_s.wait_event(done_ev)
+        q.check(q.lib().qtnh_memcpy_d2h(q._ptr(host_out), q._ptr(res), q.ctypes.c_size_t(16 * N), q._stream(d2h_s)))
+        free_ev[i % 2].record(d2h_s)
+    stream.wait_stream(d2h_s)
     f1.record(stream)
     torch.cuda.synchronize()
     barrier()
     ems = f0.elapsed_time(f1)
+    last_c, last_o = bufs[(a.steps - 1) % 2]
+    cur, oth = (res, last_o) if res is last_c else (res, last_c)
+    del bufs
     if dist is not None:
         t = torch.tensor([ems], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
