@@ -399,16 +399,48 @@ def main_contract(a):
     host_out = torch.empty(max_out, dtype=torch.complex128, pin_memory=True)
     h2d = sum(16 * (t1.data.numel() + t2.data.numel()) for t1, t2, _ in tens)
     d2h = sum(16 * M * N for _, _, _, M, N, _ in pairs)
+    # copies on two copy streams: the next pair's operands go in while this pair contracts,
+    # results come out of two alternating output buffers
+    h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
+    outs = [out, torch.empty_like(out)]
+    in_ev = [torch.cuda.Event() for _ in tens]
+    done_ev = [torch.cuda.Event() for _ in tens]
+    free_out = [torch.cuda.Event(), torch.cuda.Event()]
+    for e in done_ev + free_out:
+        e.record(stream)
+
+    def h2d(j):
+        t1, t2, _ = tens[j]
+        ha, hb = hosts[j]
+        h2d_s.wait_event(done_ev[j])  # the pair's previous contraction has read its operands
+        with torch.cuda.stream(h2d_s):
+            t1.data.copy_(ha, non_blocking=True)
+            t2.data.copy_(hb, non_blocking=True)
+        in_ev[j].record(h2d_s)
+
     barrier()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
-    for _ in range(a.steps):
-        for (t1, t2, wires), (ha, hb), (_, _, _, M, N, _) in zip(tens, hosts, pairs):
-            t1.data.copy_(ha, non_blocking=True)
-            t2.data.copy_(hb, non_blocking=True)
-            q.contract(t1, t2, wires, out=out[:M * N])
-            host_out[:M * N].copy_(out[:M * N], non_blocking=True)
+    h2d_s.wait_event(f0)
+    h2d(0)
+    k = 0
+    for st in range(a.steps):
+        for j, ((t1, t2, wires), (_, _, _, M, N, _)) in enumerate(zip(tens, pairs)):
+            o = outs[k % 2]
+            stream.wait_event(in_ev[j])
+            stream.wait_event(free_out[k % 2])
+            q.contract(t1, t2, wires, out=o[:M * N])
+            done_ev[j].record(stream)
+            nj = (j + 1) % len(tens)
+            if not (st == a.steps - 1 and nj == 0):
+                h2d(nj)
+            d2h_s.wait_event(done_ev[j])
+            with torch.cuda.stream(d2h_s):
+                host_out[:M * N].copy_(o[:M * N], non_blocking=True)
+            free_out[k % 2].record(d2h_s)
+            k += 1
+    stream.wait_stream(d2h_s)
     f1.record(stream)
     torch.cuda.synchronize()
     barrier()
