@@ -409,7 +409,7 @@ def main_contract(a):
     for e in done_ev + free_out:
         e.record(stream)
 
-    def h2d(j):
+    def copy_in(j):
         t1, t2, _ = tens[j]
         ha, hb = hosts[j]
         h2d_s.wait_event(done_ev[j])  # the pair's previous contraction has read its operands
@@ -423,7 +423,7 @@ def main_contract(a):
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     h2d_s.wait_event(f0)
-    h2d(0)
+    copy_in(0)
     k = 0
     for st in range(a.steps):
         for j, ((t1, t2, wires), (_, _, _, M, N, _)) in enumerate(zip(tens, pairs)):
@@ -434,7 +434,7 @@ def main_contract(a):
             done_ev[j].record(stream)
             nj = (j + 1) % len(tens)
             if not (st == a.steps - 1 and nj == 0):
-                h2d(nj)
+                copy_in(nj)
             d2h_s.wait_event(done_ev[j])
             with torch.cuda.stream(d2h_s):
                 host_out[:M * N].copy_(o[:M * N], non_blocking=True)
@@ -1102,7 +1102,7 @@ def main():
     free_ev = [torch.cuda.Event(), torch.cuda.Event()]
     done_ev = torch.cuda.Event()
 
-    def h2d(i):
+    def copy_in(i):
         c = bufs[i % 2][0]
         h2d_s.wait_event(free_ev[i % 2])  # that buffer's previous result has been copied out
         q.check(q.lib().qtnh_memcpy_h2d(q._ptr(c), q._ptr(host_in), q.ctypes.c_size_t(16 * N), q._stream(h2d_s)))
@@ -1115,14 +1115,14 @@ def main():
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     h2d_s.wait_event(f0)
-    h2d(0)
+    copy_in(0)
     for i in range(a.steps):
         c, o = bufs[i % 2]
         stream.wait_event(in_ev[i % 2])
         res = dc.run(c, o)
         done_ev.record(stream)
         if i + 1 < a.steps:
-            h2d(i + 1)
+            copy_in(i + 1)
         d2h_s.wait_event(done_ev)
         q.check(q.lib().qtnh_memcpy_d2h(q._ptr(host_out), q._ptr(res), q.ctypes.c_size_t(16 * N), q._stream(d2h_s)))
         free_ev[i % 2].record(d2h_s)
