@@ -20,7 +20,7 @@
 // Kernels: split_a / split_b write the pieces as bf16 planes in the UMMA K-major
 // core-matrix layout (8 rows x 16 bytes; per tile and K-step of 16 a contiguous block,
 // LBO 128 B, SBO 256 B). The GEMM is persistent, one CTA per SM, tiles of 128 rows of C^
-// x 256 columns x one K-slice: warp 0 streams each K-step's six blocks (36 KB) into a 4-stage
+// x 256 columns x one K-slice: warp 0 streams each K-step's six blocks (36 KB) into a 5-stage
 // shared-memory ring with bulk copies (cp.async.bulk, mbarrier transaction counts),
 // warp 1's elected thread issues six tcgen05.mma (M 128, N 256, K 16) per K-step into
 // the two TMEM accumulators and commits the stage back to the producer, and warps 2-5
@@ -49,7 +49,7 @@ constexpr int GM_M = 128;  // MMA M: rows of the real-form tile
 constexpr int GM_N = 256;  // MMA N: columns of C per tile
 constexpr int GM_K = bx3::K_STEP;  // bf16 K per MMA
 constexpr int GM_P = bx3::PIECES;  // bf16 pieces per real
-constexpr int GM_STAGES = 4;
+constexpr int GM_STAGES = 5;
 constexpr int GM_A_BLOCK = GM_M * GM_K * 2;  // 4096 bytes: one plane, one tile, one K-step
 constexpr int GM_B_BLOCK = GM_N * GM_K * 2;  // 8192 bytes
 constexpr int GM_STAGE_BYTES = GM_P * (GM_A_BLOCK + GM_B_BLOCK);
