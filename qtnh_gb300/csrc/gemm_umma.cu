@@ -404,35 +404,6 @@ __global__ void split_b_kernel(const double2* __restrict__ B, uint64_t K, uint64
   }
 }
 
-// Four columns per thread (N % 4 == 0): float4 loads of the Re and Im rows of every slice.
-__global__ void reduce_partials4_kernel(const float* __restrict__ P, uint32_t S, uint64_t rows, uint64_t ldp,
-                                        double2* __restrict__ C, uint64_t M, uint64_t N) {
-  const uint64_t N4 = N / 4, total = M * N4;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t m = i / N4, n = (i % N4) * 4;
-    float sr[4] = {0, 0, 0, 0}, er[4] = {0, 0, 0, 0}, si[4] = {0, 0, 0, 0}, ei[4] = {0, 0, 0, 0};
-    for (uint32_t s = 0; s < S; ++s) {
-      const float* ps = P + (uint64_t)s * rows * ldp;
-      const float4 a = *reinterpret_cast<const float4*>(ps + (2 * m) * ldp + n);
-      const float4 b = *reinterpret_cast<const float4*>(ps + (2 * m + 1) * ldp + n);
-      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        float t, e;
-        df::two_sum(sr[c], av[c], t, e);
-        sr[c] = t;
-        er[c] = __fadd_rn(er[c], e);
-        df::two_sum(si[c], bv[c], t, e);
-        si[c] = t;
-        ei[c] = __fadd_rn(ei[c], e);
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-      C[m * N + n + c] = make_double2((double)sr[c] + (double)er[c], (double)si[c] + (double)ei[c]);
-  }
-}
-
 // C[m][n] = sum over the S slices of the partials of rows 2m (Re) and 2m + 1 (Im) of
 // C^, with compensated FP32 additions (TwoSum), rounded once to double.
 __global__ void reduce_partials_kernel(const float* __restrict__ P, uint32_t S, uint64_t rows, uint64_t ldp,
@@ -537,12 +508,8 @@ static void gemm_core(const Prep& pa, const Prep& pb, void* Cv, uint64_t M, uint
     }
     count_launch();
     if (p.S > 1) {
-      if (N % 4 == 0)
-        reduce_partials4_kernel<<<grid_for((M * N / 4 + 255) / 256, 8), 256, 0, s>>>(
-            p.partial, p.S, (uint64_t)p.MT * GM_M, (uint64_t)p.NT * GM_N, C, M, N);
-      else
-        reduce_partials_kernel<<<grid_for((M * N + 255) / 256, 8), 256, 0, s>>>(
-            p.partial, p.S, (uint64_t)p.MT * GM_M, (uint64_t)p.NT * GM_N, C, M, N);
+      reduce_partials_kernel<<<grid_for((M * N + 255) / 256, 8), 256, 0, s>>>(
+          p.partial, p.S, (uint64_t)p.MT * GM_M, (uint64_t)p.NT * GM_N, C, M, N);
       count_launch();
     }
     check_cuda(cudaGetLastError(), "split GEMM launch");
