@@ -144,3 +144,24 @@ def test_split_fused_permutes(d1, d2, wires, bf16x3):
     q.set_gemm_precision(q.GEMM_BF16X3)
     rel, mx = errors(host(split.data), host(plain.data))
     assert rel < 2e-6 and mx < 2e-5, (d1, d2, wires, rel, mx)
+
+
+@pytest.mark.parametrize("d1,d2,wires", [
+    ([4, 2], [2, 4, 3], [(1, 0), (0, 1)]),      # A fully wired and permuted: M = 1
+    ([3, 5, 2], [2, 5], [(2, 0), (1, 1)]),      # B fully wired: N = 1
+    ([1, 6, 1, 3], [3, 1, 7], [(3, 0)]),        # size-1 axes on both sides
+    ([5, 1, 4], [1, 9], [(1, 0)]),              # K = 1 (one wire of size 1)
+    ([2, 2, 2, 2, 2, 2], [2, 2, 2, 2], [(5, 0), (0, 3)]),  # qubit tensors, wires at both ends
+])
+def test_split_fused_edge_shapes(d1, d2, wires, bf16x3):
+    # degenerate shapes through the fused permute-split and padding kernels
+    rng = np.random.default_rng(7 * len(d1) + len(d2))
+    a = crandn(rng, d1)
+    b = crandn(rng, d2)
+    t1, t2 = q.Tensor(q.DENSE, [], d1, dev(a)), q.Tensor(q.DENSE, [], d2, dev(b))
+    split, _, _, _ = q.contract(t1, t2, wires)
+    q.set_gemm_precision(q.GEMM_FP64)
+    plain, _, _, _ = q.contract(t1, t2, wires)
+    q.set_gemm_precision(q.GEMM_BF16X3)
+    rel, mx = errors(host(split.data), host(plain.data))
+    assert rel < 2e-6 and mx < 2e-5, (d1, d2, wires, rel, mx)
