@@ -235,6 +235,11 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
       key = max(key, sm.key[t][h ^ 1][r]);
       const uint32_t emax = oz::key_exponent(key), escale = oz::digit_scale(emax);
       const bool ok = gok && tc_scale_ok(emax);
+      // this thread's stage slots are read again only by the other half of its row, and
+      // only when that row takes the FP64 path: a warp whose rows all take the tensor path
+      // refills its slots with the next tile now, the others after the whole team arrived
+      const bool early = __all_sync(0xffffffffu, ok);
+      if (early) fetch(tile_of(m + UM_WG));
       // digits of this thread's 16 reals: K core h (real parts of amplitudes 8h..8h+7)
       // and K core 2 + h (their imaginary parts)
 #pragma unroll
@@ -260,13 +265,20 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
       if (!ok) half_group_fp64<IT>(psi, gbase, p, sm.U16, &sm.stage[t][0][r], h);
       fence_proxy_async();
       mbar_arrive(&sm.full[t]);
+      if (!early) {
+        // every thread of the team has arrived: the FP64 path of the rows is done with the stage
+        if (!mbar_wait_warp(&sm.full[t], it & 1u, &sm.abort)) {
+          atomicOr(&g_umma_error, 2u);
+          sm.abort = 1;
+          break;
+        }
+        fetch(tile_of(m + UM_WG));
+      }
       if (!mbar_wait_warp(&sm.done[t], it & 1u, &sm.abort)) {
         atomicOr(&g_umma_error, 2u);
         sm.abort = 1;
         break;
       }
-      // every thread of the team has arrived (the MMAs ran): the stage is free
-      fetch(tile_of(m + UM_WG));
       tc_fence_after();
       // level sums: TMEM lane r, columns t * UM_COLS + 32 l + o (o < 16: real part of
       // amplitude o, o >= 16: imaginary part of amplitude o - 16)
