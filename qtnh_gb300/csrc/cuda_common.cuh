@@ -20,6 +20,11 @@ __device__ __forceinline__ c128 cmul(c128 a, c128 b) {
                       __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
 }
 
+// a*b in four FP64 instructions (two multiplies, two fused multiply-adds).
+__device__ __forceinline__ c128 cmul_fused(c128 a, c128 b) {
+  return make_double2(fma(a.x, b.x, -(a.y * b.y)), fma(a.x, b.y, a.y * b.x));
+}
+
 __device__ __forceinline__ c128 cfma(c128 a, c128 b, c128 acc) {
   // acc + a*b with fused multiply-adds (one rounding per FMA).
   acc.x = fma(a.x, b.x, acc.x);

@@ -159,6 +159,10 @@ struct DiagParams {
 // arithmetic, so that enough bytes are in flight per SM to keep HBM busy. IT is the index
 // type (32-bit when the state and the grid stride fit).
 constexpr int DU = 4;
+// Elements of a thread's DU per step that the default arithmetic mode multiplies in native
+// FP64 beside the float-float ones (QTNH_ARITH_F32X2 keeps all DU in float-float).
+constexpr int DIAG_FP64_SLOTS = 1;
+constexpr int LAYER_FP64_SLOTS = 1;
 
 template <typename IT>
 __device__ __forceinline__ IT diag_index(IT e, const DiagParams& p) {
@@ -208,24 +212,36 @@ __global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const
 
 // The same in float-float: the diagonal comes pre-split (ds, table_split_kernel; a NaN hi
 // part flags an entry outside the float-float range), the amplitude is split per element.
-template <typename IT>
+// The first NF64 of a thread's DU elements per step are multiplied in native FP64 instead:
+// the FP64 unit and the FP32 pipes then work side by side in one instruction stream (each
+// alone caps the kernel below the HBM rate: FP64 by its throughput, float-float by issue).
+template <typename IT, int NF64>
 __global__ void __launch_bounds__(256) diag_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ d,
                                                          const df::cf2* __restrict__ ds,
                                                          const __grid_constant__ DiagParams p) {
+  static_assert(NF64 >= 0 && NF64 < DU, "at least one float-float element per step");
   const IT n = (IT)p.n, step = (IT)gridDim.x * blockDim.x * DU;
   for (IT base = (IT)blockIdx.x * blockDim.x * DU + threadIdx.x; base < n; base += step) {
-    c128 x[DU];
+    c128 x[DU], fd[NF64 > 0 ? NF64 : 1];
     df::cf2 f[DU];
     IT idx[DU];
 #pragma unroll
     for (int u = 0; u < DU; ++u) {
       const IT e = base + (IT)(u * blockDim.x);
-      if (e < n) idx[u] = diag_index<IT>(e, p), x[u] = psi[e], f[u] = ds[idx[u]];
+      if (e < n) {
+        idx[u] = diag_index<IT>(e, p), x[u] = psi[e];
+        if (u < NF64) fd[u < NF64 ? u : 0] = __ldg(d + idx[u]);
+        else f[u] = ds[idx[u]];
+      }
     }
 #pragma unroll
     for (int u = 0; u < DU; ++u) {
       const IT e = base + (IT)(u * blockDim.x);
       if (e >= n) continue;
+      if (u < NF64) {
+        psi[e] = cmul_fused(x[u], fd[u < NF64 ? u : 0]);
+        continue;
+      }
       const bool ok = f[u].re.h == f[u].re.h && df::in_range_state(x[u].x) && df::in_range_state(x[u].y);
       if (__all_sync(__activemask(), ok)) {
         df::acc re, im;
@@ -305,15 +321,18 @@ __global__ void table_split_kernel(const c128* __restrict__ t, df::cf2* __restri
   }
 }
 
-template <typename IT>
+// Float-float layer; the first NF64 of a thread's DU elements per step in native FP64
+// (as diag_kernel_f32x2).
+template <typename IT, int NF64>
 __global__ void __launch_bounds__(256) layer_apply_kernel_f32x2(c128* __restrict__ psi, const c128* __restrict__ hi,
                                                                 const c128* __restrict__ lo,
                                                                 const df::cf2* __restrict__ his,
                                                                 const df::cf2* __restrict__ los, uint64_t n64,
                                                                 uint64_t lo_size64, uint32_t lo_log2) {
+  static_assert(NF64 >= 0 && NF64 < DU, "at least one float-float element per step");
   const IT n = (IT)n64, lo_size = (IT)lo_size64, step = (IT)gridDim.x * blockDim.x * DU;
   for (IT base = (IT)blockIdx.x * blockDim.x * DU + threadIdx.x; base < n; base += step) {
-    c128 x[DU];
+    c128 x[DU], ad[NF64 > 0 ? NF64 : 1], bd[NF64 > 0 ? NF64 : 1];
     df::cf2 a[DU], b[DU];
 #pragma unroll
     for (int u = 0; u < DU; ++u) {
@@ -322,14 +341,23 @@ __global__ void __launch_bounds__(256) layer_apply_kernel_f32x2(c128* __restrict
         IT h, l;
         hi_lo<IT>(e, lo_size, lo_log2, h, l);
         x[u] = psi[e];
-        a[u] = his[h];
-        b[u] = los[l];
+        if (u < NF64) {
+          ad[u < NF64 ? u : 0] = __ldg(hi + h);
+          bd[u < NF64 ? u : 0] = __ldg(lo + l);
+        } else {
+          a[u] = his[h];
+          b[u] = los[l];
+        }
       }
     }
 #pragma unroll
     for (int u = 0; u < DU; ++u) {
       const IT e = base + (IT)(u * blockDim.x);
       if (e >= n) continue;
+      if (u < NF64) {
+        psi[e] = cmul_fused(x[u], cmul_fused(ad[u < NF64 ? u : 0], bd[u < NF64 ? u : 0]));
+        continue;
+      }
       const bool ok = a[u].re.h == a[u].re.h && b[u].re.h == b[u].re.h && df::in_range_state(x[u].x) &&
                       df::in_range_state(x[u].y);
       if (__all_sync(__activemask(), ok)) {
@@ -468,8 +496,14 @@ void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16
     // the diagonal's entries split once into float pairs
     df::cf2* ds = static_cast<df::cf2*>(workspace_alloc(m * sizeof(df::cf2), stream));
     table_split_kernel<<<grid_for((m + 255) / 256, 4), 256, 0, s>>>(d_, ds, m);
-    if (index32(n, grid)) diag_kernel_f32x2<uint32_t><<<grid, 256, 0, s>>>(st_, d_, ds, p);
-    else diag_kernel_f32x2<uint64_t><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+    const bool i32 = index32(n, grid);
+    if (arithmetic_mode() == QTNH_ARITH_F32X2) {
+      if (i32) diag_kernel_f32x2<uint32_t, 0><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+      else diag_kernel_f32x2<uint64_t, 0><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+    } else {
+      if (i32) diag_kernel_f32x2<uint32_t, DIAG_FP64_SLOTS><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+      else diag_kernel_f32x2<uint64_t, DIAG_FP64_SLOTS><<<grid, 256, 0, s>>>(st_, d_, ds, p);
+    }
     count_launch(2);
     const cudaError_t e = cudaGetLastError();
     workspace_free(ds, stream);
@@ -526,12 +560,21 @@ void apply_diag_layer_device(void* state, const dims_t& dims, const std::vector<
   if (ff) {
     df::cf2* split_tab = reinterpret_cast<df::cf2*>(tables + tab);
     table_split_kernel<<<grid_for((tab + 255) / 256, 4), 256, 0, s>>>(tables, split_tab, tab);
-    if (i32)
-      layer_apply_kernel_f32x2<uint32_t><<<grid, 256, 0, s>>>(st_, tables + lo_size, tables, split_tab + lo_size,
-                                                              split_tab, n, lo_size, lo_log2);
-    else
-      layer_apply_kernel_f32x2<uint64_t><<<grid, 256, 0, s>>>(st_, tables + lo_size, tables, split_tab + lo_size,
-                                                              split_tab, n, lo_size, lo_log2);
+    const c128* hi_t = tables + lo_size;
+    const df::cf2* his = split_tab + lo_size;
+    if (arithmetic_mode() == QTNH_ARITH_F32X2) {
+      if (i32)
+        layer_apply_kernel_f32x2<uint32_t, 0><<<grid, 256, 0, s>>>(st_, hi_t, tables, his, split_tab, n, lo_size, lo_log2);
+      else
+        layer_apply_kernel_f32x2<uint64_t, 0><<<grid, 256, 0, s>>>(st_, hi_t, tables, his, split_tab, n, lo_size, lo_log2);
+    } else {
+      if (i32)
+        layer_apply_kernel_f32x2<uint32_t, LAYER_FP64_SLOTS><<<grid, 256, 0, s>>>(st_, hi_t, tables, his, split_tab, n,
+                                                                                lo_size, lo_log2);
+      else
+        layer_apply_kernel_f32x2<uint64_t, LAYER_FP64_SLOTS><<<grid, 256, 0, s>>>(st_, hi_t, tables, his, split_tab, n,
+                                                                                lo_size, lo_log2);
+    }
     count_launch(4);
   } else {
     if (i32)
