@@ -958,7 +958,9 @@ def main_kernels(a):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         gbs = bpe * N / (ms * 1e-3) / 1e9
-        label = {"fp64": "fp64", "f32x2": "f32x2", "bf16x6": "default: fp64 + f32x2"}[arith]
+        label = {"fp64": "fp64", "f32x2": "f32x2",
+                 "bf16x6": "default: tensor cores, gate (x) identity" if name.startswith("gate")
+                 else "default: fp64 + f32x2"}[arith]
         out["%s [%s]" % (name, label)] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "bytes": bpe * N}
     launches = q.launches() - l0
     ck = clocks.stop()

@@ -179,17 +179,6 @@ __device__ __forceinline__ IT diag_index(IT e, const DiagParams& p) {
 
 __device__ __noinline__ c128 cmul_fp64_outofline(c128 a, c128 b) { return cmul(a, b); }
 
-// a * b in float-float when both are in range (warp-uniform decision), else FP64.
-__device__ __forceinline__ c128 cmul_f32x2(c128 a, c128 b) {
-  bool ok = df::in_range_state(a.x) && df::in_range_state(a.y) && df::in_range_gate(b.x) && df::in_range_gate(b.y);
-  if (__all_sync(__activemask(), ok)) {
-    df::acc re, im;
-    df::cmul_acc(df::csplit(a.x, a.y), df::csplit(b.x, b.y), re, im);
-    return make_double2(df::to_double(re), df::to_double(im));
-  }
-  return cmul_fp64_outofline(a, b);
-}
-
 // psi[e] *= d[index of e over the targets] in FP64.
 template <typename IT>
 __global__ void __launch_bounds__(256) diag_kernel(c128* __restrict__ psi, const c128* __restrict__ d,
@@ -417,6 +406,7 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
   uint64_t D = 1;
   for (auto t : targets) D *= dims[t];
   if (product(dims) == 0) return;
+  if (arithmetic_mode() == QTNH_ARITH_BF16X6 && apply_gate_tc_single(state, dims, targets, gate, stream)) return;
   GateParams p;
   other_axes(dims, targets, p.other);
   dims_t st = row_strides(dims);

@@ -242,9 +242,55 @@ PairParams make_pair_params(const dims_t& dims, const uint16_t all[4]) {
   return p;
 }
 
+namespace {
+
+// The 4x4 identity in SymmTensor layout: the second gate of a lone gate's pair.
+__device__ const double2 g_identity4[16] = {{1.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0},
+                                            {0.0, 0.0}, {1.0, 0.0}, {0.0, 0.0}, {0.0, 0.0},
+                                            {0.0, 0.0}, {0.0, 0.0}, {1.0, 0.0}, {0.0, 0.0},
+                                            {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {1.0, 0.0}};
+
+// tcgen05 kernel from one 128-group tile up, mma.sync kernel below.
+void launch_fused_pair(double2* psi, const double2* a, const double2* b, const PairParams& p, uint64_t n,
+                       cudaStream_t s) {
+  if (!launch_pair_umma(psi, a, b, p, s)) {
+    if (n <= (1ull << 32))
+      launch_pair<uint32_t>(psi, a, b, p, s);
+    else
+      launch_pair<uint64_t>(psi, a, b, p, s);
+  }
+  count_launch();
+  check_cuda(cudaGetLastError(), "gate pair kernel launch");
+}
+
+}  // namespace
+
+bool apply_gate_tc_single(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* gate,
+                          void* stream) {
+  if (targets.size() != 2) return false;
+  for (auto d : dims)
+    if (log2_or_none(d) == 0xFFFFFFFFu) return false;
+  if (dims[targets[0]] != 2 || dims[targets[1]] != 2) return false;
+  const uint64_t n = product(dims);
+  if (n < 128) return false;
+  // the identity takes the two free size-2 axes of largest stride: the groups' varying
+  // bits then stay above the low bits that consecutive groups run over
+  uint16_t idle[2];
+  int found = 0;
+  for (size_t a = 0; a < dims.size() && found < 2; ++a)
+    if (dims[a] == 2 && a != targets[0] && a != targets[1]) idle[found++] = (uint16_t)a;
+  if (found < 2) return false;
+  const uint16_t tg[4] = {targets[0], targets[1], idle[0], idle[1]};
+  void* ident = nullptr;
+  check_cuda(cudaGetSymbolAddress(&ident, g_identity4), "identity gate address");
+  launch_fused_pair(static_cast<double2*>(state), static_cast<const double2*>(gate),
+                    static_cast<const double2*>(ident), make_pair_params(dims, tg), n, (cudaStream_t)stream);
+  return true;
+}
+
 // Pairs of consecutive, disjoint two-qubit gates on a power-of-two state are fused and
-// applied on the tensor cores; everything else goes through apply_gate_device. Returns
-// after issuing all launches.
+// applied on the tensor cores; everything else goes through apply_gate_device (where a
+// lone two-qubit gate is paired with the identity). Returns after issuing all launches.
 void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
                          const std::vector<const void*>& gates, void* stream) {
   const size_t r = dims.size();
@@ -266,19 +312,8 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
       ok = ok && std::adjacent_find(srt.begin(), srt.end()) == srt.end();
       if (ok) {
         const uint16_t tg[4] = {ta[0], ta[1], tb[0], tb[1]};
-        const PairParams p = make_pair_params(dims, tg);
-        double2* psi = static_cast<double2*>(state);
-        const double2* a = static_cast<const double2*>(gates[g]);
-        const double2* b = static_cast<const double2*>(gates[g + 1]);
-        // tcgen05 kernel from one 128-group tile up, mma.sync kernel below
-        if (!launch_pair_umma(psi, a, b, p, s)) {
-          if (n <= (1ull << 32))
-            launch_pair<uint32_t>(psi, a, b, p, s);
-          else
-            launch_pair<uint64_t>(psi, a, b, p, s);
-        }
-        count_launch();
-        check_cuda(cudaGetLastError(), "gate pair kernel launch");
+        launch_fused_pair(static_cast<double2*>(state), static_cast<const double2*>(gates[g]),
+                          static_cast<const double2*>(gates[g + 1]), make_pair_params(dims, tg), n, s);
         g += 2;
         fused = true;
       }

@@ -453,6 +453,29 @@ def test_gate_pairs_tensor_core_fall_back_out_of_range(bf16x6):
         assert rel_l2(out[sl], ref[sl]) < REL_TOL
 
 
+@pytest.mark.parametrize("dims,targets,scale", [
+    ([2] * 14, [0, 1], 1.0),              # targets on the two top axes: identity on axes 2, 3
+    ([2] * 14, [13, 6], 1.0),             # innermost target: identity on axes 0, 1
+    ([2] * 8, [5, 2], 1.0),               # 16 groups: the mma.sync kernel
+    ([4, 2, 8, 2, 2, 2, 2, 2, 2, 2], [3, 9], 1.0),  # identity skips the size-4 and size-8 axes
+    ([2] * 12, [4, 7], 1e250),            # entries out of the digit range: FP64 groups
+    ([3, 2, 2, 2, 2, 2, 2, 2, 2], [1, 5], 1.0),     # not a power of two: float-float kernel
+], ids=["top", "inner", "small", "mixed-radix", "huge-gate", "qutrit-axis"])
+def test_lone_gate_on_tensor_cores(dims, targets, scale, bf16x6):
+    # a single two-qubit gate runs as the pair gate (x) identity on the tensor cores
+    nrng = np.random.default_rng(len(dims) * 7 + targets[0])
+    psi = crandn(nrng, dims)
+    els = crandn(nrng, [16]) * scale
+    st = dev(psi)
+    before = q.launches()
+    q.apply_gate(st, dims, targets, dev(els))
+    if 3 not in dims:
+        assert q.launches() - before == 1
+    ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], dims, psi), orc.Tensor(orc.SYMM, [], [2] * 4, els),
+                             [(targets[0], 0), (targets[1], 1)])
+    assert rel_l2(host(st), ref.els) < REL_TOL
+
+
 def test_gate_pairs_tensor_core_general_gate_and_fallback(bf16x6):
     # non-unitary gates: rows of very different scale; a gate with huge entries runs FP64
     nrng = np.random.default_rng(14)
