@@ -3,8 +3,10 @@
 //
 // A tile is 128 groups (16 amplitudes each). Per tile, D_l[g][o] = sum over digit pairs
 // (i, j), i + j = l, of X_j[g][k] * R_i[o][k] (M = 128 groups, N = 32 output reals, K = 32
-// input reals) -- 21 digit pairs x 2 K-steps = 42 tcgen05.mma (kind::f16, bf16 operands,
-// FP32 accumulators) into six level column blocks of TMEM.
+// input reals), the 21 digit pairs i + j <= 5, into six level column blocks of TMEM. The
+// gate digits of one K-step lie stacked along N (digit i at rows 32 i ..), so state digit
+// j meets gate digits 0 .. 5 - j in one tcgen05.mma (kind::f16, bf16 operands, FP32
+// accumulators) of N = 32 (6 - j) into columns 32 j ..: 6 digits x 2 K-steps = 12 MMAs.
 //
 // CTA = a team of eight warps + one MMA warp; two CTAs per SM (persistent; each holds half
 // of the SM's tensor memory and ~97 KB of shared memory):
@@ -14,7 +16,7 @@
 //     cp.async, the two exchange their largest exponents through shared memory (an
 //     mbarrier), and each writes its 6 x 16 digits into shared memory in the UMMA
 //     K-major core-matrix layout (8 rows x 16 bytes) and arrives on full;
-//   * the MMA warp waits on full, issues the 42 MMAs into the CTA's TMEM columns and
+//   * the MMA warp waits on full, issues the 12 MMAs into the CTA's TMEM columns and
 //     commits them to done;
 //   * the team waits on done, and each thread reads the level sums of its 8 amplitudes
 //     from its TMEM lane with tcgen05.ld, recombines and stores them.
@@ -53,7 +55,7 @@ constexpr long long UM_WAIT_CYCLES = 1ll << 31;  // ~1 s at 2 GHz
 // core (row group rg, K half kh) sits at rg * 256 + kh * 128: LBO = 128, SBO = 256.
 struct UmSmem {
   uint8_t adig[UM_WG][oz::NS][2][UM_M * 32];  // state digits: team, digit, K-step (4 KB each)
-  uint8_t bdig[oz::NS][2][UM_N * 32];         // gate digits: digit, K-step (1 KB each)
+  uint8_t bdig[2][oz::NS][UM_N * 32];         // gate digits: K-step, digit (1 KB each; digits stack along N)
   double2 stage[UM_WG][16][UM_M];             // fetched amplitudes: team, amplitude, group
   uint32_t key[UM_WG][2][UM_M];               // largest exponent key of each half group
   double2 U16[256];                           // fused unitary, U16[o * 16 + i]
@@ -108,14 +110,18 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
 
 // Instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12
 // = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(UM_N >> 3) << 17) |
-                              ((uint32_t)(UM_M >> 4) << 24);
+__host__ __device__ constexpr uint32_t um_idesc(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(UM_M >> 4) << 24);
+}
+static_assert(oz::NS == oz::NL, "state digit j meets gate digits 0 .. NL - 1 - j");
+static_assert(UM_N * oz::NL <= 256, "an MMA's N is at most 256");
 
-__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(UM_IDESC), "r"(accumulate));
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
@@ -190,7 +196,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
     for (int j = 0; j < oz::NS; ++j) {
       const uint4 v = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]), oz::pack(d[4][j], d[5][j]),
                                  oz::pack(d[6][j], d[7][j]));
-      *reinterpret_cast<uint4*>(&sm.bdig[j][kc >> 1][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) = v;
+      *reinterpret_cast<uint4*>(&sm.bdig[kc >> 1][j][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) = v;
     }
   }
   fence_proxy_async();
@@ -308,7 +314,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
     }
     cp_async_wait_all();
   } else {
-    // ---- MMA warp: one elected thread issues each tile's 42 MMAs ----
+    // ---- MMA warp: one elected thread issues each tile's 12 MMAs ----
     const uint32_t bbase = smem_u32(&sm.bdig[0][0][0]);
     for (uint64_t m = 0; tile_of(m) < ntiles; ++m) {
       const int w = (int)(m % UM_WG);
@@ -322,20 +328,16 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
       if (lane == 0) {
         const uint32_t abase = smem_u32(&sm.adig[w][0][0][0]);
         const uint32_t dcol = tmem + (uint32_t)(w * UM_COLS);
+        // state digit j x gate digits 0 .. NL-1-j (stacked along N) -> levels j .. NL-1;
+        // the first MMA (j = 0, all six levels) overwrites, the rest accumulate
 #pragma unroll
-        for (int l = 0; l < oz::NL; ++l) {
-          uint32_t acc = 0;
+        for (int j = 0; j < oz::NS; ++j) {
 #pragma unroll
-          for (int i = 0; i < oz::NS; ++i) {
-            const int j = l - i;
-            if (j < 0 || j >= oz::NS) continue;
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks) {
-              const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
-              const uint64_t bd = smem_desc(bbase + (uint32_t)((i * 2 + ks) * UM_N * 32));
-              umma_bf16(dcol + (uint32_t)(l * UM_N), ad, bd, acc);
-              acc = 1;
-            }
+          for (int ks = 0; ks < 2; ++ks) {
+            const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
+            const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * oz::NS * UM_N * 32));
+            umma_bf16(dcol + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (oz::NL - j))),
+                      (j | ks) != 0 ? 1u : 0u);
           }
         }
         umma_commit(&sm.done[w]);
