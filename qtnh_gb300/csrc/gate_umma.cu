@@ -14,7 +14,7 @@
 //     (warp quarter q = r / 32 of the team's first and second four warps), each
 //     owning 8 of the group's 16 amplitudes: it fetches them one tile ahead with
 //     cp.async, the two exchange their largest exponents through shared memory (an
-//     mbarrier), and each writes its 6 x 16 digits into shared memory in the UMMA
+//     mbarrier of the two warps of quarter q), and each writes its 6 x 16 digits into shared memory in the UMMA
 //     K-major core-matrix layout (8 rows x 16 bytes) and arrives on full;
 //   * the MMA warp waits on full, issues the 12 MMAs into the CTA's TMEM columns and
 //     commits them to done;
@@ -61,7 +61,7 @@ struct UmSmem {
   double2 U16[256];                           // fused unitary, U16[o * 16 + i]
   int32_t erow[16];                           // largest exponent of row o of U16
   uint32_t krow[16];                          // oz::scale_bits(erow[o])
-  uint64_t keyx[UM_WG];                       // both halves' keys (and fetched amplitudes) are visible
+  uint64_t keyx[UM_WG][4];                    // per row quarter: both halves' keys (and amplitudes) are visible
   uint64_t full[UM_WG];                       // digits of team t's tile are ready
   uint64_t done[UM_WG];                       // MMAs of team t's tile are complete
   uint32_t tmem_base;
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
     sm.gate_ok = 1;
     sm.abort = 0;
     for (int w = 0; w < UM_WG; ++w) {
-      mbar_init(&sm.keyx[w], UM_TEAM);
+      for (int qq = 0; qq < 4; ++qq) mbar_init(&sm.keyx[w][qq], 64);  // the quarter's two warps
       mbar_init(&sm.full[w], UM_TEAM);
       mbar_init(&sm.done[w], 1);
     }
@@ -232,8 +232,8 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
 #pragma unroll
       for (int c = 0; c < 8; ++c) key = max(key, max(oz::group_key(df::words(x[c].x)), oz::group_key(df::words(x[c].y))));
       sm.key[t][h][r] = key;
-      mbar_arrive(&sm.keyx[t]);  // both halves' keys and fetched amplitudes become visible
-      if (!mbar_wait_warp(&sm.keyx[t], it & 1u, &sm.abort)) {
+      mbar_arrive(&sm.keyx[t][q]);  // both halves' keys and fetched amplitudes become visible
+      if (!mbar_wait_warp(&sm.keyx[t][q], it & 1u, &sm.abort)) {
         atomicOr(&g_umma_error, 4u);
         sm.abort = 1;
         break;
