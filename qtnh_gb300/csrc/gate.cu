@@ -352,7 +352,10 @@ __global__ void __launch_bounds__(256) layer_apply_kernel_f32x2(c128* __restrict
       if (__all_sync(__activemask(), ok)) {
         df::acc pr, pi;
         df::cmul_acc(a[u], b[u], pr, pi);
-        df::cf2 ph{df::renorm(pr), df::renorm(pi)};
+        // the unnormalised pairs (sum, error) enter the next product as they are: its
+        // TwoProduct multiplies out all four hi/lo terms, and the error part is a few
+        // units in the last place of the sum
+        const df::cf2 ph{{pr.s, pr.c}, {pi.s, pi.c}};
         df::acc re, im;
         df::cmul_acc(df::csplit(x[u].x, x[u].y), ph, re, im);
         psi[e] = make_double2(df::to_double(re), df::to_double(im));
