@@ -907,6 +907,10 @@ def main_kernels(a):
     m = rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))
     u, _ = np.linalg.qr(m)
     gate = torch.tensor(np.ascontiguousarray(u.T).reshape(-1), dtype=torch.complex128, device=dev)
+    m4 = rng.standard_normal((16, 16)) + 1j * rng.standard_normal((16, 16))
+    u4, _ = np.linalg.qr(m4)
+    gate4 = torch.tensor(np.ascontiguousarray(u4.T).reshape(-1), dtype=torch.complex128, device=dev)
+    t4 = [2, 9, n - 12, n - 3]
 
     def top3_with(lo):
         pt = list(range(n))
@@ -937,6 +941,10 @@ def main_kernels(a):
          lambda: q.apply_gate(x, dims, [4, n - 3], gate)),
         ("gate: two-qubit SymmTensor on (4, %d)" % (n - 3), "bf16x6", 32,
          lambda: q.apply_gate(x, dims, [4, n - 3], gate)),
+        ("gate: four-qubit SymmTensor on (%d, %d, %d, %d)" % tuple(t4), "f32x2", 32,
+         lambda: q.apply_gate(x, dims, t4, gate4)),
+        ("gate: four-qubit SymmTensor on (%d, %d, %d, %d)" % tuple(t4), "bf16x6", 32,
+         lambda: q.apply_gate(x, dims, t4, gate4)),
         ("norm: FP64 sum of squares", "fp64", 16, lambda: q.norm2(x)),
     ]
     old = q.get_arithmetic()
@@ -959,7 +967,7 @@ def main_kernels(a):
         ms = e0.elapsed_time(e1) / reps
         gbs = bpe * N / (ms * 1e-3) / 1e9
         label = {"fp64": "fp64", "f32x2": "f32x2",
-                 "bf16x6": "default: tensor cores, gate (x) identity" if name.startswith("gate")
+                 "bf16x6": "default: tensor cores" if name.startswith("gate")
                  else "default: fp64 + f32x2"}[arith]
         out["%s [%s]" % (name, label)] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "bytes": bpe * N}
     launches = q.launches() - l0

@@ -109,9 +109,10 @@ int qtnh_take_device_errors(uint32_t* flags);
  *   level is summed exactly in FP32 (Ozaki scheme), and the levels are recombined to ~48
  *   bits; relative error ~1e-14 per fused pair. Groups whose largest magnitude lies
  *   outside 2^-200..2^200 (or holds an infinity/NaN) take FP64; subnormal amplitudes
- *   count as zero there. A lone two-qubit gate (qtnh_apply_gate, or the odd one of a
- *   layer) on a power-of-two state with two more size-2 indices runs the same way as the
- *   pair gate (x) identity. Every other gate runs as QTNH_ARITH_F32X2; diagonals (single
+ *   count as zero there. A lone gate on 2, 3 or 4 size-2 indices (qtnh_apply_gate, or
+ *   the odd one of a layer) of a power-of-two state runs the same way as one 16x16
+ *   operator: gate (x) I4, gate (x) I2 (free size-2 indices), or the four-qubit gate
+ *   itself. Every other gate runs as QTNH_ARITH_F32X2; diagonals (single
  *   DiagTensors and per-index layers) multiply one element in four in native FP64 (two
  *   fused multiply-adds per component) and the other three as QTNH_ARITH_F32X2, so the
  *   FP64 unit works beside the FP32 pipes.

@@ -10,6 +10,13 @@
 
 namespace qtnh_impl {
 
+// How the 16x16 operator of a group is formed from the gate pointers (ga, gb).
+enum PairGate : uint32_t {
+  PAIR_KRON = 0,   // two two-qubit gates: U16 = Ua (x) Ub
+  PAIR_FULL = 1,   // one four-qubit gate: U16 = Ua (16 x 16; gb unused)
+  PAIR_KRON_I2 = 2 // one three-qubit gate on the first three targets: U16 = Ua (8 x 8) (x) I2
+};
+
 struct PairParams {
   uint64_t ngroups;     // state size / 16
   uint32_t ins_pos[4];  // the four target bit positions, ascending
@@ -50,10 +57,15 @@ __device__ __forceinline__ bool tc_element_ok(df::dwords w) {
 
 __device__ __forceinline__ bool tc_scale_ok(uint32_t emax) { return emax == 0 || (emax >= TC_EMIN && emax <= TC_EMAX); }
 
-// U16[o * 16 + i] = Ua[oa][ia] Ub[ob][ib] (o = oa * 4 + ob, i = ia * 4 + ib) from two
-// gates in SymmTensor layout G[in * 4 + out] = U[out][in].
+// U16[o * 16 + i] from gates in SymmTensor layout G[in * D + out] = U[out][in]:
+// PAIR_KRON: Ua[oa][ia] Ub[ob][ib] (o = oa * 4 + ob, i = ia * 4 + ib); PAIR_FULL: Ua[o][i];
+// PAIR_KRON_I2: Ua[o >> 1][i >> 1] where the last bits of o and i agree, else 0.
+// (MODE is a template parameter of the kernels, so the gate-pair path compiles as before.)
+template <uint32_t MODE>
 __device__ __forceinline__ double2 fused_entry(const double2* __restrict__ ga, const double2* __restrict__ gb, int t) {
   const int o = t >> 4, i = t & 15;
+  if (MODE == PAIR_FULL) return ga[i * 16 + o];
+  if (MODE == PAIR_KRON_I2) return ((o ^ i) & 1) ? make_double2(0.0, 0.0) : ga[(i >> 1) * 8 + (o >> 1)];
   return cmul(ga[(i >> 2) * 4 + (o >> 2)], gb[(i & 3) * 4 + (o & 3)]);
 }
 
@@ -92,7 +104,8 @@ __device__ __forceinline__ double2 group_output_fp64(const double2* U16, const d
 PairParams make_pair_params(const dims_t& dims, const uint16_t all[4]);
 
 // tcgen05 kernel for states of at least 2048 amplitudes; false if it does not apply.
-bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s);
+bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
+                      uint32_t mode = PAIR_KRON);
 
 // Reads and clears the tcgen05 kernel's device error flags (bounded waits that expired).
 uint32_t take_umma_error();

@@ -74,7 +74,7 @@ __device__ __noinline__ void pair_tile_fp64(double2* __restrict__ psi, IT gbase,
 
 // Two CTAs per SM: up to 128 registers a thread, none spilled (three CTAs spill and run
 // slower).
-template <typename IT>
+template <typename IT, uint32_t MODE>
 __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __restrict__ psi,
                                                                      const double2* __restrict__ ga,
                                                                      const double2* __restrict__ gb,
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __
 
   // ---- the fused gate: U16, row exponents, A fragments of its six digits ----
   if (tid == 0) sm.gate_ok = 1;
-  for (int t = tid; t < 256; t += TC_THREADS) sm.U16[t] = fused_entry(ga, gb, t);
+  for (int t = tid; t < 256; t += TC_THREADS) sm.U16[t] = fused_entry<MODE>(ga, gb, t);
   __syncthreads();
   if (tid < 16) {
     bool ok;
@@ -218,13 +218,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gate_pair_tc_kernel(double2* __
   cp_async_wait_all();
 }
 
-template <typename IT>
+template <typename IT, uint32_t MODE>
 void launch_pair(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
   const size_t smem = sizeof(TcSmem);
-  check_cuda(cudaFuncSetAttribute(gate_pair_tc_kernel<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  check_cuda(cudaFuncSetAttribute(gate_pair_tc_kernel<IT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
              "gate_pair_tc_kernel shared memory");
   const int grid = grid_for(((p.ngroups / 8) + TC_WARPS - 1) / TC_WARPS, 2);
-  gate_pair_tc_kernel<IT><<<grid, TC_THREADS, smem, s>>>(psi, ga, gb, p);
+  gate_pair_tc_kernel<IT, MODE><<<grid, TC_THREADS, smem, s>>>(psi, ga, gb, p);
 }
 
 }  // namespace
@@ -252,12 +252,18 @@ __device__ const double2 g_identity4[16] = {{1.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, 
 
 // tcgen05 kernel from one 128-group tile up, mma.sync kernel below.
 void launch_fused_pair(double2* psi, const double2* a, const double2* b, const PairParams& p, uint64_t n,
-                       cudaStream_t s) {
-  if (!launch_pair_umma(psi, a, b, p, s)) {
-    if (n <= (1ull << 32))
-      launch_pair<uint32_t>(psi, a, b, p, s);
-    else
-      launch_pair<uint64_t>(psi, a, b, p, s);
+                       cudaStream_t s, uint32_t mode = PAIR_KRON) {
+  if (!launch_pair_umma(psi, a, b, p, s, mode)) {
+    if (mode == PAIR_KRON) {
+      if (n <= (1ull << 32))
+        launch_pair<uint32_t, PAIR_KRON>(psi, a, b, p, s);
+      else
+        launch_pair<uint64_t, PAIR_KRON>(psi, a, b, p, s);
+    } else if (mode == PAIR_FULL) {
+      launch_pair<uint32_t, PAIR_FULL>(psi, a, b, p, s);
+    } else {
+      launch_pair<uint32_t, PAIR_KRON_I2>(psi, a, b, p, s);
+    }
   }
   count_launch();
   check_cuda(cudaGetLastError(), "gate pair kernel launch");
@@ -267,30 +273,41 @@ void launch_fused_pair(double2* psi, const double2* a, const double2* b, const P
 
 bool apply_gate_tc_single(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* gate,
                           void* stream) {
-  if (targets.size() != 2) return false;
+  const size_t k = targets.size();
+  if (k < 2 || k > 4) return false;
   for (auto d : dims)
     if (log2_or_none(d) == 0xFFFFFFFFu) return false;
-  if (dims[targets[0]] != 2 || dims[targets[1]] != 2) return false;
+  for (auto t : targets)
+    if (dims[t] != 2) return false;
   const uint64_t n = product(dims);
-  if (n < 128) return false;
-  // the identity takes the two free size-2 axes of largest stride: the groups' varying
+  if (n < 128 || (k > 2 && n > (1ull << 32))) return false;
+  // the identity factor takes the free size-2 axes of largest stride: the groups' varying
   // bits then stay above the low bits that consecutive groups run over
-  uint16_t idle[2];
-  int found = 0;
-  for (size_t a = 0; a < dims.size() && found < 2; ++a)
-    if (dims[a] == 2 && a != targets[0] && a != targets[1]) idle[found++] = (uint16_t)a;
-  if (found < 2) return false;
-  const uint16_t tg[4] = {targets[0], targets[1], idle[0], idle[1]};
-  void* ident = nullptr;
-  check_cuda(cudaGetSymbolAddress(&ident, g_identity4), "identity gate address");
-  launch_fused_pair(static_cast<double2*>(state), static_cast<const double2*>(gate),
-                    static_cast<const double2*>(ident), make_pair_params(dims, tg), n, (cudaStream_t)stream);
+  uint16_t tg[4];
+  for (size_t j = 0; j < k; ++j) tg[j] = targets[j];
+  size_t found = k;
+  for (size_t a = 0; a < dims.size() && found < 4; ++a)
+    if (dims[a] == 2 && std::find(targets.begin(), targets.end(), (uint16_t)a) == targets.end()) tg[found++] = (uint16_t)a;
+  if (found < 4) return false;
+  const double2* g = static_cast<const double2*>(gate);
+  const double2* second = nullptr;
+  uint32_t mode = PAIR_FULL;
+  if (k == 2) {
+    void* ident = nullptr;
+    check_cuda(cudaGetSymbolAddress(&ident, g_identity4), "identity gate address");
+    second = static_cast<const double2*>(ident);
+    mode = PAIR_KRON;
+  } else if (k == 3) {
+    mode = PAIR_KRON_I2;
+  }
+  launch_fused_pair(static_cast<double2*>(state), g, second, make_pair_params(dims, tg), n, (cudaStream_t)stream, mode);
   return true;
 }
 
 // Pairs of consecutive, disjoint two-qubit gates on a power-of-two state are fused and
 // applied on the tensor cores; everything else goes through apply_gate_device (where a
-// lone two-qubit gate is paired with the identity). Returns after issuing all launches.
+// lone gate on two, three or four qubits runs on the tensor cores too). Returns after
+// issuing all launches.
 void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
                          const std::vector<const void*>& gates, void* stream) {
   const size_t r = dims.size();

@@ -149,7 +149,7 @@ __device__ __noinline__ void half_group_fp64(double2* __restrict__ psi, IT gbase
   for (int o = 8 * h; o < 8 * h + 8; ++o) psi[gbase + (IT)p.off[o]] = group_output_fp64(U16, x, o);
 }
 
-template <typename IT>
+template <typename IT, uint32_t MODE>
 __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* __restrict__ psi,
                                                                        const double2* __restrict__ ga,
                                                                        const double2* __restrict__ gb,
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  for (int t = tid; t < 256; t += UM_THREADS) sm.U16[t] = fused_entry(ga, gb, t);
+  for (int t = tid; t < 256; t += UM_THREADS) sm.U16[t] = fused_entry<MODE>(ga, gb, t);
   __syncthreads();
   if (tid < 16) {
     bool ok;
@@ -355,24 +355,35 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
   }
 }
 
-template <typename IT>
+template <typename IT, uint32_t MODE>
 void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
   const size_t smem = sizeof(UmSmem);
-  check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem),
              "gate_pair_umma_kernel shared memory");
   const uint64_t ntiles = p.ngroups / UM_M;
   const int grid = (int)std::min<uint64_t>(ntiles, 2 * (uint64_t)sm_count());  // two CTAs per SM
-  gate_pair_umma_kernel<IT><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p);
+  gate_pair_umma_kernel<IT, MODE><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p);
 }
 
 }  // namespace
 
-bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
+bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
+                      uint32_t mode) {
   if (p.ngroups < (uint64_t)UM_M || p.ngroups % UM_M) return false;
-  if (p.ngroups * 16 <= (1ull << 32))
-    launch_umma<uint32_t>(psi, ga, gb, p, s);
+  const bool i32 = p.ngroups * 16 <= (1ull << 32);
+  if (mode == PAIR_KRON) {
+    if (i32)
+      launch_umma<uint32_t, PAIR_KRON>(psi, ga, gb, p, s);
+    else
+      launch_umma<uint64_t, PAIR_KRON>(psi, ga, gb, p, s);
+    return true;
+  }
+  if (!i32) return false;  // single three- and four-qubit gates: states up to 2^32 amplitudes
+  if (mode == PAIR_FULL)
+    launch_umma<uint32_t, PAIR_FULL>(psi, ga, gb, p, s);
   else
-    launch_umma<uint64_t>(psi, ga, gb, p, s);
+    launch_umma<uint32_t, PAIR_KRON_I2>(psi, ga, gb, p, s);
   return true;
 }
 

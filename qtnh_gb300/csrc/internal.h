@@ -91,8 +91,9 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
                        void* stream);
 void apply_diag_device(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* diag,
                        void* stream);
-// A lone two-qubit gate (power-of-two state, two free size-2 axes) applied on the tensor
-// cores as the pair gate (x) identity; false (nothing launched) where that does not apply.
+// A lone gate on 2, 3 or 4 size-2 indices of a power-of-two state applied on the tensor
+// cores as one 16x16 operator (gate (x) I4, gate (x) I2, or the gate itself; the identity
+// on free size-2 indices); false (nothing launched) where that does not apply.
 bool apply_gate_tc_single(void* state, const dims_t& dims, const std::vector<uint16_t>& targets, const void* gate,
                           void* stream);
 // Gate list in order; consecutive disjoint two-qubit pairs fused onto the tensor cores.

@@ -460,19 +460,27 @@ def test_gate_pairs_tensor_core_fall_back_out_of_range(bf16x6):
     ([4, 2, 8, 2, 2, 2, 2, 2, 2, 2], [3, 9], 1.0),  # identity skips the size-4 and size-8 axes
     ([2] * 12, [4, 7], 1e250),            # entries out of the digit range: FP64 groups
     ([3, 2, 2, 2, 2, 2, 2, 2, 2], [1, 5], 1.0),     # not a power of two: float-float kernel
-], ids=["top", "inner", "small", "mixed-radix", "huge-gate", "qutrit-axis"])
+    ([2] * 13, [12, 3, 7], 1.0),          # three-qubit gate (x) I2
+    ([2] * 8, [0, 7, 2], 1.0),            # three-qubit gate, mma.sync kernel
+    ([2] * 13, [5, 0, 12, 9], 1.0),       # four-qubit gate as the 16x16 operator itself
+    ([2, 4, 2, 2, 8, 2, 2, 2], [0, 2, 3, 7], 1.0),  # four-qubit gate, mixed power-of-two dims
+    ([2] * 11, [1, 6, 2, 10], 1e-250),    # four-qubit gate out of the digit range: FP64 groups
+], ids=["top", "inner", "small", "mixed-radix", "huge-gate", "qutrit-axis", "3q", "3q-small", "4q",
+        "4q-mixed-radix", "4q-tiny-gate"])
 def test_lone_gate_on_tensor_cores(dims, targets, scale, bf16x6):
-    # a single two-qubit gate runs as the pair gate (x) identity on the tensor cores
-    nrng = np.random.default_rng(len(dims) * 7 + targets[0])
+    # a single gate on 2, 3 or 4 qubits runs on the tensor cores as one 16x16 operator
+    # (gate (x) I4, gate (x) I2, or the gate itself)
+    k = len(targets)
+    nrng = np.random.default_rng(len(dims) * 7 + targets[0] + 100 * k)
     psi = crandn(nrng, dims)
-    els = crandn(nrng, [16]) * scale
+    els = crandn(nrng, [4 ** k]) * scale
     st = dev(psi)
     before = q.launches()
     q.apply_gate(st, dims, targets, dev(els))
     if 3 not in dims:
         assert q.launches() - before == 1
-    ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], dims, psi), orc.Tensor(orc.SYMM, [], [2] * 4, els),
-                             [(targets[0], 0), (targets[1], 1)])
+    ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], dims, psi), orc.Tensor(orc.SYMM, [], [2] * (2 * k), els),
+                             [(t, j) for j, t in enumerate(targets)])
     assert rel_l2(host(st), ref.els) < REL_TOL
 
 
