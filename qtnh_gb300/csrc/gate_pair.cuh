@@ -1,8 +1,10 @@
 // Shared pieces of the fused gate-pair kernels (gate_tc.cu: mma.sync, gate_umma.cu:
 // tcgen05): two disjoint two-qubit gates of a layer act on a group of 16 amplitudes (the
-// four target bits varying) as one 16x16 unitary U16 = Ua (x) Ub, in real form
+// four target bits varying) as one 16x16 operator U16 = Ua (x) Ub, in real form
 // R = [[Re U16, -Im U16], [Im U16, Re U16]] (32 x 32) on the group's 32 reals
 // (real parts k = 0..15, imaginary parts k = 16..31), through bf16 digits (ozaki.cuh).
+// A lone gate uses the same kernels with U16 = gate (x) I4, gate (x) I2 or a four-qubit
+// gate itself (PairGate).
 #pragma once
 
 #include "cuda_common.cuh"
