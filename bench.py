@@ -911,6 +911,7 @@ def main_kernels(a):
     u4, _ = np.linalg.qr(m4)
     gate4 = torch.tensor(np.ascontiguousarray(u4.T).reshape(-1), dtype=torch.complex128, device=dev)
     t4 = [2, 9, n - 12, n - 3]
+    h1 = torch.tensor(np.array([1, 1, 1, -1]) / math.sqrt(2.0), dtype=torch.complex128, device=dev)  # Hadamard
 
     def top3_with(lo):
         pt = list(range(n))
@@ -941,6 +942,10 @@ def main_kernels(a):
          lambda: q.apply_gate(x, dims, [4, n - 3], gate)),
         ("gate: two-qubit SymmTensor on (4, %d)" % (n - 3), "bf16x6", 32,
          lambda: q.apply_gate(x, dims, [4, n - 3], gate)),
+        ("gate: one-qubit SymmTensor (Hadamard) on %d" % (n - 6), "fp64", 32,
+         lambda: q.apply_gate(x, dims, [n - 6], h1)),
+        ("gate: one-qubit SymmTensor (Hadamard) on %d" % (n - 6), "f32x2", 32,
+         lambda: q.apply_gate(x, dims, [n - 6], h1)),
         ("gate: four-qubit SymmTensor on (%d, %d, %d, %d)" % tuple(t4), "f32x2", 32,
          lambda: q.apply_gate(x, dims, t4, gate4)),
         ("gate: four-qubit SymmTensor on (%d, %d, %d, %d)" % tuple(t4), "bf16x6", 32,
