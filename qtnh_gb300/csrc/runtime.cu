@@ -12,6 +12,7 @@
 #include <string>
 
 #include "cuda_common.cuh"
+#include "df32.cuh"
 
 namespace qtnh_impl {
 
@@ -82,10 +83,29 @@ void workspace_free(void* p, void* stream) {
   if (p) check_cuda(cudaFreeAsync(p, (cudaStream_t)stream), "cudaFreeAsync");
 }
 
-// FP64 sum of |x|^2: grid-stride partial sums, one atomic per block.
+// A square added to a float-float accumulator (fs, fc): x = h + l split exactly, x^2 =
+// h^2 (product and its exact FMA error) + 2 h l (the l^2 term, below 2^-48 of x^2, is left
+// out).
+__device__ __forceinline__ void ff_square_add(df::dwords w, float& fs, float& fc) {
+  const df::f2 a = df::split(w);
+  const float p = df::mul(a.h, a.h);
+  float e = df::fma(a.h, a.h, -p);
+  e = df::fma(df::add(a.h, a.h), a.l, e);
+  float t, err;
+  df::two_sum(fs, p, t, err);
+  fs = t;
+  fc = df::add(fc, df::add(err, e));
+}
+
+// Sum of |x|^2 to FP64 accuracy: grid-stride partial sums, one atomic per block. Of a
+// thread's four elements per step, two are squared with FP64 FMAs and two as exact
+// float-float squares (a warp with an element outside the float-float range takes FP64
+// for them), so that the FP64 unit does half of the work and the FP32 pipes the rest:
+// FP64 alone caps this read-only stream at about half of the HBM rate on GB300.
 __global__ void norm2_kernel(const double2* __restrict__ x, uint64_t n, double* __restrict__ acc) {
-  // four elements per thread per step, loads first, two independent accumulators
+  // four elements per thread per step, loads first, independent accumulators
   double s = 0.0, s2 = 0.0;
+  float fs = 0.0f, fc = 0.0f;
   const uint64_t step = (uint64_t)gridDim.x * blockDim.x * 4;
   for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x * 4 + threadIdx.x; b < n; b += step) {
     double2 v[4];
@@ -95,12 +115,23 @@ __global__ void norm2_kernel(const double2* __restrict__ x, uint64_t n, double* 
       v[u] = i < n ? x[i] : make_double2(0.0, 0.0);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
       s = fma(v[u].x, v[u].x, s);
       s2 = fma(v[u].y, v[u].y, s2);
     }
+#pragma unroll
+    for (int u = 2; u < 4; ++u) {
+      const df::dwords wx = df::words(v[u].x), wy = df::words(v[u].y);
+      if (__all_sync(__activemask(), df::in_range_state(wx) && df::in_range_state(wy))) {
+        ff_square_add(wx, fs, fc);
+        ff_square_add(wy, fs, fc);
+      } else {
+        s = fma(v[u].x, v[u].x, s);
+        s2 = fma(v[u].y, v[u].y, s2);
+      }
+    }
   }
-  s += s2;
+  s += s2 + ((double)fs + (double)fc);
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   __shared__ double ws[32];
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

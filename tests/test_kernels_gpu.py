@@ -269,9 +269,19 @@ def test_diagonal_in_place_and_layer(arith):
 
 
 def test_norm2():
+    # against the correctly rounded sum of the squares; half of the elements are squared
+    # in float-float, so also with amplitudes outside that range (FP64 there), zeros and
+    # a length that is not a multiple of the kernel's step
     nrng = np.random.default_rng(8)
-    a = crandn(nrng, [1 << 18])
-    assert abs(q.norm2(dev(a)) - np.vdot(a, a).real) < 1e-9 * np.vdot(a, a).real
+    for n, scale_blocks in ((1 << 18, False), ((1 << 18) + 77, True)):
+        a = crandn(nrng, [n])
+        if scale_blocks:
+            a[:4096] *= 1e-40
+            a[4096:8192] *= 1e40
+            a[8192:9000] = 0.0
+        sq = np.concatenate([a.real ** 2, a.imag ** 2])
+        ref = math.fsum(sq.tolist())
+        assert abs(q.norm2(dev(a)) - ref) < 1e-13 * ref
 
 
 def test_distributed_identity_moves_index():
