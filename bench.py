@@ -950,7 +950,7 @@ def main_kernels(a):
          lambda: q.apply_gate(x, dims, t4, gate4)),
         ("gate: four-qubit SymmTensor on (%d, %d, %d, %d)" % tuple(t4), "bf16x6", 32,
          lambda: q.apply_gate(x, dims, t4, gate4)),
-        ("norm: FP64 sum of squares", "fp64", 16, lambda: q.norm2(x)),
+        ("norm: sum of squares (FP64-accurate)", "bf16x6", 16, lambda: q.norm2(x)),
     ]
     old = q.get_arithmetic()
     out = {}
