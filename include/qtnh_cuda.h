@@ -242,7 +242,9 @@ int qtnh_apply_diag_layer(void* state, int32_t rank, const uint64_t* dims, int32
 
 /* ---- reductions (FP64) ------------------------------------------------------------- */
 
-/* sum |x|^2 over n elements, computed in FP64 on the device; result to host. Synchronous. */
+/* sum |x|^2 over n elements to FP64 accuracy on the device (half of the squares as FP64
+ * FMAs, half as exact float-float products, partial sums combined in FP64); result to
+ * host. Synchronous. */
 int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream);
 
 /* ---- grouped operations on many resident states (request loops) ---------------------- */
