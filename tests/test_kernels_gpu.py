@@ -268,6 +268,33 @@ def test_diagonal_in_place_and_layer(arith):
     assert rel_l2(host(st), cur.els) < REL_TOL
 
 
+def test_diagonals_default_mode_out_of_range(bf16x6):
+    # the default mode's diagonal kernels mix FP64 elements, float-float elements and the
+    # FP64 fallback of a warp whose float-float elements are out of range: tiny, huge,
+    # zero and subnormal regions, each compared on its own scale
+    nrng = np.random.default_rng(17)
+    n = 13
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    psi[:1024] *= 1e-200
+    psi[1024:2048] *= 1e200
+    psi[2048:2304] = 0.0
+    psi[2304] = 5e-324
+    regions = (slice(0, 1024), slice(1024, 2048), slice(2048, 1 << n))
+    d = np.exp(1j * nrng.uniform(0, 2 * np.pi, 4)) * np.array([1.0, 1e-40, 1.0, 3.0])
+    out, ref = _run_contract((q.DENSE, [], [2] * n, psi, 0), (q.DIAG, [], [2] * 4, d, 0), [(n - 1, 0), (3, 1)])
+    for sl in regions:
+        assert rel_l2(np.asarray(out).reshape(-1)[sl], np.asarray(ref).reshape(-1)[sl]) < REL_TOL
+    factors = np.stack([np.ones(n), np.exp(1j * nrng.uniform(0, 2 * np.pi, n))], axis=1).reshape(-1)
+    st = dev(psi)
+    q.apply_diag_layer(st, [2] * n, list(range(n)), dev(factors))
+    cur = orc.Tensor(orc.DENSE, [], [2] * n, psi)
+    for j in range(n):
+        cur, _, _ = orc.contract(cur, orc.Tensor(orc.DIAG, [], [2, 2], factors[2 * j:2 * j + 2]), [(j, 0)])
+    got = host(st)
+    for sl in regions:
+        assert rel_l2(got[sl], cur.els[sl]) < REL_TOL
+
+
 def test_norm2():
     # against the correctly rounded sum of the squares; half of the elements are squared
     # in float-float, so also with amplitudes outside that range (FP64 there), zeros and
