@@ -861,8 +861,8 @@ def main_kernels(a):
     """The plain path's data-movement and streaming kernels one by one on a 2^n-amplitude
     complex128 state (n = 28: 4 GiB, far beyond L2): permutes (rescatter-style index
     exchanges, a full reversal, Tensor::swap), DiagTensor contractions (the QFT's
-    controlled phase, a per-qubit phase layer), a two-qubit SymmTensor gate and the FP64
-    norm. Each case: 3 warm-up launches, then `steps` launches timed with CUDA events;
+    controlled phase, a per-qubit phase layer), one-, two- and four-qubit SymmTensor
+    gates in each arithmetic, and the FP64-accurate norm. Each case: 3 warm-up launches, then `steps` launches timed with CUDA events;
     algorithmic bytes are the state read and written once (32 B per amplitude; the norm
     reads it, 16 B)."""
     import numpy as np
