@@ -289,7 +289,7 @@ void check_circuit(qtnh_batch* b, int32_t c) {
 extern "C" {
 
 int qtnh_batch_create_typed(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubits, int32_t precision) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (!out || ncircuits <= 0 || !nqubits) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid batch arguments");
     if (precision != QTNH_STATE_C64 && precision != QTNH_STATE_C128)
       throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown state precision");
@@ -316,14 +316,14 @@ int qtnh_batch_create(qtnh_batch** out, int32_t ncircuits, const int32_t* nqubit
 }
 
 int qtnh_batch_destroy(qtnh_batch* b) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     delete b;
     return QTNH_OK;
   });
 }
 
 int qtnh_batch_set_state(qtnh_batch* b, int32_t c, const void* psi_c128, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
     const uint64_t n = 1ull << b->nq[c];
@@ -343,7 +343,7 @@ int qtnh_batch_set_state(qtnh_batch* b, int32_t c, const void* psi_c128, void* s
 }
 
 int qtnh_batch_add_gate(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb, const void* els_c128) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     check_circuit(b, c);
     if (layer < 0 || qa >= b->nq[c] || qb >= b->nq[c] || qa == qb || !els_c128)
@@ -367,7 +367,7 @@ int qtnh_batch_add_gate(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, ui
 }
 
 int qtnh_batch_add_phases(qtnh_batch* b, int32_t c, int32_t layer, const double* phases) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     check_circuit(b, c);
     if (layer < 0 || !phases) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid phase layer");
@@ -383,7 +383,7 @@ int qtnh_batch_add_phases(qtnh_batch* b, int32_t c, int32_t layer, const double*
 }
 
 int qtnh_batch_add_swap(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, uint16_t qb) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     check_circuit(b, c);
     if (layer < 0 || qa >= b->nq[c] || qb >= b->nq[c] || qa == qb) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid swap");
@@ -399,7 +399,7 @@ int qtnh_batch_add_swap(qtnh_batch* b, int32_t c, int32_t layer, uint16_t qa, ui
 }
 
 int qtnh_batch_add_queries(qtnh_batch* b, int32_t c, int32_t nq, const uint64_t* idx) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     check_circuit(b, c);
     if (nq < 0 || (nq && !idx)) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid queries");
@@ -412,7 +412,7 @@ int qtnh_batch_add_queries(qtnh_batch* b, int32_t c, int32_t nq, const uint64_t*
 }
 
 int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     if (b->exec) throw Error(QTNH_ERR_RUNTIME, "batch already compiled");
     const size_t nc = b->nq.size();
@@ -627,7 +627,7 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
 }
 
 int qtnh_batch_run(qtnh_batch* b, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     if (!b->exec) throw Error(QTNH_ERR_RUNTIME, "batch not compiled");
     // order against the caller's stream: caller -> batch stream -> caller
@@ -645,7 +645,7 @@ int qtnh_batch_run(qtnh_batch* b, void* stream) {
 }
 
 int qtnh_batch_results(qtnh_batch* b, void* out_c128, uint64_t capacity, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     if (capacity < b->queries.size()) throw Error(QTNH_ERR_CAPACITY, "result buffer too small");
     if (!b->queries.empty())
@@ -658,7 +658,7 @@ int qtnh_batch_results(qtnh_batch* b, void* out_c128, uint64_t capacity, void* s
 
 int qtnh_batch_info(qtnh_batch* b, uint64_t* amplitudes, uint64_t* rounds, uint64_t* launches_per_run,
                     int32_t* gate_threads, uint64_t* gate_chunk) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     if (amplitudes) *amplitudes = b->total_amps;
     if (rounds) *rounds = b->rounds.size();
@@ -672,7 +672,7 @@ int qtnh_batch_info(qtnh_batch* b, uint64_t* amplitudes, uint64_t* rounds, uint6
 }
 
 int qtnh_batch_state(qtnh_batch* b, int32_t c, void* out_c128, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     checked(b);
     if (c < 0 || (size_t)c >= b->nq.size()) throw Error(QTNH_ERR_OUT_OF_RANGE, "circuit index out of range");
     const uint64_t n = 1ull << b->nq[c];

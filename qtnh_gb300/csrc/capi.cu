@@ -100,7 +100,7 @@ extern "C" {
 int qtnh_contract_plan(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, int32_t nwires, const uint16_t* wires,
                        int32_t use_default, uint16_t* repls1, uint16_t* repls2, int32_t* out_ndis, int32_t* out_nloc,
                        uint64_t* out_dims, uint64_t* out_str) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     TensorMeta m1, m2;
     run_plan(t1, t2, nwires, wires, use_default, repls1, repls2, out_ndis, out_nloc, out_dims, out_str, m1, m2);
     return QTNH_OK;
@@ -110,7 +110,7 @@ int qtnh_contract_plan(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, i
 int qtnh_contract(const qtnh_tensor_desc* t1d, const qtnh_tensor_desc* t2d, int32_t nwires, const uint16_t* wires,
                   int32_t use_default, uint16_t* repls1, uint16_t* repls2, int32_t* out_ndis, int32_t* out_nloc,
                   uint64_t* out_dims, uint64_t* out_str, void* out, uint64_t out_capacity, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     TensorMeta t1, t2;
     ContractPlan p = run_plan(t1d, t2d, nwires, wires, use_default, repls1, repls2, out_ndis, out_nloc, out_dims,
                               out_str, t1, t2);

@@ -255,7 +255,7 @@ extern "C" {
 int qtnh_contract_dense(const void* a, int32_t rank_a, const uint64_t* dims_a, const void* b, int32_t rank_b,
                         const uint64_t* dims_b, int32_t nwires, const uint16_t* wires, const uint16_t* out_pos_a,
                         const uint16_t* out_pos_b, void* c, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank_a < 0 || rank_b < 0 || rank_a > QTNH_MAX_RANK || rank_b > QTNH_MAX_RANK || nwires < 0)
       throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     std::vector<Wire> ws(nwires);

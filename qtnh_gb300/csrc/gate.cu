@@ -589,7 +589,7 @@ extern "C" {
 
 int qtnh_apply_gate(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
                     const void* gate, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK || k < 0 || k > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     apply_gate_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(targets, targets + k), gate, stream);
     return QTNH_OK;
@@ -598,7 +598,7 @@ int qtnh_apply_gate(void* state, int32_t rank, const uint64_t* dims, int32_t k, 
 
 int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32_t ngates, const int32_t* gate_k,
                           const uint16_t* targets, const void* const* gates, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK || ngates < 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     dims_t d(dims, dims + rank);
     std::vector<std::vector<uint16_t>> tl((size_t)ngates);
@@ -619,7 +619,7 @@ int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32
 
 int qtnh_apply_diag(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
                     const void* diag, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK || k < 0 || k > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     apply_diag_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(targets, targets + k), diag, stream);
     return QTNH_OK;
@@ -628,7 +628,7 @@ int qtnh_apply_diag(void* state, int32_t rank, const uint64_t* dims, int32_t k, 
 
 int qtnh_apply_diag_layer(void* state, int32_t rank, const uint64_t* dims, int32_t nfactors, const uint16_t* axes,
                           const void* factors, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK || nfactors < 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     apply_diag_layer_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(axes, axes + nfactors), factors,
                             stream);

@@ -400,7 +400,7 @@ uint32_t take_umma_error() {
 using namespace qtnh_impl;
 
 extern "C" int qtnh_take_device_errors(uint32_t* flags) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (!flags) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null flags pointer");
     check_cuda(cudaDeviceSynchronize(), "device synchronize");
     *flags = take_umma_error() | (take_gemm_error() << 8);

@@ -576,7 +576,7 @@ uint32_t take_gemm_error() {
 using namespace qtnh_impl;
 
 extern "C" int qtnh_gemm_timing(int enable, double* ms, uint64_t* launches) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     double t = 0;
     uint64_t n = 0;
     take_gemm_times(t, n);

@@ -351,7 +351,7 @@ extern "C" {
 int qtnh_group_layer(int32_t precision, int32_t nstates, void* const* states, const int32_t* nqubits,
                      const int32_t* ngates, const uint16_t* pairs, const void* gates_c128, const uint8_t* has_phases,
                      const double* phases, const uint16_t* swaps, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_precision(precision);
     if (nstates < 0 || (nstates && (!states || !nqubits || !ngates))) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid group");
     for (int32_t i = 0; i < nstates; ++i)
@@ -368,7 +368,7 @@ int qtnh_group_layer(int32_t precision, int32_t nstates, void* const* states, co
 }
 
 int qtnh_group_renorm(int32_t precision, int32_t nstates, void* const* states, const int32_t* nqubits, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_precision(precision);
     if (nstates <= 0) return QTNH_OK;
     for (int32_t i = 0; i < nstates; ++i)
@@ -383,7 +383,7 @@ int qtnh_group_renorm(int32_t precision, int32_t nstates, void* const* states, c
 
 int qtnh_gather(int32_t precision, const void* state, int32_t nqubits, int32_t nidx, const uint64_t* idx,
                 void* out_c128, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_precision(precision);
     if (nidx <= 0) return QTNH_OK;
     for (int32_t i = 0; i < nidx; ++i)
@@ -407,7 +407,7 @@ int qtnh_gather(int32_t precision, const void* state, int32_t nqubits, int32_t n
 
 int qtnh_rdm4(int32_t precision, const void* state, int32_t nqubits, const uint16_t* qubits, void* out_c128,
               void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_precision(precision);
     if (nqubits < 4 || nqubits > 40 || !qubits) throw Error(QTNH_ERR_INVALID_ARGUMENT, "invalid reduced density matrix");
     uint32_t qb[4], sb[4];
@@ -437,7 +437,7 @@ int qtnh_rdm4(int32_t precision, const void* state, int32_t nqubits, const uint1
 }
 
 int qtnh_state_convert(int32_t to_precision, const void* in, void* out, uint64_t n, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_precision(to_precision);
     convert_kernel<float2><<<grid_for((n + 255) / 256, 4), 256, 0, (cudaStream_t)stream>>>(
         in, out, n, to_precision == QTNH_STATE_C64 ? 1 : 0);

@@ -1,10 +1,13 @@
 // Shared declarations of the engine's translation units (not installed).
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "qtnh_cuda.h"
@@ -30,6 +33,25 @@ int guarded(F&& f) {
     return status_from_current_exception();
   }
 }
+
+// An NVTX range named after a C ABI entry point for the length of the call, so that a
+// profiler shows every API operation around its kernels; without a profiler attached
+// the push and pop do nothing.
+struct ApiRange {
+  explicit ApiRange(const char* name) { nvtxRangePushA(name); }
+  ~ApiRange() { nvtxRangePop(); }
+  ApiRange(const ApiRange&) = delete;
+  ApiRange& operator=(const ApiRange&) = delete;
+};
+
+template <class F>
+int guarded_api(const char* name, F&& f) {
+  ApiRange range(name);
+  return guarded(std::forward<F>(f));
+}
+
+// Body of a C ABI entry point: exceptions become status codes, the call an NVTX range.
+#define QTNH_API(...) ::qtnh_impl::guarded_api(__func__, __VA_ARGS__)
 
 extern std::atomic<uint64_t> g_launches;
 int arithmetic_mode();  // QTNH_ARITH_*

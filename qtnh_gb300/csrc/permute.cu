@@ -612,7 +612,7 @@ using namespace qtnh_impl;
 extern "C" {
 
 int qtnh_permute(const void* in, void* out, int32_t rank, const uint64_t* dims, const uint16_t* ptup, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     permute_device(in, out, dims_t(dims, dims + rank), std::vector<uint16_t>(ptup, ptup + rank), stream);
     return QTNH_OK;
@@ -620,7 +620,7 @@ int qtnh_permute(const void* in, void* out, int32_t rank, const uint64_t* dims, 
 }
 
 int qtnh_swap(const void* in, void* out, int32_t rank, const uint64_t* dims, int32_t idx1, int32_t idx2, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     if (idx1 < 0 || idx2 < 0 || idx1 >= rank || idx2 >= rank) throw Error(QTNH_ERR_OUT_OF_RANGE, "swap index out of range");
     if (dims[idx1] != dims[idx2]) throw Error(QTNH_ERR_RUNTIME, "Asymmetric swaps are currently not allowed");

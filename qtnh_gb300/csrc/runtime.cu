@@ -165,7 +165,7 @@ int qtnh_abi_version(void) { return QTNH_ABI_VERSION; }
 uint64_t qtnh_kernel_launch_count(void) { return g_launches.load(); }
 
 int qtnh_set_arithmetic(int mode) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (mode != QTNH_ARITH_FP64 && mode != QTNH_ARITH_F32X2 && mode != QTNH_ARITH_BF16X6) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown arithmetic mode");
     g_arith.store(mode);
     return QTNH_OK;
@@ -175,7 +175,7 @@ int qtnh_set_arithmetic(int mode) {
 int qtnh_get_arithmetic(void) { return arithmetic_mode(); }
 
 int qtnh_set_gemm_precision(int mode) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (mode != QTNH_GEMM_FP64 && mode != QTNH_GEMM_BF16X3) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown GEMM precision");
     g_gemm.store(mode);
     return QTNH_OK;
@@ -185,7 +185,7 @@ int qtnh_set_gemm_precision(int mode) {
 int qtnh_get_gemm_precision(void) { return gemm_mode(); }
 
 int qtnh_device_count(int* count) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess) n = 0, cudaGetLastError();
@@ -195,14 +195,14 @@ int qtnh_device_count(int* count) {
 }
 
 int qtnh_set_device(int device) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_cuda(cudaSetDevice(device), "cudaSetDevice");
     return QTNH_OK;
   });
 }
 
 int qtnh_malloc(void** ptr, size_t bytes) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     *ptr = nullptr;
     if (bytes == 0) bytes = 16;
     check_cuda(cudaMalloc(ptr, bytes), "cudaMalloc");
@@ -211,56 +211,56 @@ int qtnh_malloc(void** ptr, size_t bytes) {
 }
 
 int qtnh_free(void* ptr) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (ptr) check_cuda(cudaFree(ptr), "cudaFree");
     return QTNH_OK;
   });
 }
 
 int qtnh_memcpy_h2d(void* dst, const void* src_host, size_t bytes, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (bytes) check_cuda(cudaMemcpyAsync(dst, src_host, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream), "h2d copy");
     return QTNH_OK;
   });
 }
 
 int qtnh_memcpy_d2h(void* dst_host, const void* src, size_t bytes, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (bytes) check_cuda(cudaMemcpyAsync(dst_host, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "d2h copy");
     return QTNH_OK;
   });
 }
 
 int qtnh_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (bytes) check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream), "d2d copy");
     return QTNH_OK;
   });
 }
 
 int qtnh_memset(void* dst, int value, size_t bytes, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (bytes) check_cuda(cudaMemsetAsync(dst, value, bytes, (cudaStream_t)stream), "memset");
     return QTNH_OK;
   });
 }
 
 int qtnh_stream_synchronize(void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "stream synchronize");
     return QTNH_OK;
   });
 }
 
 int qtnh_device_synchronize(void) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     check_cuda(cudaDeviceSynchronize(), "device synchronize");
     return QTNH_OK;
   });
 }
 
 int qtnh_stream_create(void** stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     cudaStream_t s = nullptr;
     check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
     *stream = (void*)s;
@@ -269,14 +269,14 @@ int qtnh_stream_create(void** stream) {
 }
 
 int qtnh_stream_destroy(void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (stream) check_cuda(cudaStreamDestroy((cudaStream_t)stream), "cudaStreamDestroy");
     return QTNH_OK;
   });
 }
 
 int qtnh_malloc_async(void** ptr, size_t bytes, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     *ptr = nullptr;
     if (bytes == 0) bytes = 16;
     check_cuda(cudaMallocAsync(ptr, bytes, (cudaStream_t)stream), "cudaMallocAsync");
@@ -285,14 +285,14 @@ int qtnh_malloc_async(void** ptr, size_t bytes, void* stream) {
 }
 
 int qtnh_free_async(void* ptr, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     if (ptr) check_cuda(cudaFreeAsync(ptr, (cudaStream_t)stream), "cudaFreeAsync");
     return QTNH_OK;
   });
 }
 
 int qtnh_norm2(const void* x, uint64_t n, double* result_host, void* stream) {
-  return guarded([&]() -> int {
+  return QTNH_API([&]() -> int {
     cudaStream_t s = (cudaStream_t)stream;
     double* acc = (double*)workspace_alloc(sizeof(double), stream);
     check_cuda(cudaMemsetAsync(acc, 0, sizeof(double), s), "memset");
