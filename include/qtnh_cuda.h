@@ -93,6 +93,11 @@ int qtnh_malloc_async(void** ptr, size_t bytes, void* stream);
 int qtnh_free_async(void* ptr, void* stream);
 /* Number of kernels this library has launched since load (all entry points). */
 uint64_t qtnh_kernel_launch_count(void);
+/* Allocation diagnostics (no counterpart in the reference): `allocations` = how many
+ * temporary device buffers (scratch) the entry points have taken from the stream-ordered
+ * pool since load; `pool_used_bytes` = the bytes in use in the current device's default
+ * memory pool now. */
+int qtnh_workspace_stats(uint64_t* allocations, uint64_t* pool_used_bytes);
 
 /* Device-side error flags of the kernels whose waits are bounded (the tcgen05 gate-pair
  * kernel: bit 0 = a wait for converted digits expired, bit 1 = a wait for MMA completion
@@ -195,7 +200,7 @@ int qtnh_contract_dense(const void* a, int32_t rank_a, const uint64_t* dims_a, c
                         const uint64_t* dims_b, int32_t nwires, const uint16_t* wires, const uint16_t* out_pos_a,
                         const uint16_t* out_pos_b, void* c, void* stream);
 
-/* Same contraction as qtnh_contract_dense, for callers that cannot allocate device
+/* The contraction of qtnh_contract_dense, for callers that cannot allocate device
  * memory while they run: hosts whose device memory is owned by their own allocator or
  * fixed budget, and latency-critical loops where a cudaMalloc would stall or fragment.
  * It has no counterpart in the reference (which contracts on host memory over MPI).
@@ -205,7 +210,11 @@ int qtnh_contract_dense(const void* a, int32_t rank_a, const uint64_t* dims_a, c
  * allocates nothing; contractions whose permuted copies need more elements than that
  * fail with QTNH_ERR_UNSUPPORTED before any work is issued. The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress, with that device current);
- * make that first call before any stream capture. Every call shares the one array and
+ * make that first call before any stream capture. A cudaDeviceReset invalidates the
+ * address looked up then, so the entry point is not for use after a cudaDeviceReset in
+ * the same process. The GEMM is always the plain FP64 one (the QTNH_GEMM_FP64 numerics),
+ * whatever qtnh_set_gemm_precision selects: the split-precision and digit GEMMs need
+ * operand planes that this path has no room for. Every call shares the one array and
  * it keeps the previous call's contents (nothing in it needs to start at zero): calls
  * that can overlap on the GPU, on different streams or threads, race on it and must be
  * serialised by the caller. */

@@ -76,10 +76,20 @@ __global__ void __launch_bounds__(GEMM_THREADS) zgemm_kernel(const c128* __restr
   }
 }
 
+}  // namespace
+
+// The FP64 GEMM's grid has one block row per 64 rows of C (grid y is at most 65535).
+void zgemm_check_shape(uint64_t M, uint64_t N) {
+  (void)N;
+  if ((M + BM - 1) / BM > 65535) throw Error(QTNH_ERR_UNSUPPORTED, "GEMM M dimension too large");
+}
+
+namespace {
+
 void zgemm(const c128* A, const c128* B, c128* C, uint64_t M, uint64_t N, uint64_t K, cudaStream_t s) {
   if (M == 0 || N == 0) return;
+  zgemm_check_shape(M, N);
   uint64_t gx = (N + BN - 1) / BN, gy = (M + BM - 1) / BM;
-  if (gy > 65535) throw Error(QTNH_ERR_UNSUPPORTED, "GEMM M dimension too large");
   zgemm_kernel<<<dim3((unsigned)gx, (unsigned)gy), GEMM_THREADS, 0, s>>>(A, B, C, M, N, K);
   count_launch();
   check_cuda(cudaGetLastError(), "zgemm_kernel launch");

@@ -22,6 +22,8 @@ namespace {
 
 // Device address of the scratch array for the current device, looked up once per device
 // with that device current (the host-side symbol is only a stand-in, not an address).
+// A cudaDeviceReset unloads the module, so the address cached here is stale afterwards:
+// the entry point is not for use after a cudaDeviceReset in the same process.
 c128* scratch_for_current_device() {
   static std::mutex mu;
   static std::vector<void*> ptrs;
@@ -45,8 +47,9 @@ bool identity(const std::vector<uint16_t>& p) {
 
 }  // namespace
 
-// Declared in contract.cu's translation unit; reused here.
+// Defined in contract.cu; reused here.
 void zgemm_launch(const c128* A, const c128* B, c128* C, uint64_t M, uint64_t N, uint64_t K, cudaStream_t s);
+void zgemm_check_shape(uint64_t M, uint64_t N);
 
 void contract_dense_noalloc_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
                                    const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,
@@ -86,6 +89,7 @@ void contract_dense_noalloc_device(const void* a, const dims_t& dims_a, const vo
   for (size_t x = 0; x < openA.size(); ++x) pC[x] = pos_a[openA[x]];
   for (size_t y = 0; y < openB.size(); ++y) pC[openA.size() + y] = pos_b[openB[y]];
 
+  zgemm_check_shape(M, N);  // refused before any work is queued
   const bool permA = !identity(pA), permB = !identity(pB), permC = !identity(pC);
   const uint64_t need = (permA ? M * K : 0) + (permB ? K * N : 0) + (permC ? M * N : 0);
   if (need > QTNH_NOALLOC_SCRATCH_ELEMS)

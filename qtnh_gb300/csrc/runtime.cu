@@ -72,8 +72,11 @@ void check_cuda(cudaError_t e, const char* what) {
   }
 }
 
+static std::atomic<uint64_t> g_workspace_allocs{0};
+
 void* workspace_alloc(size_t bytes, void* stream) {
   if (bytes == 0) return nullptr;
+  g_workspace_allocs.fetch_add(1, std::memory_order_relaxed);
   void* p = nullptr;
   check_cuda(cudaMallocAsync(&p, bytes, (cudaStream_t)stream), "cudaMallocAsync");
   return p;
@@ -271,6 +274,21 @@ int qtnh_stream_create(void** stream) {
 int qtnh_stream_destroy(void* stream) {
   return QTNH_API([&]() -> int {
     if (stream) check_cuda(cudaStreamDestroy((cudaStream_t)stream), "cudaStreamDestroy");
+    return QTNH_OK;
+  });
+}
+
+int qtnh_workspace_stats(uint64_t* allocations, uint64_t* pool_used_bytes) {
+  return QTNH_API([&]() -> int {
+    if (!allocations || !pool_used_bytes) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null output pointer");
+    *allocations = g_workspace_allocs.load(std::memory_order_relaxed);
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaMemPool_t pool;
+    check_cuda(cudaDeviceGetDefaultMemPool(&pool, dev), "cudaDeviceGetDefaultMemPool");
+    unsigned long long used = 0;  // the attribute is a 64-bit unsigned value
+    check_cuda(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used), "cudaMemPoolGetAttribute");
+    *pool_used_bytes = (uint64_t)used;
     return QTNH_OK;
   });
 }

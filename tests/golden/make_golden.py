@@ -133,7 +133,9 @@ def write_text_fixtures(here, rt, tn):
 
 
 def main(argv):
-    ref = argv[1] if len(argv) > 1 else os.environ.get("QTNH_REFERENCE", "/root/reference")
+    if len(argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference checkout>")
+    ref = argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(ref, "tests", "gen", "random-tensors.hpp"), encoding="utf-8") as f:
         rt = parse_random_tensors(f.read())

@@ -5,8 +5,10 @@ latency-critical loop). Its scratch is a fixed 16 MiB array inside the library.
 
 Checked through the C ABI against qtnh_contract_dense on two calls in a row (the
 second call reuses the scratch left by the first), within the contraction tolerance of
-the other GPU tests; an oversized contraction must be refused before any work.
-Runs alone in a fresh process as well as after the other tests."""
+the other GPU tests; across those calls the library takes no scratch buffer and the
+device's stream-ordered pool holds no more bytes than before (qtnh_workspace_stats);
+an oversized contraction must be refused before any work. Runs alone in a fresh process
+as well as after the other tests."""
 import ctypes
 
 import numpy as np
@@ -27,6 +29,12 @@ def _call(fn, a, da, b, db, wires, pos_a, pos_b, c):
               ctypes.c_void_p(c.data_ptr()), q._stream())
 
 
+def _stats():
+    allocs, used = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    q.check(q.lib().qtnh_workspace_stats(ctypes.byref(allocs), ctypes.byref(used)))
+    return allocs.value, used.value
+
+
 def _case(rng, da, db, wires, pos_a, pos_b):
     a = torch.from_numpy(rng.standard_normal(int(np.prod(da))) + 1j * rng.standard_normal(int(np.prod(da)))).cuda()
     b = torch.from_numpy(rng.standard_normal(int(np.prod(db))) + 1j * rng.standard_normal(int(np.prod(db)))).cuda()
@@ -40,8 +48,12 @@ def _case(rng, da, db, wires, pos_a, pos_b):
     ref = torch.empty(n_out, dtype=torch.complex128, device="cuda")
     out = torch.full((n_out,), complex(float("nan"), 0.0), dtype=torch.complex128, device="cuda")
     q.check(_call(q.lib().qtnh_contract_dense, a, da, b, db, wires, pos_a, pos_b, ref))
+    torch.cuda.synchronize()
+    before = _stats()
     q.check(_call(q.lib().qtnh_contract_dense_noalloc, a, da, b, db, wires, pos_a, pos_b, out))
     torch.cuda.synchronize()
+    after = _stats()
+    assert after == before, "the allocation-free path allocated: %s -> %s" % (before, after)
     r, o = ref.cpu().numpy(), out.cpu().numpy()
     return np.linalg.norm(o - r) / np.linalg.norm(r)
 
