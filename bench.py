@@ -168,6 +168,19 @@ class _Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def _device_state_errors(out, ref):
+    """Device tensors -> (relative L2, max |out - ref| / max |ref|, 1 - fidelity). The
+    infidelity 1 - |<ref|out>|^2 / (<ref|ref> <out|out>) is computed as the squared norm of
+    out's component orthogonal to ref over |out|^2, which keeps its digits far below 1e-16."""
+    import torch
+    d = out - ref
+    rel = (torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref)).item()
+    mx = (d.abs().max() / ref.abs().max()).item()
+    perp = out - (torch.vdot(ref, out) / torch.vdot(ref, ref)) * ref
+    infid = (torch.vdot(perp, perp).real / torch.vdot(out, out).real).item()
+    return rel, mx, infid
+
+
 def _cpu_sample(n, layers, seed, reps=1):
     """Oracle port on one core: seconds per gate-layer at n qubits over `layers` layers."""
     from oracle import oracle as orc
@@ -355,6 +368,30 @@ def main_contract(a):
     e1.record(stream)
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
+
+    # plain on the tensor cores (QTNH_GEMM_OZ6, the default): exact digit products,
+    # FP64-level results; timed over the same steps, errors against the FP64 FMA arm
+    q.set_gemm_precision(q.GEMM_OZ6)
+    q.take_device_errors()
+    step(out)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(a.steps):
+        step(out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    oz_ms = e0.elapsed_time(e1) / a.steps
+    oz_rels, oz_maxs = [], []
+    for (t1, t2, wires), (_, _, _, M, N, _) in zip(tens, pairs):
+        q.set_gemm_precision(q.GEMM_FP64)
+        q.contract(t1, t2, wires, out=ref[:M * N])
+        q.set_gemm_precision(q.GEMM_OZ6)
+        q.contract(t1, t2, wires, out=out[:M * N])
+        d = out[:M * N] - ref[:M * N]
+        oz_rels.append((torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref[:M * N])).item())
+        oz_maxs.append((d.abs().max() / ref[:M * N].abs().max()).item())
+    oz_errors = q.take_device_errors()
+
     q.set_gemm_precision(q.GEMM_BF16X3)
     q.take_device_errors()
     rels, maxs = [], []
@@ -461,6 +498,11 @@ def main_contract(a):
             "data": "synthetic (seeded dense pairs, complex Gaussian entries)", "config": _contract_config(a, pairs),
             "plain_fp64": {"tflops": flops / (plain_ms * 1e-3) / 1e12, "ms_per_step": plain_ms,
                            "speedup_of_split": (flops / (ms / a.steps * 1e-3)) / (flops / (plain_ms * 1e-3))},
+            "plain_oz6": {"tflops": flops / (oz_ms * 1e-3) / 1e12, "ms_per_step": oz_ms,
+                          "speedup_over_fp64_fma": plain_ms / oz_ms,
+                          "error_vs_fp64_fma": {"rel_l2_median": statistics.median(oz_rels), "rel_l2_max": max(oz_rels),
+                                                "max_abs_over_max_max": max(oz_maxs)},
+                          "device_errors": oz_errors},
             "error_vs_fp64": {"rel_l2_median": statistics.median(rels), "rel_l2_max": max(rels),
                               "max_abs_over_max_median": statistics.median(maxs), "max_abs_over_max_max": max(maxs)},
             "roofline": {"bound": "tensor", "kernel": "gemm_bf16x3_umma_kernel", "achieved": achieved, "peak": peak,
@@ -524,9 +566,12 @@ def _state_errors(got, ref):
     |<ref|got>|^2 / (|ref|^2 |got|^2) of a state against its FP64 reference."""
     import numpy as np
     nr, ng = np.vdot(ref, ref).real, np.vdot(got, got).real
+    # 1 - fidelity as |got_perp|^2 / |got|^2 (got_perp: got's component orthogonal to ref)
+    perp = got - (np.vdot(ref, got) / nr) * ref
+    infid = float(np.vdot(perp, perp).real / ng)
     return {"rel_l2": float(np.linalg.norm(got - ref) / np.sqrt(nr)),
             "max_abs": float(np.max(np.abs(got - ref)) / np.max(np.abs(ref))),
-            "fidelity": float(abs(np.vdot(ref, got)) ** 2 / (nr * ng))}
+            "fidelity": 1.0 - infid, "infidelity": infid}
 
 
 def _worst_state_errors(errs):
@@ -534,7 +579,7 @@ def _worst_state_errors(errs):
         return None
     return {"rel_l2_max": max(e["rel_l2"] for e in errs), "max_abs_max": max(e["max_abs"] for e in errs),
             "fidelity_min": min(e["fidelity"] for e in errs), "one_minus_fidelity_max":
-            max(1.0 - e["fidelity"] for e in errs)}
+            max(e["infidelity"] for e in errs)}
 
 
 def main_batch(a):
@@ -1196,8 +1241,10 @@ def main():
             res = dc.run(cur, oth)
             outs[m] = res.clone()
         q.set_arithmetic(q.ARITH_NAMES[a.arith])
-        diff = torch.linalg.vector_norm(outs[mode] - outs["fp64"]).item()
-        arith_check = {"circuit_rel_l2_%s_vs_fp64" % mode: diff / torch.linalg.vector_norm(outs["fp64"]).item(),
+        rel, mx, infid = _device_state_errors(outs[mode], outs["fp64"])
+        arith_check = {"circuit_rel_l2_%s_vs_fp64" % mode: rel,
+                       "circuit_max_abs_rel_%s_vs_fp64" % mode: mx,
+                       "circuit_infidelity_%s_vs_fp64" % mode: infid,
                        "gates": dc.gate_count, "qubits": a.n}
         del outs
 
@@ -1211,7 +1258,8 @@ def main():
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                          "traffic": _traffic(kernel, a.n), "alg_bytes_per_launch": alg_bytes,
-                         "launch_ms": gate_launch_ms, "time_share": share},
+                         "launch_ms": gate_launch_ms, "time_share": share,
+                         "layer_frac": value / world * 2 * 16 * N / (peak * 1e9)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
             "clocks": ck,

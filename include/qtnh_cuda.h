@@ -101,9 +101,9 @@ int qtnh_workspace_stats(uint64_t* allocations, uint64_t* pool_used_bytes);
 
 /* Device-side error flags of the kernels whose waits are bounded (the tcgen05 gate-pair
  * kernel: bit 0 = a wait for converted digits expired, bit 1 = a wait for MMA completion
- * expired, bit 2 = a wait for the other half of a group expired; the tcgen05 GEMM:
- * bits 8-10 = a producer / MMA / epilogue wait expired; the kernel then stops early and
- * its output is incomplete). Synchronizes the device, returns the flags raised since the
+ * expired, bit 2 = a wait for the other half of a group expired; the tcgen05 GEMMs:
+ * bits 8-10 (split precision) and 16-18 (QTNH_GEMM_OZ6) = a producer / MMA / epilogue
+ * wait expired; the kernel then stops early and its output is incomplete). Synchronizes the device, returns the flags raised since the
  * previous call and clears them. */
 int qtnh_take_device_errors(uint32_t* flags);
 
@@ -133,14 +133,23 @@ int qtnh_get_arithmetic(void);
 
 /* Precision of the complex GEMM inside dense contractions (_contract_dense,
  * src/tensor/contract.cpp:12-201).
- * QTNH_GEMM_FP64 (default): complex128 FP64 fused multiply-adds, the plain method
- *   (reproduces the reference within 1e-12 relative L2).
+ * QTNH_GEMM_OZ6 (default): the plain method on the tcgen05 tensor cores. Every real of a
+ *   row of A (column of B) is cut into six error-free balanced 8-bit digits at the row's
+ *   (column's) largest exponent, the 21 digit-pair products of levels 0..5 are summed
+ *   exactly in FP32 over chunks of 128 reals of K, and the chunks are accumulated exactly
+ *   in 64-bit integers (levels 0-3) and FP32 (levels 4-5, below 2^-32): each result is
+ *   accurate to ~2^-48 of its row's and column's largest products, whatever K (reproduces
+ *   the reference within 1e-12 relative L2). Rows or columns holding an infinity or NaN
+ *   are recomputed in FP64. GEMMs below 2^18 complex multiply-adds or with a contracted
+ *   size below 16, and contractions with a SwapTensor or IdenTensor operand, run as
+ *   QTNH_GEMM_FP64 (which keeps relabellings by 0/1 tensors bit-exact).
+ * QTNH_GEMM_FP64: complex128 FP64 fused multiply-adds on the FP64 pipe.
  * QTNH_GEMM_BF16X3: split precision on the tcgen05 tensor cores: every real split into
  *   three bf16 pieces (24 bits), the six piece products with i + j <= 2 accumulated in
  *   FP32 on the tensor cores; FP32-level error (~1e-6 relative L2 at K ~ 100, growing
  *   with K; report it against QTNH_GEMM_FP64).
- * The environment variable QTNH_GEMM=fp64|bf16x3 sets the initial mode. Process-wide. */
-enum { QTNH_GEMM_FP64 = 0, QTNH_GEMM_BF16X3 = 1 };
+ * The environment variable QTNH_GEMM=oz6|fp64|bf16x3 sets the initial mode. Process-wide. */
+enum { QTNH_GEMM_FP64 = 0, QTNH_GEMM_BF16X3 = 1, QTNH_GEMM_OZ6 = 2 };
 int qtnh_set_gemm_precision(int mode);
 int qtnh_get_gemm_precision(void);
 
@@ -176,6 +185,17 @@ int qtnh_swap(const void* in, void* out, int32_t rank, const uint64_t* dims, int
 int qtnh_contract_plan(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, int32_t nwires,
                        const uint16_t* wires, int32_t use_default, uint16_t* repls1, uint16_t* repls2,
                        int32_t* out_ndis, int32_t* out_nloc, uint64_t* out_dims, uint64_t* out_str);
+
+/* Host-only companion of qtnh_contract: plans as qtnh_contract_plan (same outputs) and
+ * reports whether qtnh_contract would apply t2 in place to t1 -- a SymmTensor gate or a
+ * DiagTensor whose inputs are exactly the wired indices, with the in-place rule of
+ * contract.cpp:250-289 -- and, if so (*inplace = 1), t1's indices wired to t2's inputs in
+ * input order (*ntargets entries of `targets`, which must hold QTNH_MAX_RANK). The C++
+ * API uses it to queue such contractions and apply runs of them as fused layers. */
+int qtnh_contract_inplace(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, int32_t nwires,
+                          const uint16_t* wires, int32_t use_default, uint16_t* repls1, uint16_t* repls2,
+                          int32_t* out_ndis, int32_t* out_nloc, uint64_t* out_dims, uint64_t* out_str,
+                          int32_t* inplace, int32_t* ntargets, uint16_t* targets);
 
 /* ---- contraction ------------------------------------------------------------------- */
 

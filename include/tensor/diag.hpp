@@ -86,6 +86,7 @@ namespace qtnh {
 
       virtual DiagTensor* toDiag() noexcept override { return this; }
       virtual DiagTensor* rebcast(BcParams params) override;
+      virtual detail::DeviceArray releaseStorage() override { return std::move(diag_); }
       bool diag_index(const qtnh::tidx_tup& tot_idxs, std::size_t& i) const;
 
       detail::DeviceArray diag_;

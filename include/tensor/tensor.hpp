@@ -9,6 +9,7 @@
 #ifndef QTNH_TENSOR_TENSOR_HPP
 #define QTNH_TENSOR_TENSOR_HPP
 
+#include <cstdint>
 #include <memory>
 #include <vector>
 
@@ -48,6 +49,15 @@ namespace qtnh {
         std::vector<qtnh::tel> to_host() const;
         DeviceArray clone() const;
         const QTNHEnv* env() const noexcept { return env_; }
+        /// Queues an in-place application of `op` (a SymmTensor gate, kind QTNH_KIND_SYMM, or
+        /// a DiagTensor diagonal, QTNH_KIND_DIAG) to these elements, with dims the tensor's
+        /// total dims and targets its indices wired to op's inputs. Queued applications
+        /// run, in order and fused into as few passes as their targets allow, before the
+        /// elements are next read, written, copied or fetched.
+        void defer(int kind, const std::vector<std::uint16_t>& targets, const std::vector<std::uint64_t>& dims,
+                   DeviceArray&& op);
+        /// Runs the queued applications now (on the environment's stream).
+        void settle() const;
 
       private:
         void flush() const;

@@ -254,11 +254,12 @@ def get_arithmetic():
     return int(lib().qtnh_get_arithmetic())
 
 
-GEMM_FP64, GEMM_BF16X3 = 0, 1
+GEMM_FP64, GEMM_BF16X3, GEMM_OZ6 = 0, 1, 2
 
 
 def set_gemm_precision(mode):
-    """QTNH_GEMM_FP64 (0, plain) or QTNH_GEMM_BF16X3 (1, split precision on tcgen05)."""
+    """QTNH_GEMM_OZ6 (2, default: FP64-accurate digit products on tcgen05), QTNH_GEMM_FP64
+    (0, FP64 fused multiply-adds) or QTNH_GEMM_BF16X3 (1, split precision on tcgen05)."""
     check(lib().qtnh_set_gemm_precision(ctypes.c_int(mode)))
 
 

@@ -4,9 +4,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <mutex>
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 
 #include "qtnh.hpp"
 #include "qtnh_cuda.h"
@@ -30,6 +32,137 @@ void check(int rc) {
 // Host mirrors above this size are dropped after upload (re-read on demand).
 static const std::size_t kKeepMirrorElems = (std::size_t)16 << 20;
 
+// ---- in-place contractions queued on a tensor's elements ----------------------------
+//
+// Tensor::contract(state, gate, wires) with a SymmTensor gate or DiagTensor applied in
+// place (the in-place rule, src/tensor/contract.cpp:250-289) is queued on the state's
+// device array instead of running at once. The queue is applied when the elements are
+// next needed: runs of gates through qtnh_apply_gate_layer (consecutive disjoint two-qubit
+// gates share one pass over the state), runs of one-index diagonals through
+// qtnh_apply_diag_layer (one pass), other diagonals one by one. The queue is keyed by the
+// device pointer, which moves with the array. QTNH_LAZY=0 turns queuing off.
+
+struct DeferredOp {
+  int kind;
+  std::vector<uint16_t> targets;
+  DeviceArray op;
+};
+
+struct DeferredQueue {
+  const QTNHEnv* env = nullptr;
+  std::vector<uint64_t> dims;
+  std::vector<DeferredOp> ops;
+};
+
+static std::mutex g_deferred_mu;
+static std::unordered_map<const void*, DeferredQueue>& deferred_queues() {
+  static std::unordered_map<const void*, DeferredQueue> q;
+  return q;
+}
+static const std::size_t kMaxDeferred = 1024;  // applied once this many are queued
+
+static void drop_queue(const void* dev) {
+  if (!dev) return;
+  DeferredQueue dead;
+  {
+    std::lock_guard<std::mutex> lk(g_deferred_mu);
+    auto it = deferred_queues().find(dev);
+    if (it == deferred_queues().end()) return;
+    dead = std::move(it->second);
+    deferred_queues().erase(it);
+  }
+}
+
+static void apply_queue(void* dev, DeferredQueue& q) {
+  const int32_t rank = (int32_t)q.dims.size();
+  void* st = q.env->stream;
+  std::size_t i = 0;
+  while (i < q.ops.size()) {
+    std::size_t j = i;
+    if (q.ops[i].kind == QTNH_KIND_SYMM) {
+      while (j < q.ops.size() && q.ops[j].kind == QTNH_KIND_SYMM) ++j;
+      std::vector<int32_t> ks;
+      std::vector<uint16_t> tg;
+      std::vector<const void*> ptrs;
+      for (std::size_t g = i; g < j; ++g) {
+        ks.push_back((int32_t)q.ops[g].targets.size());
+        tg.insert(tg.end(), q.ops[g].targets.begin(), q.ops[g].targets.end());
+        ptrs.push_back(q.ops[g].op.read());
+      }
+      check(qtnh_apply_gate_layer(dev, rank, q.dims.data(), (int32_t)ks.size(), ks.data(), tg.data(), ptrs.data(), st));
+    } else if (q.ops[i].targets.size() == 1) {
+      while (j < q.ops.size() && q.ops[j].kind == QTNH_KIND_DIAG && q.ops[j].targets.size() == 1) ++j;
+      if (j - i == 1) {
+        check(qtnh_apply_diag(dev, rank, q.dims.data(), 1, q.ops[i].targets.data(), q.ops[i].op.read(), st));
+      } else {
+        // the one-index diagonals of the run, concatenated for one streaming pass
+        std::vector<uint16_t> axes;
+        std::size_t total = 0;
+        for (std::size_t g = i; g < j; ++g) axes.push_back(q.ops[g].targets[0]), total += q.dims[q.ops[g].targets[0]];
+        DeviceArray factors(*q.env, total);
+        char* f = static_cast<char*>(factors.write());
+        std::size_t off = 0;
+        for (std::size_t g = i; g < j; ++g) {
+          const std::size_t n = q.dims[q.ops[g].targets[0]];
+          check(qtnh_memcpy_d2d(f + off * sizeof(tel), q.ops[g].op.read(), n * sizeof(tel), st));
+          off += n;
+        }
+        check(qtnh_apply_diag_layer(dev, rank, q.dims.data(), (int32_t)axes.size(), axes.data(), factors.read(), st));
+      }
+    } else {
+      ++j;
+      check(qtnh_apply_diag(dev, rank, q.dims.data(), (int32_t)q.ops[i].targets.size(), q.ops[i].targets.data(),
+                            q.ops[i].op.read(), st));
+    }
+    i = j;
+  }
+}
+
+void DeviceArray::settle() const {
+  if (!dev_) return;
+  DeferredQueue q;
+  {
+    std::lock_guard<std::mutex> lk(g_deferred_mu);
+    auto it = deferred_queues().find(dev_);
+    if (it == deferred_queues().end()) return;
+    q = std::move(it->second);
+    deferred_queues().erase(it);
+  }
+  apply_queue(dev_, q);  // the operands are freed (stream-ordered) after their kernels
+}
+
+static bool lazy_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("QTNH_LAZY");
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
+void DeviceArray::defer(int kind, const std::vector<uint16_t>& targets, const std::vector<uint64_t>& dims,
+                        DeviceArray&& op) {
+  if (!dev_) throw std::runtime_error("tensor has no storage");
+  flush();  // host edits made so far come first
+  host_valid_ = false;
+  host_.clear();
+  host_.shrink_to_fit();
+  op.flush();
+  std::size_t queued = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_deferred_mu);
+    DeferredQueue& q = deferred_queues()[dev_];
+    if (q.ops.empty()) {
+      q.env = env_;
+      q.dims = dims;
+    } else if (q.dims != dims) {
+      throw std::logic_error("queued contractions on differently shaped elements");
+    }
+    q.ops.push_back(DeferredOp{kind, targets, std::move(op)});
+    queued = q.ops.size();
+  }
+  if (queued >= kMaxDeferred || !lazy_enabled()) settle();
+}
+
 DeviceArray::DeviceArray(const QTNHEnv& env, std::vector<tel>&& host) : env_(&env), n_(host.size()) {
   check(qtnh_malloc_async(&dev_, std::max<std::size_t>(n_, 1) * sizeof(tel), env.stream));
   if (n_) check(qtnh_memcpy_h2d(dev_, host.data(), n_ * sizeof(tel), env.stream));
@@ -44,6 +177,7 @@ DeviceArray::DeviceArray(const QTNHEnv& env, std::size_t n) : env_(&env), n_(n) 
 }
 
 DeviceArray::~DeviceArray() {
+  drop_queue(dev_);
   if (dev_) qtnh_free_async(dev_, env_->stream);
 }
 
@@ -57,6 +191,7 @@ DeviceArray::DeviceArray(DeviceArray&& o) noexcept
 
 DeviceArray& DeviceArray::operator=(DeviceArray&& o) noexcept {
   if (this != &o) {
+    drop_queue(dev_);
     if (dev_) qtnh_free_async(dev_, env_->stream);
     env_ = o.env_;
     dev_ = o.dev_;
@@ -80,6 +215,7 @@ void DeviceArray::flush() const {
 }
 
 void DeviceArray::pull() const {
+  settle();
   if (host_valid_) return;
   if (!dev_) throw std::runtime_error("tensor has no storage");
   host_.resize(n_);
@@ -89,11 +225,13 @@ void DeviceArray::pull() const {
 }
 
 const void* DeviceArray::read() const {
+  settle();
   flush();
   return dev_;
 }
 
 void* DeviceArray::write() {
+  settle();
   flush();
   host_valid_ = false;
   host_.clear();
@@ -120,6 +258,7 @@ std::vector<tel> DeviceArray::to_host() const {
 
 DeviceArray DeviceArray::clone() const {
   DeviceArray c(*env_, n_);
+  settle();
   flush();
   if (n_) check(qtnh_memcpy_d2d(c.dev_, dev_, n_ * sizeof(tel), env_->stream));
   if (host_valid_ && !host_dirty_) {

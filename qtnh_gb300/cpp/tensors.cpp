@@ -451,14 +451,20 @@ IdenTensor* IdenTensor::rebcast(BcParams params) {
 // DenseTensor like the reference's (contract.cpp:200) with broadcast
 // {product of contracted distributed dims, 1, min(off)}. When the result has the size of
 // the first tensor its device buffer is reused (the first tensor is consumed).
+//
+// A SymmTensor gate or DiagTensor applied in place to a DenseTensor (qtnh_contract_inplace)
+// is not run at once: it is queued on the state's device array (DeviceArray::defer), which
+// applies queued runs as fused layers before the elements are next used. The metadata
+// (dimension replacements, result dims, broadcaster) is the same either way.
 tptr contract_on_device(tptr tp1, tptr tp2, ConParams& params) {
   const QTNHEnv& env = tp1->bc().env;
   const tidx_tup d1 = tp1->totDims(), d2 = tp2->totDims();
   auto u1 = u64(d1), u2 = u64(d2);
+  // metadata first (host only): the element pointers are taken only when the work runs now
   qtnh_tensor_desc a{tp1->engineKind(), (int32_t)tp1->disDims().size(), (int32_t)tp1->locDims().size(),
-                     tp1->engineDisIn(), u1.data(), tp1->engineData()};
+                     tp1->engineDisIn(), u1.data(), nullptr};
   qtnh_tensor_desc b{tp2->engineKind(), (int32_t)tp2->disDims().size(), (int32_t)tp2->locDims().size(),
-                     tp2->engineDisIn(), u2.data(), tp2->engineData()};
+                     tp2->engineDisIn(), u2.data(), nullptr};
   std::vector<uint16_t> w;
   for (auto& x : params.wires) w.push_back(x.first), w.push_back(x.second);
   std::vector<uint16_t> r1(d1.size(), X), r2(d2.size(), X);
@@ -468,13 +474,30 @@ tptr contract_on_device(tptr tp1, tptr tp2, ConParams& params) {
     std::copy(params.dimRepls1.begin(), params.dimRepls1.end(), r1.begin());
     std::copy(params.dimRepls2.begin(), params.dimRepls2.end(), r2.begin());
   }
-  int32_t ndis = 0, nloc = 0;
+  int32_t ndis = 0, nloc = 0, inplace = 0, ntg = 0;
   uint64_t str = 1;
   std::vector<uint64_t> od(d1.size() + d2.size() + 1);
-  check(qtnh_contract_plan(&a, &b, (int32_t)params.wires.size(), w.data(), params.useDefRepls ? 1 : 0, r1.data(), r2.data(),
-                           &ndis, &nloc, od.data(), &str));
+  std::vector<uint16_t> targets(QTNH_MAX_RANK);
+  check(qtnh_contract_inplace(&a, &b, (int32_t)params.wires.size(), w.data(), params.useDefRepls ? 1 : 0, r1.data(),
+                              r2.data(), &ndis, &nloc, od.data(), &str, &inplace, &ntg, targets.data()));
   std::size_t nout = 1;
   for (int32_t i = 0; i < ndis + nloc; ++i) nout *= od[i];
+  BcParams bp((qtnh::uint)str, 1, std::min(tp1->bc().off, tp2->bc().off));
+  tidx_tup dis(od.begin(), od.begin() + ndis), loc(od.begin() + ndis, od.begin() + ndis + nloc);
+
+  if (inplace && a.kind == QTNH_KIND_DENSE && nout == tp1->totSize()) {
+    DeviceArray st = tp1->releaseStorage();
+    DeviceArray op = tp2->releaseStorage();
+    if (!st.empty() && !op.empty()) {
+      st.defer(b.kind, std::vector<uint16_t>(targets.begin(), targets.begin() + ntg), u1, std::move(op));
+      params.dimRepls1.assign(r1.begin(), r1.end());
+      params.dimRepls2.assign(r2.begin(), r2.end());
+      return tptr(new DenseTensor(env, dis, loc, std::move(st), bp));
+    }
+    throw std::logic_error("in-place contraction without element storage");
+  }
+  a.data = tp1->engineData();
+  b.data = tp2->engineData();
 
   DeviceArray out;
   if (nout == tp1->totSize() && (a.kind == QTNH_KIND_DENSE || a.kind == QTNH_KIND_SYMM)) out = tp1->releaseStorage();
@@ -483,8 +506,6 @@ tptr contract_on_device(tptr tp1, tptr tp2, ConParams& params) {
                       out.write(), nout, env.stream));
   params.dimRepls1.assign(r1.begin(), r1.end());
   params.dimRepls2.assign(r2.begin(), r2.end());
-  tidx_tup dis(od.begin(), od.begin() + ndis), loc(od.begin() + ndis, od.begin() + ndis + nloc);
-  BcParams bp((qtnh::uint)str, 1, std::min(tp1->bc().off, tp2->bc().off));
   return tptr(new DenseTensor(env, dis, loc, std::move(out), bp));
 }
 

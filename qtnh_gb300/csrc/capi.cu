@@ -69,6 +69,18 @@ bool inplace_targets(const ContractPlan& p, const TensorMeta& t1, const TensorMe
   return true;
 }
 
+// Case 1 in full: the kinds, the in-place rule and the sizes the in-place kernels take.
+bool inplace_dispatch(const ContractPlan& p, const TensorMeta& t1, const TensorMeta& t2, std::vector<uint16_t>& targets) {
+  if (!((t2.kind == QTNH_KIND_SYMM || t2.kind == QTNH_KIND_DIAG) &&
+        (t1.kind == QTNH_KIND_DENSE || t1.kind == QTNH_KIND_SYMM) && inplace_targets(p, t1, t2, targets)))
+    return false;
+  const dims_t d1 = t1.tot();
+  uint64_t D = 1;
+  for (auto t : targets) D *= d1[t];
+  return (t2.kind == QTNH_KIND_DIAG) ? targets.size() <= 8
+                                      : (D == 1 || D == 2 || D == 3 || D == 4 || D == 8 || D == 9 || D == 16);
+}
+
 // Case 2: delta tensors. Partner of index i: Swap (0<->3, 1<->2); Iden (i <-> i +- m).
 bool relabel_ptup(const ContractPlan& p, const TensorMeta& t1, const TensorMeta& t2, std::vector<uint16_t>& ptup) {
   if (t2.kind != QTNH_KIND_SWAP && t2.kind != QTNH_KIND_IDEN) return false;
@@ -107,6 +119,23 @@ int qtnh_contract_plan(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, i
   });
 }
 
+int qtnh_contract_inplace(const qtnh_tensor_desc* t1, const qtnh_tensor_desc* t2, int32_t nwires, const uint16_t* wires,
+                          int32_t use_default, uint16_t* repls1, uint16_t* repls2, int32_t* out_ndis, int32_t* out_nloc,
+                          uint64_t* out_dims, uint64_t* out_str, int32_t* inplace, int32_t* ntargets, uint16_t* targets) {
+  return QTNH_API([&]() -> int {
+    if (!inplace || !ntargets || !targets) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null output pointer");
+    TensorMeta m1, m2;
+    ContractPlan p = run_plan(t1, t2, nwires, wires, use_default, repls1, repls2, out_ndis, out_nloc, out_dims, out_str,
+                              m1, m2);
+    std::vector<uint16_t> tg;
+    const bool yes = inplace_dispatch(p, m1, m2, tg);
+    *inplace = yes ? 1 : 0;
+    *ntargets = yes ? (int32_t)tg.size() : 0;
+    if (yes) std::copy(tg.begin(), tg.end(), targets);
+    return QTNH_OK;
+  });
+}
+
 int qtnh_contract(const qtnh_tensor_desc* t1d, const qtnh_tensor_desc* t2d, int32_t nwires, const uint16_t* wires,
                   int32_t use_default, uint16_t* repls1, uint16_t* repls2, int32_t* out_ndis, int32_t* out_nloc,
                   uint64_t* out_dims, uint64_t* out_str, void* out, uint64_t out_capacity, void* stream) {
@@ -125,17 +154,11 @@ int qtnh_contract(const qtnh_tensor_desc* t1d, const qtnh_tensor_desc* t2d, int3
 
     // 1. in-place gate / diagonal
     std::vector<uint16_t> targets;
-    if ((t2.kind == QTNH_KIND_SYMM || t2.kind == QTNH_KIND_DIAG) && (t1.kind == QTNH_KIND_DENSE || t1.kind == QTNH_KIND_SYMM) &&
-        inplace_targets(p, t1, t2, targets)) {
-      uint64_t D = 1;
-      for (auto t : targets) D *= d1[t];
-      bool ok = (t2.kind == QTNH_KIND_DIAG) ? targets.size() <= 8 : (D == 1 || D == 2 || D == 3 || D == 4 || D == 8 || D == 9 || D == 16);
-      if (ok) {
-        if (out != t1d->data) check_cuda(cudaMemcpyAsync(out, t1d->data, n1 * sizeof(c128), cudaMemcpyDeviceToDevice, s), "copy");
-        if (t2.kind == QTNH_KIND_SYMM) apply_gate_device(out, d1, targets, t2d->data, stream);
-        else apply_diag_device(out, d1, targets, t2d->data, stream);
-        return QTNH_OK;
-      }
+    if (inplace_dispatch(p, t1, t2, targets)) {
+      if (out != t1d->data) check_cuda(cudaMemcpyAsync(out, t1d->data, n1 * sizeof(c128), cudaMemcpyDeviceToDevice, s), "copy");
+      if (t2.kind == QTNH_KIND_SYMM) apply_gate_device(out, d1, targets, t2d->data, stream);
+      else apply_diag_device(out, d1, targets, t2d->data, stream);
+      return QTNH_OK;
     }
 
     // 2. delta tensors relabel indices
@@ -179,7 +202,11 @@ int qtnh_contract(const qtnh_tensor_desc* t1d, const qtnh_tensor_desc* t2d, int3
       }
       void* c = out;
       if (out == t1d->data || out == t2d->data) c = c_tmp = workspace_alloc(nout * sizeof(c128), stream);
-      contract_dense_device(a, d1, b, d2, p.wires, p.repls1, p.repls2, c, stream);
+      // a SwapTensor or IdenTensor operand holds only 0/1 weights with one nonzero term per
+      // output: the FP64 FMA GEMM reproduces such relabellings bit-exactly, whatever the mode
+      const bool delta = t1.kind == QTNH_KIND_SWAP || t1.kind == QTNH_KIND_IDEN || t2.kind == QTNH_KIND_SWAP ||
+                         t2.kind == QTNH_KIND_IDEN;
+      contract_dense_device(a, d1, b, d2, p.wires, p.repls1, p.repls2, c, stream, delta ? QTNH_GEMM_FP64 : -1);
       if (c_tmp) check_cuda(cudaMemcpyAsync(out, c_tmp, nout * sizeof(c128), cudaMemcpyDeviceToDevice, s), "copy");
     } catch (...) {
       workspace_free(a_tmp, stream);

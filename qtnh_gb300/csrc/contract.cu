@@ -143,6 +143,16 @@ bool is_identity(const std::vector<uint16_t>& p) {
 
 }  // namespace
 
+// Whether the default plain GEMM runs on the tensor cores (gemm_oz.cu): from 2^18 complex
+// multiply-adds and a contracted size of 16 on. Below that the digit preparation costs
+// more than FP64 FMAs, and the FMA GEMM keeps the small-K contractions of relabelling
+// tensors (0/1 entries, one term per output, e.g. a SwapTensor wrapped in identity tensors)
+// bit-exact.
+bool oz6_applies(uint64_t M, uint64_t N, uint64_t K) {
+  const double work = (double)M * (double)N * (double)K;
+  return work >= 262144.0 && K >= 16;
+}
+
 // GEMM launcher shared with the allocation-free contraction (noalloc.cu).
 void zgemm_launch(const c128* A, const c128* B, c128* C, uint64_t M, uint64_t N, uint64_t K, cudaStream_t s) {
   zgemm(A, B, C, M, N, K, s);
@@ -172,7 +182,8 @@ void materialise_device(const TensorMeta& t, const void* data, void* out, void* 
 
 void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
                            const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,
-                           const std::vector<uint16_t>& pos_b, void* c, void* stream) {
+                           const std::vector<uint16_t>& pos_b, void* c, void* stream, int gemm) {
+  if (gemm < 0) gemm = gemm_mode();
   const size_t ra = dims_a.size(), rb = dims_b.size();
   std::vector<char> wa(ra, 0), wb(rb, 0);
   for (auto& w : wires) {
@@ -214,7 +225,37 @@ void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, c
   c128* Ap = nullptr;
   c128* Bp = nullptr;
   c128* Cp = nullptr;
-  if (gemm_mode() == QTNH_GEMM_BF16X3) {
+  if (gemm == QTNH_GEMM_OZ6 && oz6_applies(M, N, K)) {
+    // FP64-accurate digit products on the tensor cores: A permuted to [open A | wired]
+    // (M x K), B to [open B | wired] (N x K), the contracted index innermost in both
+    std::vector<uint16_t> pBt(rb);
+    for (size_t y = 0; y < openB.size(); ++y) pBt[openB[y]] = (uint16_t)y;
+    for (size_t j = 0; j < wires.size(); ++j) pBt[wires[j].second] = (uint16_t)(openB.size() + j);
+    const bool direct = is_identity(pC);
+    try {
+      if (!is_identity(pA)) {
+        Ap = static_cast<c128*>(workspace_alloc(M * K * sizeof(c128), stream));
+        permute_device(A, Ap, dims_a, pA, stream);
+      }
+      if (!is_identity(pBt)) {
+        Bp = static_cast<c128*>(workspace_alloc(K * N * sizeof(c128), stream));
+        permute_device(B, Bp, dims_b, pBt, stream);
+      }
+      if (!direct) Cp = static_cast<c128*>(workspace_alloc(M * N * sizeof(c128), stream));
+      gemm_oz6(Ap ? Ap : A, Bp ? Bp : B, direct ? static_cast<c128*>(c) : Cp, M, N, K, stream);
+      if (!direct) permute_device(Cp, c, dC, pC, stream);
+    } catch (...) {
+      workspace_free(Ap, stream);
+      workspace_free(Bp, stream);
+      workspace_free(Cp, stream);
+      throw;
+    }
+    workspace_free(Ap, stream);
+    workspace_free(Bp, stream);
+    workspace_free(Cp, stream);
+    return;
+  }
+  if (gemm == QTNH_GEMM_BF16X3) {
     // split precision: the operand permutes are fused into the piece splits
     std::vector<uint16_t> pBt(rb);
     for (size_t y = 0; y < openB.size(); ++y) pBt[openB[y]] = (uint16_t)y;

@@ -403,7 +403,7 @@ extern "C" int qtnh_take_device_errors(uint32_t* flags) {
   return QTNH_API([&]() -> int {
     if (!flags) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null flags pointer");
     check_cuda(cudaDeviceSynchronize(), "device synchronize");
-    *flags = take_umma_error() | (take_gemm_error() << 8);
+    *flags = take_umma_error() | (take_gemm_error() << 8) | (take_ozg_error() << 16);
     return QTNH_OK;
   });
 }

@@ -133,9 +133,14 @@ void permute_split_device(const void* in, const dims_t& dims, const std::vector<
                           uint64_t rows, uint64_t rows_pad, uint64_t K, uint64_t kcs, uint8_t* planes,
                           uint64_t plane_bytes, uint32_t tile_rows, uint32_t KS, bool two_rows, void* stream);
 uint32_t take_gemm_error();
+// C (M x N) = A'' (M x K) B''^T, A'' and B'' (N x K) complex128 row-major, FP64-accurate
+// through exact digit products on tcgen05 (gemm_oz.cu).
+void gemm_oz6(const void* A, const void* Bt, void* C, uint64_t M, uint64_t N, uint64_t K, void* stream);
+uint32_t take_ozg_error();
+// gemm: the GEMM precision (QTNH_GEMM_*), -1 for the process-wide mode.
 void contract_dense_device(const void* a, const dims_t& dims_a, const void* b, const dims_t& dims_b,
                            const std::vector<Wire>& wires, const std::vector<uint16_t>& pos_a,
-                           const std::vector<uint16_t>& pos_b, void* c, void* stream);
+                           const std::vector<uint16_t>& pos_b, void* c, void* stream, int gemm = -1);
 // Dense materialisation of an implicit kind (swap/iden/diag) into `out` (prod(dims) elements).
 void materialise_device(const TensorMeta& t, const void* data, void* out, void* stream);
 

@@ -22,6 +22,8 @@
 // addition: (floor(m / 2^(s-1)) + 2B + 1) >> 1 = round(m / 2^s) + B.
 #pragma once
 
+#include <math.h>
+
 #include "df32.cuh"
 
 namespace qtnh_impl {
@@ -110,6 +112,36 @@ DF_HD double combine(const float* C, uint32_t K20) {
   df::two_sum(C[0], s2, s, e2);
   e = df::add(e, e2);
   return scaled_double(s, K20) + scaled_double(e, K20);
+}
+
+// ---- the dense GEMM form (gemm_oz.cu): digits per row of A and per column of B ----
+//
+// C^[r][n] = 2^(ea + eb - 2060) sum_l 2^(-8l) S_l with S_l the level sums of the digit
+// products. A chunk's level sums are exact integers of at most 2^24 in magnitude; they are
+// accumulated as T += S_0 2^24 + S_1 2^16 + S_2 2^8 + S_3 (exact 64-bit integer) and
+// F += S_4 + 2^-8 S_5 (FP32, below 2^-32 of T's units), and C^ = 2^(ea + eb - 2084) (T +
+// 2^-8 F).
+
+// Adds one chunk's six level sums (exact integers held in floats) to (T, F).
+DF_HD void gemm_accumulate(const float lv[NL], long long& T, float& F) {
+  const long long s0 = (long long)(int)lv[0], s1 = (long long)(int)lv[1];
+  const long long s2 = (long long)(int)lv[2], s3 = (long long)(int)lv[3];
+  T += (s0 << 24) + (s1 << 16) + (s2 << 8) + s3;
+  F = df::add(F, df::fma(lv[5], 0.00390625f, lv[4]));
+}
+
+// Exponent e of C^'s scale 2^e for row exponent ea and column exponent eb.
+DF_HD int gemm_scale(uint32_t ea, uint32_t eb) { return (int)digit_scale(ea) + (int)digit_scale(eb) - 2084; }
+
+// 2^e (T + 2^-8 F) as a double: one rounding of T + 2^-8 F, then an exact scaling while
+// the result stays a normal double (else scalbn: overflow to infinity, gradual underflow).
+DF_HD double gemm_finish(long long T, float F, int e) {
+  const double v = fma((double)F, 0.00390625, (double)T);
+  if (v == 0.0) return 0.0;
+  const uint64_t b = df::d2u(v);
+  const int en = (int)((b >> 52) & 0x7FFull) + e;
+  if (en >= 1 && en <= 2046) return df::u2d(b + ((uint64_t)(int64_t)e << 52));
+  return scalbn(v, e);
 }
 
 }  // namespace oz

@@ -41,7 +41,9 @@ int gemm_mode() {
   int m = g_gemm.load(std::memory_order_relaxed);
   if (m < 0) {
     const char* e = std::getenv("QTNH_GEMM");
-    m = (e && std::strcmp(e, "bf16x3") == 0) ? QTNH_GEMM_BF16X3 : QTNH_GEMM_FP64;
+    m = QTNH_GEMM_OZ6;
+    if (e && std::strcmp(e, "bf16x3") == 0) m = QTNH_GEMM_BF16X3;
+    if (e && std::strcmp(e, "fp64") == 0) m = QTNH_GEMM_FP64;
     g_gemm.store(m);
   }
   return m;
@@ -179,7 +181,8 @@ int qtnh_get_arithmetic(void) { return arithmetic_mode(); }
 
 int qtnh_set_gemm_precision(int mode) {
   return QTNH_API([&]() -> int {
-    if (mode != QTNH_GEMM_FP64 && mode != QTNH_GEMM_BF16X3) throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown GEMM precision");
+    if (mode != QTNH_GEMM_FP64 && mode != QTNH_GEMM_BF16X3 && mode != QTNH_GEMM_OZ6)
+      throw Error(QTNH_ERR_INVALID_ARGUMENT, "unknown GEMM precision");
     g_gemm.store(mode);
     return QTNH_OK;
   });

@@ -23,3 +23,14 @@ def test_ozaki_slices_exact_and_accurate(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "ok" in out.stdout
+
+
+def test_ozaki_gemm_arithmetic(tmp_path):
+    """The digit GEMM's chunked exact level sums, integer/FP32 accumulation and final
+    scaling (ozaki.cuh, as gemm_oz.cu uses them) against long double."""
+    exe = str(tmp_path / "ozaki_gemm_check")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "qtnh_gb300", "csrc"),
+                           "-o", exe, os.path.join(HERE, "cpp", "ozaki_gemm_check.cpp")])
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "ok" in out.stdout
