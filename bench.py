@@ -73,12 +73,15 @@ def _args():
     p.add_argument("--arith", default="bf16x6", choices=["bf16x6", "f32x2", "fp64"],
                    help="arithmetic of the gate/diagonal kernels (storage is complex128 either way)")
     p.add_argument("--no-arith-check", action="store_true")
-    p.add_argument("--workload", default="circuit", choices=["circuit", "contract", "batch", "serve", "kernels"],
+    p.add_argument("--workload", default="circuit",
+                   choices=["circuit", "contract", "batch", "serve", "kernels", "qft", "api"],
                    help="circuit: the n=28 random layered circuit (headline); contract: 64 seeded dense "
                         "contraction pairs, split-precision BF16x3 GEMM vs FP64 plain (precision study); batch: "
                         "2048 uneven circuits in mixed precision under one CUDA graph; serve: a Poisson request "
                         "stream through the request loop, plain complex128 vs mixed complex64; kernels: the "
-                        "plain path's permute, diag, gate and norm kernels one by one (HBM fractions)")
+                        "plain path's permute, diag, gate and norm kernels one by one (HBM fractions); qft: the "
+                        "16-qubit QFT network through the C++ API's TensorNetwork::contractAll; api: the headline "
+                        "circuit through the C++ API, one Tensor::contract per gate")
     p.add_argument("--requests", type=int, default=400)
     p.add_argument("--circuits", type=int, default=2048)
     p.add_argument("--pairs", type=int, default=64)
@@ -237,6 +240,122 @@ def run_reference(a):
                          "sample": _sample_desc(a.n, cores) + "; one independent replica per core"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line), flush=True)
+
+
+# ---- the drop-in path: workloads through the C++ API (qtnh_gb300/drivers/api_bench.cpp) ----
+
+QFT_METRIC = "QFT networks/s (n=16, TensorNetwork::contractAll through the C++ API)"
+API_METRIC = "gate-layers/s through the C++ API (one Tensor::contract per gate)"
+
+
+def _qft_config(n):
+    return {"workload": "QFT on n=%d qubits as a TensorNetwork (random complex Gaussian state, Hadamard SymmTensors, "
+                        "controlled-phase DiagTensors, SwapTensor reversals; DIST identities for distributed qubits), "
+                        "TensorNetwork::contractAll(order)" % n,
+            "qubits": n, "element": "complex128", "l2_flush": "not needed: every run copies its state in and out",
+            "parallelism": "single GPU"}
+
+
+def _qft_oracle_seconds(n, dq, seed):
+    """One QFT run of the oracle port (the same contractions, one core)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_qft_gpu import OracleEngine, run_qft
+    from oracle import oracle as orc
+    orc.build()
+    rng = np.random.default_rng(seed)
+    psi = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+    psi /= np.linalg.norm(psi)
+    t0 = time.perf_counter()
+    run_qft(OracleEngine(), psi, n, dq, lambda *x: None)
+    return time.perf_counter() - t0
+
+
+def main_qft(a):
+    """configs[0]: the QFT network on n=16 through the C++ API; every run copies the state in
+    (DenseTensor::make) and the result out, so value and e2e are the same measurement."""
+    import numpy as np
+    from qtnh_gb300 import build as bld
+    from qtnh_gb300 import workload as wl
+    n = 16 if a.n == 28 else a.n
+    bld.build()
+    if a.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        times = [_qft_oracle_seconds(n, 0, a.seed) for _ in range(a.warmup + a.steps)][a.warmup:]
+        sec = statistics.median(times)
+        line = {"metric": QFT_METRIC, "value": 1.0 / sec, "unit": "QFT/s", "impl": "reference", "n_gpus": a.gpus,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+                "config": _qft_config(n),
+                "cpu_baseline": {"value": 1.0 / sec, "unit": "QFT/s", "cores": 1, "kind": "port",
+                                 "sample": "one full QFT run (dq = 0) of the oracle port per step"},
+                "e2e": {"value": 1.0 / sec, "unit": "QFT/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    cpu = None
+    if not a.no_cpu_baseline:
+        s0, s1 = _qft_oracle_seconds(n, 0, a.seed), _qft_oracle_seconds(n, 1, a.seed)
+        cpu = {"value": 1.0 / s0, "unit": "QFT/s", "cores": 1, "kind": "port",
+               "sample": "one full QFT run of the oracle port (dq = 0; dq = 1: %.3f QFT/s)" % (1.0 / s1)}
+    rng = np.random.default_rng(a.seed)
+    psi = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+    psi /= np.linalg.norm(psi)
+    tmp = tempfile.mkdtemp(prefix="qtnh_qft_")
+    fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
+    psi.astype(np.complex128).tofile(fin)
+    runs = {}
+    clocks = _Clocks(0)
+    clocks.start()
+    for dq in (1, 0):
+        runs[dq] = wl.run_api_driver(["qft", n, dq, fin, fout, a.warmup, a.steps])
+    ck = clocks.stop()
+    # dq = 0 ran last: every gate in place and the swaps reverse the qubits, so the result in
+    # its own index order is the discrete Fourier transform of the input
+    out = np.fromfile(fout, dtype=np.complex128)
+    dft = np.fft.ifft(psi) * math.sqrt(2 ** n)
+    err = float(np.linalg.norm(out - dft) / np.linalg.norm(dft))
+    v = 1e3 / runs[0]["ms_per_run"]
+    line = {"metric": QFT_METRIC, "value": v, "unit": "QFT/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": runs[0]["ms_per_run"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic (seeded state)", "config": _qft_config(n),
+            "timing": "host clock around the stream (the C++ API path); every run includes DenseTensor::make's copy "
+                      "in and the result's copy out",
+            "contractions_per_run": runs[0]["contractions_per_run"],
+            "dq1": {"value": 1e3 / runs[1]["ms_per_run"], "ms_per_run": runs[1]["ms_per_run"],
+                    "contractions_per_run": runs[1]["contractions_per_run"]},
+            "result_check": {"rel_l2_vs_dft": err},
+            "cpu_baseline": cpu,
+            "e2e": {"value": v, "unit": "QFT/s", "h2d_bytes_per_step": 16 * 2 ** n, "d2h_bytes_per_step": 16 * 2 ** n},
+            "clocks": ck, "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+
+
+def main_api(a):
+    """The headline circuit through the C++ API: one Tensor::contract per gate and per phase
+    diagonal, rescatter/permute/rescatter every 8th layer; the state is made once (seeded)."""
+    from qtnh_gb300 import build as bld
+    from qtnh_gb300 import workload as wl
+    bld.build()
+    circ = wl.random_circuit(a.n, a.depth, seed=a.seed)
+    tmp = tempfile.mkdtemp(prefix="qtnh_api_")
+    fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
+    wl.write_api_circuit(fin, circ, seed=a.seed + 1)
+    clocks = _Clocks(0)
+    clocks.start()
+    r = wl.run_api_driver(["circuit", fin, fout, a.warmup, a.steps])
+    ck = clocks.stop()
+    os.remove(fout)
+    v = a.depth / (r["ms_per_run"] * 1e-3)
+    line = {"metric": API_METRIC, "value": v, "unit": "gate-layers/s", "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": r["ms_per_run"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "arith": a.arith, "data": "synthetic (seeded circuit and state)",
+            "config": _config(a),
+            "timing": "host clock around the stream; every step applies the circuit through per-gate "
+                      "Tensor::contract calls (queued in-place contractions applied as fused layers) and ends with "
+                      "Tensor::copy",
+            "contractions_per_step": r["contractions_per_run"], "clocks": ck}
     print(json.dumps(line), flush=True)
 
 
@@ -1088,6 +1207,15 @@ def main():
             run_reference(a)
         else:
             main_batch(a)
+        return
+    if a.workload == "qft":
+        main_qft(a)
+        return
+    if a.workload == "api":
+        if a.impl == "reference":
+            run_reference(a)
+        else:
+            main_api(a)
         return
     if a.workload == "contract":
         if a.impl == "reference":

@@ -107,6 +107,14 @@ int qtnh_workspace_stats(uint64_t* allocations, uint64_t* pool_used_bytes);
  * previous call and clears them. */
 int qtnh_take_device_errors(uint32_t* flags);
 
+/* Test hook of the bounded waits (no counterpart in the reference; off by default): while
+ * on != 0, every launch of the tcgen05 gate-pair kernel makes its first exponent exchange
+ * wait on a shared-memory barrier that nothing completes, with a limit of ~2^20 cycles.
+ * The wait expires before any tensor-core work of the CTA is issued; the CTA raises error
+ * bit 2, frees its tensor memory and returns without writing, so the state is left as it
+ * was and the next launch (hook off) runs normally. Synchronous with the host; process-wide. */
+int qtnh_debug_expire_exchange_wait(int on);
+
 /* Arithmetic of the complex128 gate and diagonal kernels (storage is always complex128).
  * QTNH_ARITH_BF16X6 (default): qtnh_apply_gate_layer fuses consecutive disjoint pairs of
  *   two-qubit gates (all dims 2) into 16x16 unitaries applied on the bf16 tensor cores:

@@ -4,6 +4,8 @@
 ``libqtnh.so``       the qtnh C++ API (``include/qtnh.hpp``), from ``cpp/*.cpp``; calls only
                      the C ABI and needs no CUDA headers.
 ``tests/cpp/_build/api_test``  the C++ API test driver.
+``_build/api_bench``  workloads through the C++ API (drivers/api_bench.cpp), for the
+                     benchmark and the drop-in tests.
 
 Every .cu file is compiled with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo`` in parallel; the CUDA
@@ -26,6 +28,8 @@ API_LIB = "libqtnh.so"
 CPP = os.path.join(HERE, "cpp")
 TEST_SRC = os.path.join(ROOT, "tests", "cpp", "api_test.cpp")
 TEST_BIN = os.path.join(ROOT, "tests", "cpp", "_build", "api_test")
+DRIVER_SRC = os.path.join(HERE, "drivers", "api_bench.cpp")
+DRIVER_BIN = os.path.join(BUILD, "api_bench")
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-I", INCLUDE, "-I", CPP]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -76,6 +80,7 @@ def build(force=False, verbose=False):
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
     api = _build_api(lib, force)
     _build_test(api, force)
+    _build_driver(api, force)
     if verbose:
         print("built", lib, api, TEST_BIN)
     return lib
@@ -116,6 +121,17 @@ def _build_test(api, force):
     if r.returncode != 0:
         raise RuntimeError("API test build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
     return TEST_BIN
+
+
+def _build_driver(api, force):
+    if not force and _newer(DRIVER_BIN, [DRIVER_SRC, api] + _api_headers()):
+        return DRIVER_BIN
+    cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-O3", "-o", DRIVER_BIN, DRIVER_SRC, "-L", LIBDIR, "-lqtnh",
+                                                        "-lqtnh_cuda", "-Wl,-rpath," + LIBDIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("API driver build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return DRIVER_BIN
 
 
 if __name__ == "__main__":

@@ -105,9 +105,36 @@ __device__ __forceinline__ double2 group_output_fp64(const double2* U16, const d
 // Host side: the pair's parameters (targets of gate a, then gate b; all dims 2).
 PairParams make_pair_params(const dims_t& dims, const uint16_t all[4]);
 
+struct ChainRec;
 // tcgen05 kernel for states of at least 2048 amplitudes; false if it does not apply.
+// rec (may be null) receives the largest group key of the outputs and the smallest
+// nonzero half group (ChainRec::maxkey, ::minc; atomicMax).
 bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
-                      uint32_t mode = PAIR_KRON);
+                      uint32_t mode = PAIR_KRON, ChainRec* rec = nullptr);
+
+// What one pass of a gate layer's fixed-point chain wrote (device memory; the host zeroes
+// the chain's records before its first pass).
+struct ChainRec {
+  uint32_t maxkey;  // doubles written: the largest oz::group_key of the outputs
+  uint32_t maxhi;   // fixed point written: the largest |hi word| of the outputs
+  int32_t F;        // fixed point written: value = Y 2^-F
+  int32_t fmt;      // 1: fixed point written, 0: doubles
+  uint32_t minc;    // doubles written by the first pass: 2047 - the smallest exponent of a
+                    // nonzero half group's largest output (0: none)
+  uint32_t pad[3];
+};
+
+// A chain starts only when every nonzero half group the first pass wrote lies within
+// 2^CHAIN_RANGE of the largest magnitude: fixed point carries ~46 bits of the largest
+// magnitude, so every group keeps ~40 bits of its own.
+constexpr int CHAIN_RANGE = 6;
+
+// Whether the chain kernel takes a pair of this shape (the tcgen05 tile shape).
+bool chain_applies(const PairParams& p);
+// A later pass of a chain (two disjoint two-qubit gates): reads what rin describes, writes
+// fixed point (want_fixed, when the scales allow) or doubles, and records it in rout.
+void launch_pair_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
+                       const ChainRec* rin, ChainRec* rout, bool want_fixed);
 
 // Reads and clears the tcgen05 kernel's device error flags (bounded waits that expired).
 uint32_t take_umma_error();

@@ -24,6 +24,8 @@
 // 2^-822.
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "gate_pair.cuh"
@@ -304,10 +306,32 @@ bool apply_gate_tc_single(void* state, const dims_t& dims, const std::vector<uin
   return true;
 }
 
+namespace {
+
+// QTNH_GATE_CHAIN=0 keeps every pass of a layer in doubles (no fixed-point chain).
+bool chain_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("QTNH_GATE_CHAIN");
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
+struct LayerStep {
+  size_t g;        // first gate
+  bool pair;       // gates g and g + 1 fused, else gate g alone
+  PairParams p;    // pair parameters
+};
+
+}  // namespace
+
 // Pairs of consecutive, disjoint two-qubit gates on a power-of-two state are fused and
 // applied on the tensor cores; everything else goes through apply_gate_device (where a
-// lone gate on two, three or four qubits runs on the tensor cores too). Returns after
-// issuing all launches.
+// lone gate on two, three or four qubits runs on the tensor cores too). A run of two or
+// more fused pairs on the tcgen05 tile shape is a chain: the first pass reads and writes
+// doubles and records their largest exponent, the next ones cut the state at that one
+// scale and pass it on as 64-bit fixed point, the last writes doubles (ozaki.cuh,
+// gate_umma.cu). Returns after issuing all launches.
 void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
                          const std::vector<const void*>& gates, void* stream) {
   const size_t r = dims.size();
@@ -315,6 +339,7 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
   for (auto d : dims) pow2 = pow2 && log2_or_none(d) != 0xFFFFFFFFu;
   const uint64_t n = product(dims);
   cudaStream_t s = (cudaStream_t)stream;
+  std::vector<LayerStep> steps;
   size_t g = 0;
   while (g < gates.size()) {
     bool fused = false;
@@ -329,16 +354,50 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
       ok = ok && std::adjacent_find(srt.begin(), srt.end()) == srt.end();
       if (ok) {
         const uint16_t tg[4] = {ta[0], ta[1], tb[0], tb[1]};
-        launch_fused_pair(static_cast<double2*>(state), static_cast<const double2*>(gates[g]),
-                          static_cast<const double2*>(gates[g + 1]), make_pair_params(dims, tg), n, s);
+        steps.push_back({g, true, make_pair_params(dims, tg)});
         g += 2;
         fused = true;
       }
     }
     if (!fused) {
-      apply_gate_device(state, dims, targets[g], gates[g], stream);
+      steps.push_back({g, false, PairParams{}});
       g += 1;
     }
+  }
+  double2* psi = static_cast<double2*>(state);
+  auto gate_ptr = [&](size_t i) { return static_cast<const double2*>(gates[i]); };
+  size_t i = 0;
+  while (i < steps.size()) {
+    size_t j = i;
+    while (j < steps.size() && steps[j].pair && chain_applies(steps[j].p)) ++j;
+    const size_t R = j - i;
+    if (R >= 2 && chain_enabled()) {
+      ChainRec* recs = static_cast<ChainRec*>(workspace_alloc(R * sizeof(ChainRec), stream));
+      try {
+        check_cuda(cudaMemsetAsync(recs, 0, R * sizeof(ChainRec), s), "clear chain records");
+        const LayerStep& s0 = steps[i];
+        launch_pair_umma(psi, gate_ptr(s0.g), gate_ptr(s0.g + 1), s0.p, s, PAIR_KRON, &recs[0]);
+        count_launch();
+        for (size_t k = 1; k < R; ++k) {
+          const LayerStep& sk = steps[i + k];
+          launch_pair_chain(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, &recs[k - 1], &recs[k], k + 1 < R);
+          count_launch();
+        }
+        check_cuda(cudaGetLastError(), "gate chain launch");
+      } catch (...) {
+        workspace_free(recs, stream);
+        throw;
+      }
+      workspace_free(recs, stream);
+      i = j;
+      continue;
+    }
+    const LayerStep& st = steps[i];
+    if (st.pair)
+      launch_fused_pair(psi, gate_ptr(st.g), gate_ptr(st.g + 1), st.p, n, s);
+    else
+      apply_gate_device(state, dims, targets[st.g], gates[st.g], stream);
+    ++i;
   }
 }
 

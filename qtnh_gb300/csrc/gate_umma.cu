@@ -37,6 +37,9 @@ namespace qtnh_impl {
 // bit 0: a wait for digits expired, bit 1: a wait for MMA completion expired, bit 2: a
 // wait for the partner half's exponent expired
 __device__ unsigned int g_umma_error;
+// Test hook (qtnh_debug_expire_exchange_wait): nonzero makes the pair kernel's first
+// exponent exchange wait on a barrier that nothing completes, with a short limit.
+__device__ int g_umma_test_expire;
 
 namespace {
 
@@ -49,6 +52,7 @@ constexpr int UM_COLS = 256;             // TMEM column stride of a team (its le
 constexpr uint32_t UM_TMEM_COLS = 256;   // allocation (power of two >= UM_WG * UM_COLS): half of an SM's TMEM
 static_assert(oz::NL * UM_N <= UM_COLS, "level sums exceed a team's TMEM columns");
 constexpr long long UM_WAIT_CYCLES = 1ll << 31;  // ~1 s at 2 GHz
+constexpr long long UM_TEST_WAIT_CYCLES = 1ll << 20;  // the test hook's wait: ~0.5 ms
 
 // Shared memory of one CTA (dynamic). Operand layout (K-major, no swizzle): an 8-row x
 // 16-byte core matrix is 128 contiguous bytes (row at 16 * row); for one K-step of 16,
@@ -62,6 +66,8 @@ struct UmSmem {
   int32_t erow[16];                           // largest exponent of row o of U16
   uint32_t krow[16];                          // oz::scale_bits(erow[o])
   uint64_t keyx[UM_WG][4];                    // per row quarter: both halves' keys (and amplitudes) are visible
+  uint64_t never;                             // test hook: a barrier no thread arrives on
+  int test_expire;
   uint64_t full[UM_WG];                       // digits of team t's tile are ready
   uint64_t done[UM_WG];                       // MMAs of team t's tile are complete
   uint32_t tmem_base;
@@ -88,12 +94,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Warp-uniform bounded wait for the phase of parity `parity`; false on expiry or abort.
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, volatile int* abort) {
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                               long long limit = UM_WAIT_CYCLES) {
   const long long t0 = clock64();
   while (true) {
     const bool ok = mbar_try_wait(bar, parity);
     if (__all_sync(0xffffffffu, ok)) return true;
-    if (__any_sync(0xffffffffu, *abort != 0 || clock64() - t0 > UM_WAIT_CYCLES)) return false;
+    if (__any_sync(0xffffffffu, *abort != 0 || clock64() - t0 > limit)) return false;
   }
 }
 
@@ -137,23 +144,38 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&v)[4]) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Largest group key (oz::group_key) of an amplitude's two parts.
+__device__ __forceinline__ uint32_t amp_key(double2 v) {
+  return max(oz::group_key(df::words(v.x)), oz::group_key(df::words(v.y)));
+}
+
 // FP64 outputs 8 h .. 8 h + 7 of one group whose 16 amplitudes are in the stage
-// (stride UM_M); the two halves' inputs are all read before either thread writes.
+// (stride UM_M); the two halves' inputs are all read before either thread writes. Returns
+// the largest key of the outputs.
 template <typename IT>
-__device__ __noinline__ void half_group_fp64(double2* __restrict__ psi, IT gbase, const PairParams& p,
-                                             const double2* U16, const double2* stage_r, int h) {
+__device__ __noinline__ uint32_t half_group_fp64(double2* __restrict__ psi, IT gbase, const PairParams& p,
+                                                 const double2* U16, const double2* stage_r, int h) {
   double2 x[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) x[c] = stage_r[c * UM_M];
+  uint32_t key = 0;
 #pragma unroll 1
-  for (int o = 8 * h; o < 8 * h + 8; ++o) psi[gbase + (IT)p.off[o]] = group_output_fp64(U16, x, o);
+  for (int o = 8 * h; o < 8 * h + 8; ++o) {
+    const double2 v = group_output_fp64(U16, x, o);
+    key = max(key, amp_key(v));
+    psi[gbase + (IT)p.off[o]] = v;
+  }
+  return key;
 }
 
-template <typename IT, uint32_t MODE>
+// RECORD: rec receives the largest group key of the outputs and the smallest exponent of a
+// nonzero half group's largest output (atomicMax), for the next pass of a fixed-point chain.
+template <typename IT, uint32_t MODE, bool RECORD>
 __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* __restrict__ psi,
                                                                        const double2* __restrict__ ga,
                                                                        const double2* __restrict__ gb,
-                                                                       const __grid_constant__ PairParams p) {
+                                                                       const __grid_constant__ PairParams p,
+                                                                       ChainRec* __restrict__ rec) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   UmSmem& sm = *reinterpret_cast<UmSmem*>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -163,11 +185,13 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
   if (tid == 0) {
     sm.gate_ok = 1;
     sm.abort = 0;
+    sm.test_expire = *(volatile int*)&g_umma_test_expire;
     for (int w = 0; w < UM_WG; ++w) {
       for (int qq = 0; qq < 4; ++qq) mbar_init(&sm.keyx[w][qq], 64);  // the quarter's two warps
       mbar_init(&sm.full[w], UM_TEAM);
       mbar_init(&sm.done[w], 1);
     }
+    mbar_init(&sm.never, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == UM_WG * 8) {
@@ -221,7 +245,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
       cp_async_commit();
     };
     fetch(tile_of(t));
-    uint32_t it = 0;
+    uint32_t it = 0, okey = 0, ominc = 0;
     for (uint64_t m = t; tile_of(m) < ntiles; m += UM_WG, ++it) {
       const IT gbase = pair_base<IT>((IT)(tile_of(m) * UM_M + r), p);
       cp_async_wait_all();
@@ -233,7 +257,11 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
       for (int c = 0; c < 8; ++c) key = max(key, max(oz::group_key(df::words(x[c].x)), oz::group_key(df::words(x[c].y))));
       sm.key[t][h][r] = key;
       mbar_arrive(&sm.keyx[t][q]);  // both halves' keys and fetched amplitudes become visible
-      if (!mbar_wait_warp(&sm.keyx[t][q], it & 1u, &sm.abort)) {
+      // (test hook: the first exchange waits on a barrier nothing completes; no MMA, tensor
+      // memory load or bulk copy of this CTA is in flight yet)
+      const bool expire = sm.test_expire != 0 && it == 0;
+      if (!mbar_wait_warp(expire ? &sm.never : &sm.keyx[t][q], expire ? 0u : (it & 1u), &sm.abort,
+                          expire ? UM_TEST_WAIT_CYCLES : UM_WAIT_CYCLES)) {
         atomicOr(&g_umma_error, 4u);
         sm.abort = 1;
         break;
@@ -268,7 +296,13 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
           *reinterpret_cast<uint4*>(&sm.adig[t][j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
         }
       }
-      if (!ok) half_group_fp64<IT>(psi, gbase, p, sm.U16, &sm.stage[t][0][r], h);
+      if (!ok) {
+        const uint32_t k = half_group_fp64<IT>(psi, gbase, p, sm.U16, &sm.stage[t][0][r], h);
+        if (RECORD) {
+          okey = max(okey, k);
+          if (k) ominc = max(ominc, 2047u - oz::key_exponent(k));
+        }
+      }
       fence_proxy_async();
       mbar_arrive(&sm.full[t]);
       if (!early) {
@@ -289,6 +323,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
       // level sums: TMEM lane r, columns t * UM_COLS + 32 l + o (o < 16: real part of
       // amplitude o, o >= 16: imaginary part of amplitude o - 16)
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * UM_COLS);
+      uint32_t hkey = 0;  // largest key of this half group's outputs
 #pragma unroll
       for (int c4 = 0; c4 < 2; ++c4) {
         const int a0 = 8 * h + 4 * c4;
@@ -306,13 +341,30 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
             float lr[oz::NL], li[oz::NL];
 #pragma unroll
             for (int l = 0; l < oz::NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
-            psi[gbase + (IT)p.off[a0 + a]] = make_double2(oz::combine(lr, K20), oz::combine(li, K20));
+            const double2 v = make_double2(oz::combine(lr, K20), oz::combine(li, K20));
+            if (RECORD) hkey = max(hkey, amp_key(v));
+            psi[gbase + (IT)p.off[a0 + a]] = v;
           }
         }
+      }
+      if (RECORD && ok) {
+        okey = max(okey, hkey);
+        if (hkey) ominc = max(ominc, 2047u - oz::key_exponent(hkey));
       }
       tc_fence_before();
     }
     cp_async_wait_all();
+    if (RECORD) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        okey = max(okey, __shfl_xor_sync(0xffffffffu, okey, o));
+        ominc = max(ominc, __shfl_xor_sync(0xffffffffu, ominc, o));
+      }
+      if (lane == 0) {
+        if (okey) atomicMax(&rec->maxkey, okey);
+        if (ominc) atomicMax(&rec->minc, ominc);
+      }
+    }
   } else {
     // ---- MMA warp: one elected thread issues each tile's 12 MMAs ----
     const uint32_t bbase = smem_u32(&sm.bdig[0][0][0]);
@@ -355,28 +407,308 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
   }
 }
 
+// ---- a later pass of a gate layer's chain --------------------------------------------
+//
+// The input is what the previous pass wrote (rin): doubles with the largest group key of
+// all of them, or 64-bit fixed point at scale rin->F with the largest |hi word|. Both are
+// cut into digits at one scale for the whole state -- no per-group exponent exchange, and
+// for fixed point no per-element exponent alignment (oz::digits_fixed). The output is
+// fixed point at scale F = 2100 - E - max erow (want_fixed) or doubles; rout records it.
+// When the input is doubles whose largest magnitude lies outside 2^-200..2^201 or the gate
+// has entries the digits cannot carry (then gate_ok is 0), every group is computed in FP64
+// (from the converted fixed-point input where that is the input) and doubles are written.
 template <typename IT, uint32_t MODE>
-void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s) {
+__global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __restrict__ psiv,
+                                                                        const double2* __restrict__ ga,
+                                                                        const double2* __restrict__ gb,
+                                                                        const __grid_constant__ PairParams p,
+                                                                        const ChainRec* __restrict__ rin,
+                                                                        ChainRec* __restrict__ rout, int want_fixed) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  UmSmem& sm = *reinterpret_cast<UmSmem*>(smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint64_t ntiles = p.ngroups / UM_M;
+  double2* psi = static_cast<double2*>(psiv);
+  int64_t* psy = static_cast<int64_t*>(psiv);
+
+  // ---- setup as the pair kernel: barriers, tensor memory, the fused gate and its digits ----
+  if (tid == 0) {
+    sm.gate_ok = 1;
+    sm.abort = 0;
+    mbar_init(&sm.full[0], UM_TEAM);
+    mbar_init(&sm.done[0], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == UM_WG * 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(UM_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  for (int t = tid; t < 256; t += UM_THREADS) sm.U16[t] = fused_entry<MODE>(ga, gb, t);
+  __syncthreads();
+  if (tid < 16) {
+    bool ok;
+    const uint32_t e = row_exponent(sm.U16, tid, ok);
+    sm.erow[tid] = (int32_t)e;
+    if (!ok) sm.gate_ok = 0;
+  }
+  __syncthreads();
+  if (tid < 128) {
+    const int o = tid >> 2, kc = tid & 3;
+    const uint32_t E = oz::digit_scale((uint32_t)sm.erow[o & 15]);
+    float d[8][oz::NS];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) oz::digits(df::words(real_form(sm.U16, o, kc * 8 + e)), E, d[e]);
+#pragma unroll
+    for (int j = 0; j < oz::NS; ++j) {
+      const uint4 v = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]), oz::pack(d[4][j], d[5][j]),
+                                 oz::pack(d[6][j], d[7][j]));
+      *reinterpret_cast<uint4*>(&sm.bdig[kc >> 1][j][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) = v;
+    }
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+
+  // ---- the scales (the same in every CTA) ----
+  const ChainRec ri = *rin;
+  const bool in_fixed = ri.fmt == 1;
+  uint32_t sh = 1;
+  int Ein;
+  bool in_ok = true;
+  if (in_fixed) {
+    sh = oz::fixed_shift(ri.maxhi);
+    Ein = 1070 + (int)sh - ri.F;
+  } else {
+    // doubles: one scale for the whole state, if its largest magnitude is in the digit range
+    // and (when recorded) no nonzero half group lies more than 2^CHAIN_RANGE below it
+    const uint32_t E = oz::key_exponent(ri.maxkey);
+    in_ok = tc_scale_ok(E) && (ri.minc == 0 || (int)E - (2047 - (int)ri.minc) <= CHAIN_RANGE);
+    Ein = (int)oz::digit_scale(E);
+  }
+  const bool uni = in_ok && sm.gate_ok != 0;
+  const bool out_fixed = uni && want_fixed != 0;
+  int max_erow = 0;
+#pragma unroll
+  for (int o = 0; o < 16; ++o) max_erow = max(max_erow, sm.erow[o]);
+  const int F_out = 2100 - Ein - max_erow;
+  if (blockIdx.x == 0 && tid == 0) {
+    rout->fmt = out_fixed ? 1 : 0;
+    rout->F = F_out;
+  }
+  auto tile_of = [&](uint64_t m) -> uint64_t { return (uint64_t)blockIdx.x + m * gridDim.x; };
+
+  if (!uni) {
+    // ---- every group in FP64 (no tensor cores): thread per group, doubles out ----
+    uint32_t okey = 0;
+    for (uint64_t g = (uint64_t)blockIdx.x * UM_THREADS + tid; g < p.ngroups; g += (uint64_t)gridDim.x * UM_THREADS) {
+      const IT gbase = pair_base<IT>((IT)g, p);
+      double2 x[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const IT ix = gbase + (IT)p.off[c];
+        x[c] = in_fixed ? make_double2(oz::fixed_to_double(psy[2 * (uint64_t)ix], 40 - ri.F),
+                                       oz::fixed_to_double(psy[2 * (uint64_t)ix + 1], 40 - ri.F))
+                        : psi[ix];
+      }
+#pragma unroll 1
+      for (int o = 0; o < 16; ++o) {
+        const double2 v = group_output_fp64(sm.U16, x, o);
+        okey = max(okey, amp_key(v));
+        psi[gbase + (IT)p.off[o]] = v;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) okey = max(okey, __shfl_xor_sync(0xffffffffu, okey, o));
+    if (lane == 0 && okey) atomicMax(&rout->maxkey, okey);
+  } else if (warp < UM_WG * 8) {
+    // ---- team: fetch, digits at the common scale, recombination, store ----
+    const int v = warp & 7, q = v & 3, h = v >> 2;
+    const int r = q * 32 + lane;  // group row of the tile (TMEM lane)
+    const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16);
+    auto fetch = [&](uint64_t T) {
+      if (T < ntiles) {
+        const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
+#pragma unroll
+        for (int c = 8 * h; c < 8 * h + 8; ++c) cp_async16(&sm.stage[0][c][r], psi + (gbase + (IT)p.off[c]));
+      }
+      cp_async_commit();
+    };
+    fetch(tile_of(0));
+    uint32_t it = 0, okey = 0, ohi = 0;
+    for (uint64_t m = 0; tile_of(m) < ntiles; ++m, ++it) {
+      const IT gbase = pair_base<IT>((IT)(tile_of(m) * UM_M + r), p);
+      cp_async_wait_all();
+      double2 x[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) x[c] = sm.stage[0][8 * h + c][r];
+      fetch(tile_of(m + 1));  // only this thread reads its stage slots
+      // digits of this thread's 16 reals: K core h (real parts of amplitudes 8h..8h+7)
+      // and K core 2 + h (their imaginary parts)
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        const int kc = 2 * part + h;
+        float d[8][oz::NS];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const double xv = part ? x[e].y : x[e].x;
+          if (in_fixed)
+            oz::digits_fixed((int64_t)df::d2u(xv), sh, d[e]);
+          else
+            oz::digits(df::words(xv), (uint32_t)Ein, d[e]);
+        }
+#pragma unroll
+        for (int j = 0; j < oz::NS; ++j) {
+          const uint4 vv = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]),
+                                      oz::pack(d[4][j], d[5][j]), oz::pack(d[6][j], d[7][j]));
+          *reinterpret_cast<uint4*>(&sm.adig[0][j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
+        }
+      }
+      fence_proxy_async();
+      mbar_arrive(&sm.full[0]);
+      if (!mbar_wait_warp(&sm.done[0], it & 1u, &sm.abort)) {
+        atomicOr(&g_umma_error, 2u);
+        sm.abort = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll
+      for (int c4 = 0; c4 < 2; ++c4) {
+        const int a0 = 8 * h + 4 * c4;
+        uint32_t re[oz::NL][4], im[oz::NL][4];
+#pragma unroll
+        for (int l = 0; l < oz::NL; ++l) {
+          tmem_ld4(tbase + (uint32_t)(32 * l + a0), re[l]);
+          tmem_ld4(tbase + (uint32_t)(32 * l + 16 + a0), im[l]);
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          float lr[oz::NL], li[oz::NL];
+#pragma unroll
+          for (int l = 0; l < oz::NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
+          const int64_t Tr = oz::fixed_levels(lr), Ti = oz::fixed_levels(li);
+          const int o = a0 + a;
+          const IT ix = gbase + (IT)p.off[o];
+          if (out_fixed) {
+            const uint32_t k = (uint32_t)min(62, max_erow - sm.erow[o]);
+            const int64_t Yr = oz::fixed_round_shift(Tr, k), Yi = oz::fixed_round_shift(Ti, k);
+            ohi = max(ohi, max(oz::fixed_hi_mag(Yr), oz::fixed_hi_mag(Yi)));
+            *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
+          } else {
+            const int e = sm.erow[o] + Ein - 2060;
+            const double2 vv = make_double2(oz::fixed_to_double(Tr, e), oz::fixed_to_double(Ti, e));
+            okey = max(okey, amp_key(vv));
+            psi[ix] = vv;
+          }
+        }
+      }
+      tc_fence_before();
+    }
+    cp_async_wait_all();
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      okey = max(okey, __shfl_xor_sync(0xffffffffu, okey, o));
+      ohi = max(ohi, __shfl_xor_sync(0xffffffffu, ohi, o));
+    }
+    if (lane == 0) {
+      if (okey) atomicMax(&rout->maxkey, okey);
+      if (ohi) atomicMax(&rout->maxhi, ohi);
+    }
+  } else {
+    // ---- MMA warp: one elected thread issues each tile's 12 MMAs ----
+    const uint32_t bbase = smem_u32(&sm.bdig[0][0][0]);
+    for (uint64_t m = 0; tile_of(m) < ntiles; ++m) {
+      const uint32_t it = (uint32_t)m;
+      if (!mbar_wait_warp(&sm.full[0], it & 1u, &sm.abort)) {
+        atomicOr(&g_umma_error, 1u);
+        sm.abort = 1;
+        break;
+      }
+      tc_fence_after();
+      if (lane == 0) {
+        const uint32_t abase = smem_u32(&sm.adig[0][0][0][0]);
+#pragma unroll
+        for (int j = 0; j < oz::NS; ++j) {
+#pragma unroll
+          for (int ks = 0; ks < 2; ++ks) {
+            const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
+            const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * oz::NS * UM_N * 32));
+            umma_bf16(tmem + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (oz::NL - j))),
+                      (j | ks) != 0 ? 1u : 0u);
+          }
+        }
+        umma_commit(&sm.done[0]);
+      }
+      __syncwarp();
+    }
+  }
+
+  // ---- teardown: all tensor-memory reads are done; free it ----
+  tc_fence_before();
+  __syncthreads();
+  if (warp == UM_WG * 8) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+  }
+}
+
+template <typename IT, uint32_t MODE>
+void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
+                 ChainRec* rec = nullptr) {
   const size_t smem = sizeof(UmSmem);
-  check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem),
-             "gate_pair_umma_kernel shared memory");
   const uint64_t ntiles = p.ngroups / UM_M;
   const int grid = (int)std::min<uint64_t>(ntiles, 2 * (uint64_t)sm_count());  // two CTAs per SM
-  gate_pair_umma_kernel<IT, MODE><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p);
+  if (rec) {
+    check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem),
+               "gate_pair_umma_kernel shared memory");
+    gate_pair_umma_kernel<IT, MODE, true><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p, rec);
+  } else {
+    check_cuda(cudaFuncSetAttribute(gate_pair_umma_kernel<IT, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem),
+               "gate_pair_umma_kernel shared memory");
+    gate_pair_umma_kernel<IT, MODE, false><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p, nullptr);
+  }
+}
+
+template <typename IT>
+void launch_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
+                  const ChainRec* rin, ChainRec* rout, bool want_fixed) {
+  const size_t smem = sizeof(UmSmem);
+  check_cuda(cudaFuncSetAttribute(gate_pair_chain_kernel<IT, PAIR_KRON>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem),
+             "gate_pair_chain_kernel shared memory");
+  const uint64_t ntiles = p.ngroups / UM_M;
+  const int grid = (int)std::min<uint64_t>(ntiles, 2 * (uint64_t)sm_count());
+  gate_pair_chain_kernel<IT, PAIR_KRON><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0);
 }
 
 }  // namespace
 
+bool chain_applies(const PairParams& p) { return p.ngroups >= (uint64_t)UM_M && p.ngroups % UM_M == 0; }
+
+void launch_pair_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
+                       const ChainRec* rin, ChainRec* rout, bool want_fixed) {
+  if (p.ngroups * 16 <= (1ull << 32))
+    launch_chain<uint32_t>(psi, ga, gb, p, s, rin, rout, want_fixed);
+  else
+    launch_chain<uint64_t>(psi, ga, gb, p, s, rin, rout, want_fixed);
+}
+
 bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
-                      uint32_t mode) {
+                      uint32_t mode, ChainRec* rec) {
   if (p.ngroups < (uint64_t)UM_M || p.ngroups % UM_M) return false;
   const bool i32 = p.ngroups * 16 <= (1ull << 32);
   if (mode == PAIR_KRON) {
     if (i32)
-      launch_umma<uint32_t, PAIR_KRON>(psi, ga, gb, p, s);
+      launch_umma<uint32_t, PAIR_KRON>(psi, ga, gb, p, s, rec);
     else
-      launch_umma<uint64_t, PAIR_KRON>(psi, ga, gb, p, s);
+      launch_umma<uint64_t, PAIR_KRON>(psi, ga, gb, p, s, rec);
     return true;
   }
   if (!i32) return false;  // single three- and four-qubit gates: states up to 2^32 amplitudes
@@ -385,6 +717,10 @@ bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const 
   else
     launch_umma<uint32_t, PAIR_KRON_I2>(psi, ga, gb, p, s);
   return true;
+}
+
+void set_umma_test_expire(int on) {
+  check_cuda(cudaMemcpyToSymbol(g_umma_test_expire, &on, sizeof(on)), "set test hook");
 }
 
 uint32_t take_umma_error() {
@@ -398,6 +734,13 @@ uint32_t take_umma_error() {
 }  // namespace qtnh_impl
 
 using namespace qtnh_impl;
+
+extern "C" int qtnh_debug_expire_exchange_wait(int on) {
+  return QTNH_API([&]() -> int {
+    set_umma_test_expire(on ? 1 : 0);
+    return QTNH_OK;
+  });
+}
 
 extern "C" int qtnh_take_device_errors(uint32_t* flags) {
   return QTNH_API([&]() -> int {

@@ -114,6 +114,77 @@ DF_HD double combine(const float* C, uint32_t K20) {
   return scaled_double(s, K20) + scaled_double(e, K20);
 }
 
+// ---- fixed point between the passes of a gate layer (gate_umma.cu) ----
+//
+// Inside one gate layer the state passes from one fused pass to the next as signed 64-bit
+// fixed point at a common scale, y = Y 2^-F (the pass records F and max |Y|). A pass with
+// such an input cuts every element at one right shift sh (max |Y| < 2^(47 + sh)) into six
+// balanced digits, x ~= m48 2^(sh - F), m48 = round(Y 2^-sh) = sum_j d_j 2^(40 - 8j): the
+// digits of a double at group exponent E with E = 1070 + sh - F (the input's equivalent
+// exponent). The level sums C_l of a row o come back as the exact 64-bit integer
+// T = sum_l C_l 2^(40 - 8l) (|C_l| <= 2^22, so |T| < 2^63), and the output at scale F_out =
+// 2100 - E - max_o erow[o] is Y_o = round(T 2^(erow[o] - max erow)): a right shift, and
+// |Y_o| <= |T|.
+
+// The six balanced digits of the fixed-point value x at right shift sh (1 <= sh < 64),
+// |round(x 2^-sh)| <= 2^47.
+DF_HD void digits_fixed(int64_t x, uint32_t sh, float d[NS]) {
+  const uint64_t mb = (uint64_t)(((x >> (sh - 1u)) + 0x1010101010101ll) >> 1);  // round(x 2^-sh) + B >= 0
+  const uint32_t h = (uint32_t)(mb >> 32), l = (uint32_t)mb;
+  const float off = -8388736.0f;  // -(2^23 + 128)
+  d[0] = df::add(df::u2f(byte_perm(h, 0x4B000000u, 0x7621u)), off);  // bits 40..55 (at most 256)
+  d[1] = df::add(df::u2f(byte_perm(h, 0x4B000000u, 0x7650u)), off);
+  d[2] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7653u)), off);
+  d[3] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7652u)), off);
+  d[4] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7651u)), off);
+  d[5] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7650u)), off);
+}
+
+// The right shift of a fixed-point input whose largest |Y| has its highest set bit in the
+// 32-bit word maxhi (max over elements of |hi word|, see fixed_hi_mag), at least 1: the
+// magnitude bound is taken as 2^(32 + bit length of maxhi).
+DF_HD uint32_t fixed_shift(uint32_t maxhi) {
+  uint32_t len = 0;
+  while (len < 32 && (maxhi >> len)) ++len;
+  const int sh = 32 + (int)len - 47;
+  return sh < 1 ? 1u : (uint32_t)sh;
+}
+
+// |hi word| of a 64-bit value (one's complement for negatives: an upper bound of |x| >> 32).
+DF_HD uint32_t fixed_hi_mag(int64_t x) {
+  const int32_t hi = (int32_t)(x >> 32);
+  return (uint32_t)(hi ^ (hi >> 31));
+}
+
+// Exact T = sum_l C_l 2^(40 - 8l) from the six level sums (exact integers of at most 2^22
+// in magnitude, held in floats): each level is read through the 1.5 2^23 bias (the float's
+// bits minus 0x4B400000), pairs of levels combined in 32 bits, the three pairs in 64 bits.
+DF_HD int64_t fixed_levels(const float C[NL]) {
+  int32_t v[NL];
+  for (int l = 0; l < NL; ++l) v[l] = (int32_t)(df::f2u(df::add(C[l], 12582912.0f)) - 0x4B400000u);
+  const int64_t X = (int64_t)(int32_t)((uint32_t)v[0] * 256u + (uint32_t)v[1]);
+  const int64_t Y = (int64_t)(int32_t)((uint32_t)v[2] * 256u + (uint32_t)v[3]);
+  const int64_t Z = (int64_t)(int32_t)((uint32_t)v[4] * 256u + (uint32_t)v[5]);
+  return (int64_t)((uint64_t)X << 32) + (int64_t)((uint64_t)Y << 16) + Z;
+}
+
+// round(T 2^-k) for 0 <= k <= 62 (ties up).
+DF_HD int64_t fixed_round_shift(int64_t T, uint32_t k) {
+  return k ? ((T + ((int64_t)1 << (k - 1))) >> k) : T;
+}
+
+// T 2^(e - 40) as a double (T from fixed_levels; e = erow + E - 2060): one rounding,
+// then an exact scaling while the result stays a normal double (else scalbn).
+DF_HD double fixed_to_double(int64_t T, int e) {
+  const double v = (double)T;
+  if (v == 0.0) return 0.0;
+  const uint64_t b = df::d2u(v);
+  const int s = e - 40;
+  const int en = (int)((b >> 52) & 0x7FFull) + s;
+  if (en >= 1 && en <= 2046) return df::u2d(b + ((uint64_t)(int64_t)s << 52));
+  return scalbn(v, s);
+}
+
 // ---- the dense GEMM form (gemm_oz.cu): digits per row of A and per column of B ----
 //
 // C^[r][n] = 2^(ea + eb - 2060) sum_l 2^(-8l) S_l with S_l the level sums of the digit

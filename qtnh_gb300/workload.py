@@ -179,3 +179,43 @@ def batch_circuits(count, seed=2026, qubits=(10, 22), depth=(8, 32), diag_every=
             c.layers.append(layer)
         out.append((c, rng.integers(0, 2 ** n, size=queries, dtype=np.uint64)))
     return out
+
+
+def write_api_circuit(path, circuit, psi=None, seed=None, n_dis=3):
+    """Input file of the C++ API driver's circuit mode (qtnh_gb300/drivers/api_bench.cpp):
+    the circuit, and either the initial state or the seed of one the driver draws."""
+    import struct
+    with open(path, "wb") as f:
+        f.write(struct.pack("<ii", circuit.n, len(circuit.layers)))
+        if psi is not None:
+            f.write(struct.pack("<i", 1))
+            f.write(np.ascontiguousarray(psi, dtype=np.complex128).tobytes())
+        else:
+            f.write(struct.pack("<iQ", 0, int(seed or 0)))
+        for layer in circuit.layers:
+            f.write(struct.pack("<i", len(layer.gates)))
+            for (a, b), els in zip(layer.pairs, layer.gates):
+                f.write(struct.pack("<HH", a, b))
+                f.write(np.ascontiguousarray(els, dtype=np.complex128).tobytes())
+            if layer.phases is not None:
+                f.write(struct.pack("<i", 1))
+                f.write(np.asarray(layer.phases, dtype="<f8").tobytes())
+            else:
+                f.write(struct.pack("<i", 0))
+            if layer.ptup is not None:
+                f.write(struct.pack("<i", 1))
+                f.write(np.asarray(layer.ptup, dtype="<u2").tobytes())
+            else:
+                f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<i", n_dis))
+
+
+def run_api_driver(args, timeout=1800):
+    """Runs the C++ API driver; returns its JSON line (dict)."""
+    import json
+    import subprocess
+    from .build import DRIVER_BIN
+    r = subprocess.run([DRIVER_BIN] + [str(a) for a in args], capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError("api_bench failed (%d): %s%s" % (r.returncode, r.stdout, r.stderr))
+    return json.loads(r.stdout.strip().splitlines()[-1])

@@ -402,6 +402,110 @@ static void test_gates(QTNHEnv& env) {
   REQUIRE(utils::equal(phi->at({0, 1, 0}), s * psi[0] - s * psi[2], 1e-12));
 }
 
+// Plain-loop application of a k-qubit SymmTensor gate (els[in, out]) to a state of n
+// qubits (index q = axis q, row-major): the definition of the in-place rule.
+static std::vector<tel> apply_plain(const std::vector<tel>& psi, int n, const std::vector<int>& qs,
+                                    const std::vector<tel>& els) {
+  const int k = (int)qs.size(), D = 1 << k;
+  std::vector<tel> out(psi.size(), 0.0);
+  for (std::size_t x = 0; x < psi.size(); ++x) {
+    int o = 0;
+    for (int m = 0; m < k; ++m) o = o * 2 + (int)((x >> (n - 1 - qs[m])) & 1);
+    for (int i = 0; i < D; ++i) {
+      std::size_t y = x;
+      for (int m = 0; m < k; ++m) {
+        const int bit = (i >> (k - 1 - m)) & 1;
+        const std::size_t mask = (std::size_t)1 << (n - 1 - qs[m]);
+        y = bit ? (y | mask) : (y & ~mask);
+      }
+      out[x] += els[(std::size_t)i * D + o] * psi[y];
+    }
+  }
+  return out;
+}
+
+// Gates and diagonals contracted in place are queued on the state (DeviceArray::defer) and
+// applied, fused, when the elements are next used: every kind of use must see them all, in
+// order, and host edits made in between must stay in sequence with them.
+static void test_queued_contractions(QTNHEnv& env) {
+  g_case = "queued";
+  const int n = 8;
+  const std::size_t N = (std::size_t)1 << n;
+  std::vector<tel> psi(N);
+  for (std::size_t i = 0; i < N; ++i) psi[i] = tel(std::cos(0.37 * i + 0.1), std::sin(1.3 * i));
+  auto gate = [](int seed) {
+    std::vector<tel> g(16);
+    for (int i = 0; i < 16; ++i) g[i] = tel(std::sin(0.9 * i + seed), std::cos(0.4 * i * seed + 1.0));
+    return g;
+  };
+  auto close = [&](Tensor& t, const std::vector<tel>& ref) {
+    bool ok = true;
+    for (std::size_t i = 0; i < N; ++i) ok = ok && utils::equal(t.at(utils::i_to_idxs(i, t.totDims())), ref[i], 1e-12);
+    return ok;
+  };
+  // four two-qubit gates (two disjoint pairs, then overlapping), a one-index diagonal run
+  // and a two-index diagonal, read back through at()
+  const std::vector<std::vector<int>> qs = {{0, 5}, {2, 3}, {5, 1}, {7, 6}, {3, 0}};
+  tptr st = DenseTensor::make(env, {}, tidx_tup(n, 2), std::vector<tel>(psi));
+  std::vector<tel> ref = psi;
+  for (std::size_t g = 0; g < qs.size(); ++g) {
+    st = Tensor::contract(std::move(st), SymmTensor::make(env, {}, {2, 2, 2, 2}, 0, gate((int)g)),
+                          {{(tidx_tup_st)qs[g][0], 0}, {(tidx_tup_st)qs[g][1], 1}});
+    ref = apply_plain(ref, n, qs[g], gate((int)g));
+  }
+  for (int q : {1, 4, 6}) {
+    const std::vector<tel> d = {std::exp(0.3i * (double)q), std::exp(-1.1i * (double)q)};
+    st = Tensor::contract(std::move(st), DiagTensor::make(env, {}, {2, 2}, 0, false, std::vector<tel>(d)),
+                          {{(tidx_tup_st)q, 0}});
+    ref = apply_plain(ref, n, {q}, {d[0], 0.0, 0.0, d[1]});
+  }
+  const std::vector<tel> d2 = {1.0, std::exp(0.7i), std::exp(-0.2i), -1.0};
+  st = Tensor::contract(std::move(st), DiagTensor::make(env, {}, {2, 2, 2, 2}, 0, false, std::vector<tel>(d2)),
+                        {{2, 0}, {7, 1}});
+  std::vector<tel> e2(16, 0.0);
+  for (int i = 0; i < 4; ++i) e2[i * 4 + i] = d2[i];
+  ref = apply_plain(ref, n, {2, 7}, e2);
+  REQUIRE(close(*st, ref));
+  // a host edit between queued gates, then copy() of a tensor with queued gates
+  static_cast<DenseTensor*>(st.get())->put(utils::i_to_idxs(5, st->totDims()), tel(0.25, -0.5));
+  ref[5] = tel(0.25, -0.5);
+  st = Tensor::contract(std::move(st), SymmTensor::make(env, {}, {2, 2, 2, 2}, 0, gate(9)), {{4, 0}, {1, 1}});
+  ref = apply_plain(ref, n, {4, 1}, gate(9));
+  auto cp = st->copy();
+  REQUIRE(close(*cp, ref));
+  REQUIRE(close(*st, ref));
+  // a transform (swap) after queued gates sees them
+  st = Tensor::contract(std::move(st), SymmTensor::make(env, {}, {2, 2, 2, 2}, 0, gate(4)), {{6, 0}, {2, 1}});
+  ref = apply_plain(ref, n, {6, 2}, gate(4));
+  st = Tensor::swap(std::move(st), 0, 3);
+  std::vector<tel> sw(N);
+  for (std::size_t x = 0; x < N; ++x) {
+    auto idx = utils::i_to_idxs(x, tidx_tup(n, 2));
+    std::swap(idx[0], idx[3]);
+    sw[x] = ref[utils::idxs_to_i(idx, tidx_tup(n, 2))];
+  }
+  REQUIRE(close(*st, sw));
+  // a state dropped with gates still queued, then a fresh one: nothing leaks into it
+  {
+    tptr tmp = DenseTensor::make(env, {}, tidx_tup(n, 2), std::vector<tel>(psi));
+    tmp = Tensor::contract(std::move(tmp), SymmTensor::make(env, {}, {2, 2, 2, 2}, 0, gate(2)), {{0, 0}, {1, 1}});
+  }
+  tptr fresh = DenseTensor::make(env, {}, tidx_tup(n, 2), std::vector<tel>(psi));
+  REQUIRE(close(*fresh, psi));
+  // more than the queue's bound (1024) of gates in a row
+  tptr longrun = DenseTensor::make(env, {}, tidx_tup(n, 2), std::vector<tel>(psi));
+  std::vector<tel> lref = psi;
+  for (int g = 0; g < 1100; ++g) {
+    const int a = g % n, b = (g * 3 + 1) % n == a ? (a + 1) % n : (g * 3 + 1) % n;
+    std::vector<tel> u(16, 0.0);  // a phase-and-permutation unitary keeps the norm
+    for (int i = 0; i < 4; ++i) u[i * 4 + ((i + g) % 4)] = std::exp(1i * (0.01 * g + i));
+    longrun = Tensor::contract(std::move(longrun), SymmTensor::make(env, {}, {2, 2, 2, 2}, 0, std::vector<tel>(u)),
+                               {{(tidx_tup_st)a, 0}, {(tidx_tup_st)b, 1}});
+    lref = apply_plain(lref, n, {a, b}, u);
+  }
+  REQUIRE(close(*longrun, lref));
+}
+
 static void test_networks(QTNHEnv& env, std::map<std::string, std::vector<NetCase>>& tn) {
   auto run = [&](const NetCase& c, bool ordered) {
     TensorNetwork net;
@@ -531,6 +635,7 @@ int main(int argc, char** argv) {
     test_scatter(env);
     test_transforms(env);
     test_gates(env);
+    test_queued_contractions(env);
     test_networks(env, tn);
     test_qft(env);
   }

@@ -1,0 +1,229 @@
+// Host-side check of the fixed-point chain of a gate layer (ozaki.cuh, as gate_umma.cu
+// uses it): consecutive fused two-gate passes on one state, the first reading doubles at
+// each group's own exponent and writing doubles (recording the largest exponent), the
+// second reading doubles at that global exponent and writing 64-bit fixed point, the
+// middle ones fixed point to fixed point, the last fixed point to doubles. Every digit
+// product level is summed exactly (here in 64-bit integers), as the tensor cores' FP32
+// accumulators do for K = 32. Compared with long double after every chain, on random
+// states and unitaries, a state with a large spread of magnitudes, and a non-unitary
+// layer. Prints "ok" on success.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <random>
+#include <vector>
+
+#include "ozaki.cuh"
+
+using namespace qtnh_impl;
+typedef long double ld;
+typedef std::complex<double> cd;
+typedef std::complex<ld> cld;
+
+static int fails = 0;
+
+struct State {
+  bool fixed = false;
+  std::vector<cd> d;           // double form
+  std::vector<int64_t> y;      // fixed form: re, im interleaved
+  int F = 0;
+  uint32_t maxhi = 0, maxkey = 0;
+};
+
+static void unitary(std::mt19937_64& rng, int dim, std::vector<cd>& u, double scale) {
+  std::normal_distribution<double> nd(0, 1);
+  u.assign(dim * dim, 0);
+  for (auto& x : u) x = {nd(rng), nd(rng)};
+  for (int a = 0; a < dim; ++a) {
+    for (int b = 0; b < a; ++b) {
+      cd dot = 0;
+      for (int k = 0; k < dim; ++k) dot += std::conj(u[b * dim + k]) * u[a * dim + k];
+      for (int k = 0; k < dim; ++k) u[a * dim + k] -= dot * u[b * dim + k];
+    }
+    double nn = 0;
+    for (int k = 0; k < dim; ++k) nn += std::norm(u[a * dim + k]);
+    for (int k = 0; k < dim; ++k) u[a * dim + k] *= scale / std::sqrt(nn);
+  }
+}
+
+// One fused pass of U16 = Ua (x) Ub on targets t[0..3] (t[0], t[1] for gate a), U[o][i].
+// in_mode: 0 = doubles at each group's exponent, 1 = doubles at the recorded global exponent,
+// 2 = fixed point; out_fixed: write fixed point (else doubles).
+static State pass(const State& in, int n, const int t[4], const std::vector<cd>& Ua, const std::vector<cd>& Ub,
+                  int in_mode, bool out_fixed) {
+  const std::size_t N = (std::size_t)1 << n;
+  cd U[16][16];
+  for (int o = 0; o < 16; ++o)
+    for (int i = 0; i < 16; ++i) U[o][i] = Ua[(o >> 2) * 4 + (i >> 2)] * Ub[(o & 3) * 4 + (i & 3)];
+  double R[32][32];
+  for (int o = 0; o < 16; ++o)
+    for (int i = 0; i < 16; ++i) {
+      R[o][i] = U[o][i].real();
+      R[o][16 + i] = -U[o][i].imag();
+      R[16 + o][i] = U[o][i].imag();
+      R[16 + o][16 + i] = U[o][i].real();
+    }
+  int erow[16], max_erow = 0;
+  float rd[32][32][oz::NS];
+  for (int o = 0; o < 16; ++o) {
+    uint32_t e = 0;
+    for (int i = 0; i < 16; ++i)
+      e = std::max(e, std::max(oz::exponent(df::words(U[o][i].real())), oz::exponent(df::words(U[o][i].imag()))));
+    erow[o] = (int)e;
+    max_erow = std::max(max_erow, (int)e);
+  }
+  for (int r = 0; r < 32; ++r)
+    for (int k = 0; k < 32; ++k) oz::digits(df::words(R[r][k]), oz::digit_scale((uint32_t)erow[r & 15]), rd[r][k]);
+  uint32_t sh = 0;
+  int Ein = 0;
+  if (in_mode == 2) {
+    sh = oz::fixed_shift(in.maxhi);
+    Ein = 1070 + (int)sh - in.F;
+  } else if (in_mode == 1) {
+    Ein = (int)oz::digit_scale(oz::key_exponent(in.maxkey));
+  }
+  State out;
+  out.fixed = out_fixed;
+  out.d.assign(N, 0);
+  out.y.assign(2 * N, 0);
+  out.F = 2100 - Ein - max_erow;
+  const int p[4] = {n - 1 - t[0], n - 1 - t[1], n - 1 - t[2], n - 1 - t[3]};  // bit of target j
+  for (std::size_t base = 0; base < N; ++base) {
+    bool is_base = true;
+    for (int j = 0; j < 4; ++j) is_base = is_base && !((base >> p[j]) & 1);
+    if (!is_base) continue;
+    std::size_t idx[16];
+    for (int c = 0; c < 16; ++c) {
+      idx[c] = base;
+      for (int j = 0; j < 4; ++j)
+        if ((c >> (3 - j)) & 1) idx[c] |= (std::size_t)1 << p[j];
+    }
+    float xd[32][oz::NS];
+    int Eg = Ein;
+    if (in_mode == 0) {
+      uint32_t key = 0;
+      for (int c = 0; c < 16; ++c)
+        key = std::max(key, std::max(oz::group_key(df::words(in.d[idx[c]].real())), oz::group_key(df::words(in.d[idx[c]].imag()))));
+      Eg = (int)oz::key_exponent(key);
+    }
+    for (int c = 0; c < 16; ++c) {
+      if (in_mode == 2) {
+        oz::digits_fixed(in.y[2 * idx[c]], sh, xd[c]);
+        oz::digits_fixed(in.y[2 * idx[c] + 1], sh, xd[16 + c]);
+      } else {
+        const uint32_t es = in_mode == 0 ? oz::digit_scale((uint32_t)Eg) : (uint32_t)Eg;
+        oz::digits(df::words(in.d[idx[c]].real()), es, xd[c]);
+        oz::digits(df::words(in.d[idx[c]].imag()), es, xd[16 + c]);
+      }
+    }
+    for (int r = 0; r < 32; ++r) {
+      long long S[oz::NL] = {0, 0, 0, 0, 0, 0};
+      for (int k = 0; k < 32; ++k)
+        for (int i = 0; i < oz::NS; ++i)
+          for (int j = 0; i + j < oz::NL; ++j) S[i + j] += (long long)rd[r][k][i] * (long long)xd[k][j];
+      float C[oz::NL];
+      for (int l = 0; l < oz::NL; ++l) {
+        if (std::llabs(S[l]) > (1ll << 22)) {
+          std::printf("level sum %lld exceeds 2^22\n", S[l]);
+          ++fails;
+        }
+        C[l] = (float)S[l];
+      }
+      const int o = r & 15;
+      double v;
+      if (in_mode == 0) {
+        v = oz::combine(C, oz::scale_bits(erow[o] + Eg));
+      } else {
+        const int64_t T = oz::fixed_levels(C);
+        if (out_fixed) {
+          const int64_t Y = oz::fixed_round_shift(T, (uint32_t)(max_erow - erow[o]));
+          out.y[2 * idx[o] + (r >= 16)] = Y;
+          out.maxhi = std::max(out.maxhi, oz::fixed_hi_mag(Y));
+          continue;
+        }
+        v = oz::fixed_to_double(T, erow[o] + Ein - 2060);
+      }
+      if (r < 16) out.d[idx[o]].real(v);
+      else out.d[idx[o]].imag(v);
+    }
+  }
+  if (!out_fixed)
+    for (auto& x : out.d)
+      out.maxkey = std::max(out.maxkey, std::max(oz::group_key(df::words(x.real())), oz::group_key(df::words(x.imag()))));
+  return out;
+}
+
+// R passes of a layer as the chain does it; returns the relative L2 error against long double.
+static double chain(std::mt19937_64& rng, int n, int R, double spread, double gscale) {
+  const std::size_t N = (std::size_t)1 << n;
+  std::normal_distribution<double> nd(0, 1);
+  std::uniform_real_distribution<double> ud(-1, 1);
+  State st;
+  st.d.resize(N);
+  for (auto& x : st.d) x = cd(nd(rng), nd(rng)) * std::pow(2.0, std::round(ud(rng) * spread));
+  std::vector<cld> ref(st.d.begin(), st.d.end());
+  for (int pss = 0; pss < R; ++pss) {
+    std::vector<int> qs(n);
+    for (int q = 0; q < n; ++q) qs[q] = q;
+    std::shuffle(qs.begin(), qs.end(), rng);
+    const int t[4] = {qs[0], qs[1], qs[2], qs[3]};
+    std::vector<cd> Ua, Ub;
+    unitary(rng, 4, Ua, gscale);
+    unitary(rng, 4, Ub, 1.0);
+    const int in_mode = pss == 0 ? 0 : (pss == 1 ? 1 : 2);
+    const bool out_fixed = pss > 0 && pss < R - 1;
+    st = pass(st, n, t, Ua, Ub, in_mode, out_fixed);
+    // long double reference of the same pair
+    std::vector<cld> nx(N, 0);
+    const int p[4] = {n - 1 - t[0], n - 1 - t[1], n - 1 - t[2], n - 1 - t[3]};
+    for (std::size_t x = 0; x < N; ++x) {
+      int o = 0;
+      for (int j = 0; j < 4; ++j) o = o * 2 + (int)((x >> p[j]) & 1);
+      for (int i = 0; i < 16; ++i) {
+        std::size_t y = x;
+        for (int j = 0; j < 4; ++j) {
+          const std::size_t m = (std::size_t)1 << p[j];
+          y = ((i >> (3 - j)) & 1) ? (y | m) : (y & ~m);
+        }
+        const cld u = cld(Ua[(o >> 2) * 4 + (i >> 2)]) * cld(Ub[(o & 3) * 4 + (i & 3)]);
+        nx[x] += u * ref[y];
+      }
+    }
+    ref.swap(nx);
+  }
+  ld num = 0, den = 0;
+  for (std::size_t x = 0; x < N; ++x) {
+    num += std::norm(cld(st.d[x]) - ref[x]);
+    den += std::norm(ref[x]);
+  }
+  return (double)std::sqrt(num / den);
+}
+
+int main() {
+  std::mt19937_64 rng(4242);
+  struct Case {
+    const char* what;
+    int n, R;
+    double spread, gscale, bar;
+  } cases[] = {{"7 passes, unitary, Gaussian state", 10, 7, 0, 1.0, 1e-13},
+               {"2 passes (no fixed-point pass)", 9, 2, 0, 1.0, 1e-13},
+               {"3 passes", 9, 3, 0, 1.0, 1e-13},
+               {"state magnitudes spread over 2^+-20", 10, 6, 20, 1.0, 1e-12},
+               {"non-unitary: gate a scaled by 2^12", 9, 5, 0, 4096.0, 1e-13},
+               {"non-unitary: gate a scaled by 2^-30", 9, 5, 0, std::pow(2.0, -30), 1e-13}};
+  for (auto& c : cases) {
+    const double e = chain(rng, c.n, c.R, c.spread, c.gscale);
+    std::printf("%-42s n=%2d passes=%d  rel L2 %.2e\n", c.what, c.n, c.R, e);
+    if (!(e < c.bar)) {
+      std::printf("%s: error above %.0e\n", c.what, c.bar);
+      ++fails;
+    }
+  }
+  if (fails) {
+    std::printf("%d failures\n", fails);
+    return 1;
+  }
+  std::printf("ok\n");
+  return 0;
+}

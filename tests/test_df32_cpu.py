@@ -34,3 +34,14 @@ def test_ozaki_gemm_arithmetic(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "ok" in out.stdout
+
+
+def test_ozaki_fixed_point_chain(tmp_path):
+    """Consecutive fused gate pairs passing the state as 64-bit fixed point (ozaki.cuh, as
+    gate_umma.cu's chain uses it) against long double."""
+    exe = str(tmp_path / "ozaki_chain_check")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "qtnh_gb300", "csrc"),
+                           "-o", exe, os.path.join(HERE, "cpp", "ozaki_chain_check.cpp")])
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "ok" in out.stdout

@@ -536,3 +536,66 @@ def test_gate_pairs_tensor_core_general_gate_and_fallback(bf16x6):
     st = dev(psi)
     q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
     assert rel_l2(host(st), _oracle_layer(psi, n, gates)) < REL_TOL
+
+
+def _disjoint_pairs(nrng, n, npairs):
+    """2 * npairs two-qubit gates; each consecutive pair of gates on four distinct qubits."""
+    gates = []
+    for _ in range(npairs):
+        q4 = [int(x) for x in nrng.choice(n, size=4, replace=False)]
+        gates.append((q4[:2], haar(nrng, 4).T.reshape(-1)))
+        gates.append((q4[2:], haar(nrng, 4).T.reshape(-1)))
+    return gates
+
+
+@pytest.mark.parametrize("n,npairs", [(16, 2), (16, 3), (17, 7), (22, 4)])
+def test_gate_layer_fixed_point_chain_matches_oracle(n, npairs, bf16x6):
+    # a run of fused pairs: the first pass in doubles, the next ones carry the state as
+    # 64-bit fixed point at one scale, the last writes doubles
+    nrng = np.random.default_rng(900 + 10 * n + npairs)
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    psi /= np.linalg.norm(psi)
+    gates = _disjoint_pairs(nrng, n, npairs)
+    st = dev(psi)
+    before = q.launches()
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    assert q.launches() - before == npairs
+    out, ref = host(st), _oracle_layer(psi, n, gates)
+    assert rel_l2(out, ref) < REL_TOL
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < REL_TOL
+
+
+def test_gate_layer_chain_keeps_regions_of_very_different_scale(bf16x6):
+    # a region 2^-40 below the rest: the chain does not start (every nonzero half group
+    # must lie within 2^6 of the largest magnitude), so each region keeps its own accuracy
+    nrng = np.random.default_rng(31)
+    n = 14
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    psi[:4096] *= 2.0 ** -40  # the targets (the four lowest bits) keep groups inside a region
+    gates = [([n - 1, n - 2], haar(nrng, 4).T.reshape(-1)), ([n - 3, n - 4], haar(nrng, 4).T.reshape(-1)),
+             ([n - 1, n - 3], haar(nrng, 4).T.reshape(-1)), ([n - 2, n - 4], haar(nrng, 4).T.reshape(-1)),
+             ([n - 4, n - 1], haar(nrng, 4).T.reshape(-1)), ([n - 3, n - 2], haar(nrng, 4).T.reshape(-1))]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    out, ref = host(st), _oracle_layer(psi, n, gates)
+    assert rel_l2(out[:4096], ref[:4096]) < REL_TOL
+    assert rel_l2(out[4096:], ref[4096:]) < REL_TOL
+
+
+def test_gate_layer_chain_zero_state_and_nonfinite_gate(bf16x6):
+    nrng = np.random.default_rng(32)
+    n = 13
+    gates = _disjoint_pairs(nrng, n, 3)
+    # a zero state stays exactly zero through the chain
+    st = dev(np.zeros(2 ** n, dtype=np.complex128))
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    assert np.all(host(st) == 0)
+    # a gate of the second pair with entries beyond the digit range (1e70 ~ 2^232): that
+    # pass runs every group in FP64 from the fixed-point input and writes doubles, the next
+    # ones (the state now ~1e70) stay in FP64
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    big = [(t, g.copy()) for t, g in gates]
+    big[2] = (big[2][0], big[2][1] * 1e70)
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in big])
+    assert rel_l2(host(st), _oracle_layer(psi, n, big)) < REL_TOL
