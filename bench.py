@@ -85,6 +85,8 @@ def _args():
     p.add_argument("--requests", type=int, default=400)
     p.add_argument("--circuits", type=int, default=2048)
     p.add_argument("--pairs", type=int, default=64)
+    p.add_argument("--max-elems", type=int, default=2 ** 26,
+                   help="contract workload: largest tensor of a pair, in elements (smaller for profiling captures)")
     return p.parse_args()
 
 
@@ -453,7 +455,7 @@ def main_contract(a):
                "sample": "oracle port of _contract_dense, one %dx%dx%d complex contraction on one core" % (M, N, K)}
 
     rng = np.random.default_rng(a.seed)
-    pairs = [wl.dense_pair(rng) for _ in range(a.pairs)]
+    pairs = [wl.dense_pair(rng, max_elems=a.max_elems) for _ in range(a.pairs)]
     g = torch.Generator(device=dev)
     g.manual_seed(a.seed + 1)
     tens = []
@@ -871,6 +873,32 @@ def main_batch(a):
     s_vs_plain = [_state_errors(b.state(i).cpu().numpy(), plain_states[i]) for i in largest]
     del bp
 
+    # the plain method with the fastest plain arithmetic the grouped kernels have: complex128
+    # states, gates in float-float (QTNH_BATCH_GATES=f32x2: FP64-level results at FP32
+    # speed); the reference point of the speed-up beside the FP64 one
+    os.environ["QTNH_BATCH_GATES"] = "f32x2"
+    bq = q.Batch([c.n for c, _ in circuits], precision=q.STATE_C128)
+    g6 = torch.Generator(device=dev)
+    g6.manual_seed(a.seed + 1)
+    for i, (c, qi) in enumerate(circuits):
+        psi = torch.randn(2 ** c.n, dtype=torch.complex128, device=dev, generator=g6)
+        bq.set_state(i, psi / torch.linalg.vector_norm(psi))
+        bq.add_circuit(i, c, qi)
+    bq.compile(renorm_every=0, autotune=True)
+    del os.environ["QTNH_BATCH_GATES"]
+    bq.run()
+    torch.cuda.synchronize()
+    p0.record(stream)
+    for _ in range(a.steps):
+        bq.run()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    ff_ms = p0.elapsed_time(p1) / a.steps
+    ffres = bq.results().cpu().numpy()
+    ff_vs_fp64 = max(float(np.linalg.norm(ffres[offq[i]:offq[i + 1]] - pres[offq[i]:offq[i + 1]]) /
+                           np.linalg.norm(pres[offq[i]:offq[i + 1]])) for i in range(len(circuits)))
+    del bq
+
     # the same complex64 batch with FP32 gate sums (QTNH_BATCH_GATES=fp32): the faster,
     # less accurate point of the trade-off
     os.environ["QTNH_BATCH_GATES"] = "fp32"
@@ -927,6 +955,10 @@ def main_batch(a):
                                               "queries_rel_l2_median": statistics.median(q_vs_plain),
                                               "largest_states": _worst_state_errors(s_vs_plain),
                                               "states_checked": len(s_vs_plain)}},
+            "plain_c128_f32x2": {"value": world * layers / (ff_ms * 1e-3), "unit": "gate-layers/s", "ms_per_step": ff_ms,
+                                 "dtype": "c128 (gates in float-float, same rounds and graph)",
+                                 "speedup_of_mixed": value / (world * layers / (ff_ms * 1e-3)),
+                                 "queries_rel_l2_max_vs_fp64": ff_vs_fp64},
             "fp32_gates": {"value": world * layers / (fp32_ms * 1e-3), "unit": "gate-layers/s", "ms_per_step": fp32_ms,
                            "speedup_of_plain": (world * layers / (fp32_ms * 1e-3)) / plain_value,
                            "vs_plain": {"queries_rel_l2_max": max(f_vs_plain),
@@ -1300,11 +1332,14 @@ def main():
     value = world * a.depth * a.steps / (ms / 1e3)
 
     # roofline of the dominant kernel (two-qubit gate kernel; with bf16x6 the fused
-    # gate-pair kernel, one launch per pair of gates)
+    # gate-pair passes, one launch per pair of gates: the first pass of a run of pairs by
+    # the pair kernel, the others by the fixed-point chain kernel)
     gate_ms = [s.elapsed_time(e) for s, e in events.get("gates", [])]
-    gates_per_call = (a.n // 2 + 1) // 2 if a.arith == "bf16x6" else a.n // 2
-    kernel = {"f32x2": "gate_kernel_f32x2<4>", "fp64": "gate_kernel<4>", "bf16x6": "gate_pair_umma_kernel"}[a.arith]
-    gate_launch_ms = (sum(gate_ms) / len(gate_ms)) / gates_per_call if gate_ms else None
+    launches_per_step = sum(((args[0].value + 1) // 2 if a.arith == "bf16x6" else args[0].value)
+                            for kind, args in dc.steps if kind == "gates")
+    kernel = {"f32x2": "gate_kernel_f32x2<4>", "fp64": "gate_kernel<4>",
+              "bf16x6": "gate_pair_chain_kernel + gate_pair_umma_kernel"}[a.arith]
+    gate_launch_ms = sum(gate_ms) / (a.steps * launches_per_step) if gate_ms else None
     alg_bytes = 32.0 * N
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (gate_launch_ms * 1e-3) / 1e9 if gate_launch_ms else None

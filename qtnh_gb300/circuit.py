@@ -6,7 +6,10 @@ rule, src/tensor/contract.cpp:250-289), one rank-2 DiagTensor contraction per
 qubit for a phase layer, and ``Tensor::rescatter`` / ``Tensor::permute`` /
 ``Tensor::rescatter`` for a redistribution. The runner issues them as the
 batched entry points of the C ABI (qtnh_apply_gate_layer, qtnh_apply_diag_layer,
-qtnh_permute); rescatter is metadata-only with all slabs resident.
+qtnh_permute); rescatter is metadata-only with all slabs resident. The gates of
+consecutive layers with nothing else between them go into one qtnh_apply_gate_layer
+call (in order), as the C++ API's queue of in-place contractions does, so their fused
+passes form one fixed-point chain.
 All argument arrays are built once so the timed loop is only library calls.
 """
 import ctypes
@@ -28,20 +31,30 @@ class DeviceCircuit:
         base = self.gates.data_ptr()
         self.steps = []
         gi = 0
-        for layer in circuit.layers:
-            ng = len(layer.gates)
-            if ng:
+        pending = []  # (pair, gate index) of consecutive gate-only layers
+
+        def flush():
+            if pending:
+                ng = len(pending)
                 ks = (ctypes.c_int32 * ng)(*([2] * ng))
-                tg = _u16([x for p in layer.pairs for x in p])
-                ptrs = (ctypes.c_void_p * ng)(*[base + 16 * 16 * (gi + j) for j in range(ng)])
+                tg = _u16([x for p, _ in pending for x in p])
+                ptrs = (ctypes.c_void_p * ng)(*[base + 16 * 16 * j for _, j in pending])
                 self.steps.append(("gates", (ctypes.c_int32(ng), ks, tg, ptrs)))
-                gi += ng
+                pending.clear()
+
+        for layer in circuit.layers:
+            for j, pr in enumerate(layer.pairs):
+                pending.append((pr, gi + j))
+            gi += len(layer.gates)
+            if layer.phases is not None or layer.ptup is not None:
+                flush()
             if layer.phases is not None:
                 f = torch.from_numpy(phase_factors(layer.phases)).to(device)
                 axes = _u16(range(self.n))
                 self.steps.append(("diag", (ctypes.c_int32(self.n), axes, f)))
             if layer.ptup is not None:
                 self.steps.append(("perm", _u16(layer.ptup)))
+        flush()
         self.layers = len(circuit.layers)
         self.gate_count = gi
 

@@ -110,6 +110,7 @@ struct qtnh_batch {
   void* gates = nullptr;   // c64: U_hi[16], U_lo[16] per gate; c128: U[16]
   grp::FxGate* fx_gates = nullptr;  // c64: the exact fixed-point form (used unless fp32_gates)
   bool fp32_gates = false;          // c64: FP32 gate arithmetic (QTNH_BATCH_GATES=fp32)
+  bool ff_gates = false;            // c128: float-float gate arithmetic (QTNH_BATCH_GATES=f32x2)
   void* tables = nullptr;  // phase tables in the state's type
   double* norms = nullptr;
   uint64_t nnorms = 0;
@@ -182,6 +183,16 @@ struct qtnh_batch {
       case R_GATE: {
         const auto* t = static_cast<const GateTask*>(r.tasks);
         const int g = grid(r.total, r.threads);
+        if (ff_gates) {
+          const double2* gd = static_cast<const double2*>(gates);
+          if (r.threads == 128)
+            grp::ff_gate_kernel<128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gd, ch);
+          else if (r.threads == 512)
+            grp::ff_gate_kernel<512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gd, ch);
+          else
+            grp::ff_gate_kernel<256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gd, ch);
+          break;
+        }
         if (fx_gates && !fp32_gates) {
           if (r.threads == 128)
             grp::fx_gate_kernel<128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
@@ -202,6 +213,16 @@ struct qtnh_batch {
       case R_PAIR: {
         const auto* t = static_cast<const PairTask*>(r.tasks);
         const int g = grid(r.total, r.threads);
+        if (ff_gates) {
+          const double2* gd = static_cast<const double2*>(gates);
+          if (r.threads == 128)
+            grp::ff_pair_kernel<128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gd, ch);
+          else if (r.threads == 512)
+            grp::ff_pair_kernel<512><<<g, 512, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gd, ch);
+          else
+            grp::ff_pair_kernel<256><<<g, 256, 0, s>>>(t, r.cbeg, r.ntasks, r.total, gd, ch);
+          break;
+        }
         if (fx_gates && !fp32_gates) {
           if (r.threads == 128)
             grp::fx_pair_kernel<128><<<g, 128, 0, s>>>(t, r.cbeg, r.ntasks, r.total, fx_gates, ch);
@@ -422,6 +443,8 @@ int qtnh_batch_compile(qtnh_batch* b, int32_t renorm_every, int32_t autotune) {
       std::vector<c128> g;
       for (auto& u : b->gate_host) g.push_back(make_double2(u.real(), u.imag()));
       b->gates = b->upload(g);
+      const char* env = std::getenv("QTNH_BATCH_GATES");
+      b->ff_gates = env && std::string(env) == "f32x2";
     } else {
       std::vector<c64> g;
       for (size_t g0 = 0; g0 < b->gate_host.size(); g0 += 16) {

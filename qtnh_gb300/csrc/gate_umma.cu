@@ -29,6 +29,8 @@
 // groups when the gate has such entries, are computed in FP64 by their two threads.
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "gate_pair.cuh"
 
@@ -408,6 +410,31 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
 }
 
 // ---- a later pass of a gate layer's chain --------------------------------------------
+
+// State digits of the chain passes: six (48 bits of the state's largest magnitude; seven
+// measured 14 % slower per pass). Levels kept: 7 (level 6 = the five digit pairs i + j = 6
+// of the six-by-six product, about 2.5x less error on long chains) or 6
+// (QTNH_CHAIN_LEVELS=6).
+constexpr int CH_ND = oz::NS;
+constexpr int CH_NLMAX = 7;
+
+// Shared memory of a chain CTA: the state digits (K-major core layout as UmSmem), the six
+// gate digits and, for seven levels, a zero seventh block stacked along N (it makes the
+// first MMA write every level block), the stage, the fused gate.
+struct ChSmem {
+  uint8_t adig[CH_ND][2][UM_M * 32];     // state digits: digit, K-step (4 KB each)
+  uint8_t bdig[2][CH_NLMAX][UM_N * 32];  // gate digits: K-step, digit (1 KB each)
+  double2 stage[16][UM_M];              // fetched amplitudes (or fixed-point pairs): amplitude, group
+  double2 U16[256];
+  int32_t erow[16];
+  uint64_t full;
+  uint64_t done;
+  uint32_t tmem_base;
+  int gate_ok;
+  int abort;
+};
+static_assert(CH_NLMAX * UM_N <= UM_COLS, "chain level sums exceed a CTA's TMEM columns");
+static_assert(2 * (sizeof(ChSmem) + 1024) <= 228 * 1024, "two chain CTAs per SM");
 //
 // The input is what the previous pass wrote (rin): doubles with the largest group key of
 // all of them, or 64-bit fixed point at scale rin->F with the largest |hi word|. Both are
@@ -417,7 +444,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
 // When the input is doubles whose largest magnitude lies outside 2^-200..2^201 or the gate
 // has entries the digits cannot carry (then gate_ok is 0), every group is computed in FP64
 // (from the converted fixed-point input where that is the input) and doubles are written.
-template <typename IT, uint32_t MODE>
+template <typename IT, uint32_t MODE, int NL>
 __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __restrict__ psiv,
                                                                         const double2* __restrict__ ga,
                                                                         const double2* __restrict__ gb,
@@ -425,7 +452,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
                                                                         const ChainRec* __restrict__ rin,
                                                                         ChainRec* __restrict__ rout, int want_fixed) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  UmSmem& sm = *reinterpret_cast<UmSmem*>(smem_raw);
+  ChSmem& sm = *reinterpret_cast<ChSmem*>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint64_t ntiles = p.ngroups / UM_M;
   double2* psi = static_cast<double2*>(psiv);
@@ -435,8 +462,8 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
   if (tid == 0) {
     sm.gate_ok = 1;
     sm.abort = 0;
-    mbar_init(&sm.full[0], UM_TEAM);
-    mbar_init(&sm.done[0], 1);
+    mbar_init(&sm.full, UM_TEAM);
+    mbar_init(&sm.done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == UM_WG * 8) {
@@ -466,6 +493,9 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
                                  oz::pack(d[6][j], d[7][j]));
       *reinterpret_cast<uint4*>(&sm.bdig[kc >> 1][j][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) = v;
     }
+    if (NL > oz::NS)  // the seventh gate digit: zero (the first MMA then writes level 6 too)
+      *reinterpret_cast<uint4*>(&sm.bdig[kc >> 1][NL - 1][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) =
+          make_uint4(0u, 0u, 0u, 0u);
   }
   fence_proxy_async();
   tc_fence_before();
@@ -476,12 +506,12 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
   // ---- the scales (the same in every CTA) ----
   const ChainRec ri = *rin;
   const bool in_fixed = ri.fmt == 1;
-  uint32_t sh = 1;
+  int32_t sh = 0;
   int Ein;
   bool in_ok = true;
   if (in_fixed) {
     sh = oz::fixed_shift(ri.maxhi);
-    Ein = 1070 + (int)sh - ri.F;
+    Ein = oz::fixed_exponent(sh, ri.F);
   } else {
     // doubles: one scale for the whole state, if its largest magnitude is in the digit range
     // and (when recorded) no nonzero half group lies more than 2^CHAIN_RANGE below it
@@ -502,8 +532,9 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
   auto tile_of = [&](uint64_t m) -> uint64_t { return (uint64_t)blockIdx.x + m * gridDim.x; };
 
   if (!uni) {
-    // ---- every group in FP64 (no tensor cores): thread per group, doubles out ----
-    uint32_t okey = 0;
+    // ---- every group in FP64 (no tensor cores): thread per group, doubles out; the output
+    // range is recorded like the first pass's, so a later pass starts no chain on it ----
+    uint32_t okey = 0, ominc = 0;
     for (uint64_t g = (uint64_t)blockIdx.x * UM_THREADS + tid; g < p.ngroups; g += (uint64_t)gridDim.x * UM_THREADS) {
       const IT gbase = pair_base<IT>((IT)g, p);
       double2 x[16];
@@ -514,16 +545,25 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
                                        oz::fixed_to_double(psy[2 * (uint64_t)ix + 1], 40 - ri.F))
                         : psi[ix];
       }
+      uint32_t gkey = 0;
 #pragma unroll 1
       for (int o = 0; o < 16; ++o) {
         const double2 v = group_output_fp64(sm.U16, x, o);
-        okey = max(okey, amp_key(v));
+        gkey = max(gkey, amp_key(v));
         psi[gbase + (IT)p.off[o]] = v;
       }
+      okey = max(okey, gkey);
+      if (gkey) ominc = max(ominc, 2047u - oz::key_exponent(gkey));
     }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) okey = max(okey, __shfl_xor_sync(0xffffffffu, okey, o));
-    if (lane == 0 && okey) atomicMax(&rout->maxkey, okey);
+    for (int o = 16; o; o >>= 1) {
+      okey = max(okey, __shfl_xor_sync(0xffffffffu, okey, o));
+      ominc = max(ominc, __shfl_xor_sync(0xffffffffu, ominc, o));
+    }
+    if (lane == 0) {
+      if (okey) atomicMax(&rout->maxkey, okey);
+      if (ominc) atomicMax(&rout->minc, ominc);
+    }
   } else if (warp < UM_WG * 8) {
     // ---- team: fetch, digits at the common scale, recombination, store ----
     const int v = warp & 7, q = v & 3, h = v >> 2;
@@ -533,7 +573,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
       if (T < ntiles) {
         const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
 #pragma unroll
-        for (int c = 8 * h; c < 8 * h + 8; ++c) cp_async16(&sm.stage[0][c][r], psi + (gbase + (IT)p.off[c]));
+        for (int c = 8 * h; c < 8 * h + 8; ++c) cp_async16(&sm.stage[c][r], psi + (gbase + (IT)p.off[c]));
       }
       cp_async_commit();
     };
@@ -544,14 +584,14 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
       cp_async_wait_all();
       double2 x[8];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) x[c] = sm.stage[0][8 * h + c][r];
+      for (int c = 0; c < 8; ++c) x[c] = sm.stage[8 * h + c][r];
       fetch(tile_of(m + 1));  // only this thread reads its stage slots
       // digits of this thread's 16 reals: K core h (real parts of amplitudes 8h..8h+7)
       // and K core 2 + h (their imaginary parts)
 #pragma unroll
       for (int part = 0; part < 2; ++part) {
         const int kc = 2 * part + h;
-        float d[8][oz::NS];
+        float d[8][CH_ND];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const double xv = part ? x[e].y : x[e].x;
@@ -561,15 +601,15 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
             oz::digits(df::words(xv), (uint32_t)Ein, d[e]);
         }
 #pragma unroll
-        for (int j = 0; j < oz::NS; ++j) {
+        for (int j = 0; j < CH_ND; ++j) {
           const uint4 vv = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]),
                                       oz::pack(d[4][j], d[5][j]), oz::pack(d[6][j], d[7][j]));
-          *reinterpret_cast<uint4*>(&sm.adig[0][j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
+          *reinterpret_cast<uint4*>(&sm.adig[j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
         }
       }
       fence_proxy_async();
-      mbar_arrive(&sm.full[0]);
-      if (!mbar_wait_warp(&sm.done[0], it & 1u, &sm.abort)) {
+      mbar_arrive(&sm.full);
+      if (!mbar_wait_warp(&sm.done, it & 1u, &sm.abort)) {
         atomicOr(&g_umma_error, 2u);
         sm.abort = 1;
         break;
@@ -579,19 +619,19 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
 #pragma unroll
       for (int c4 = 0; c4 < 2; ++c4) {
         const int a0 = 8 * h + 4 * c4;
-        uint32_t re[oz::NL][4], im[oz::NL][4];
+        uint32_t re[NL][4], im[NL][4];
 #pragma unroll
-        for (int l = 0; l < oz::NL; ++l) {
+        for (int l = 0; l < NL; ++l) {
           tmem_ld4(tbase + (uint32_t)(32 * l + a0), re[l]);
           tmem_ld4(tbase + (uint32_t)(32 * l + 16 + a0), im[l]);
         }
         tmem_wait_ld();
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-          float lr[oz::NL], li[oz::NL];
+          float lr[NL], li[NL];
 #pragma unroll
-          for (int l = 0; l < oz::NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
-          const int64_t Tr = oz::fixed_levels(lr), Ti = oz::fixed_levels(li);
+          for (int l = 0; l < NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
+          const int64_t Tr = oz::fixed_levels<NL>(lr), Ti = oz::fixed_levels<NL>(li);
           const int o = a0 + a;
           const IT ix = gbase + (IT)p.off[o];
           if (out_fixed) {
@@ -624,25 +664,27 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
     const uint32_t bbase = smem_u32(&sm.bdig[0][0][0]);
     for (uint64_t m = 0; tile_of(m) < ntiles; ++m) {
       const uint32_t it = (uint32_t)m;
-      if (!mbar_wait_warp(&sm.full[0], it & 1u, &sm.abort)) {
+      if (!mbar_wait_warp(&sm.full, it & 1u, &sm.abort)) {
         atomicOr(&g_umma_error, 1u);
         sm.abort = 1;
         break;
       }
       tc_fence_after();
       if (lane == 0) {
-        const uint32_t abase = smem_u32(&sm.adig[0][0][0][0]);
+        const uint32_t abase = smem_u32(&sm.adig[0][0][0]);
+        // state digit j x gate digits 0 .. NL - 1 - j (stacked along N) -> levels j .. NL - 1;
+        // the first MMA (j = 0, all levels) overwrites, the rest accumulate
 #pragma unroll
-        for (int j = 0; j < oz::NS; ++j) {
+        for (int j = 0; j < CH_ND; ++j) {
 #pragma unroll
           for (int ks = 0; ks < 2; ++ks) {
             const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
-            const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * oz::NS * UM_N * 32));
-            umma_bf16(tmem + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (oz::NL - j))),
+            const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * CH_NLMAX * UM_N * 32));
+            umma_bf16(tmem + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (NL - j))),
                       (j | ks) != 0 ? 1u : 0u);
           }
         }
-        umma_commit(&sm.done[0]);
+        umma_commit(&sm.done);
       }
       __syncwarp();
     }
@@ -676,16 +718,25 @@ void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairP
   }
 }
 
-template <typename IT>
+template <typename IT, int NL>
 void launch_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
                   const ChainRec* rin, ChainRec* rout, bool want_fixed) {
-  const size_t smem = sizeof(UmSmem);
-  check_cuda(cudaFuncSetAttribute(gate_pair_chain_kernel<IT, PAIR_KRON>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem),
+  const size_t smem = sizeof(ChSmem);
+  check_cuda(cudaFuncSetAttribute(gate_pair_chain_kernel<IT, PAIR_KRON, NL>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
              "gate_pair_chain_kernel shared memory");
   const uint64_t ntiles = p.ngroups / UM_M;
   const int grid = (int)std::min<uint64_t>(ntiles, 2 * (uint64_t)sm_count());
-  gate_pair_chain_kernel<IT, PAIR_KRON><<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0);
+  gate_pair_chain_kernel<IT, PAIR_KRON, NL>
+      <<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0);
+}
+
+int chain_levels() {
+  static const int nl = [] {
+    const char* e = std::getenv("QTNH_CHAIN_LEVELS");
+    return (e && std::strcmp(e, "6") == 0) ? 6 : 7;
+  }();
+  return nl;
 }
 
 }  // namespace
@@ -694,10 +745,18 @@ bool chain_applies(const PairParams& p) { return p.ngroups >= (uint64_t)UM_M && 
 
 void launch_pair_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
                        const ChainRec* rin, ChainRec* rout, bool want_fixed) {
-  if (p.ngroups * 16 <= (1ull << 32))
-    launch_chain<uint32_t>(psi, ga, gb, p, s, rin, rout, want_fixed);
-  else
-    launch_chain<uint64_t>(psi, ga, gb, p, s, rin, rout, want_fixed);
+  const bool i32 = p.ngroups * 16 <= (1ull << 32);
+  if (chain_levels() == 6) {
+    if (i32)
+      launch_chain<uint32_t, 6>(psi, ga, gb, p, s, rin, rout, want_fixed);
+    else
+      launch_chain<uint64_t, 6>(psi, ga, gb, p, s, rin, rout, want_fixed);
+  } else {
+    if (i32)
+      launch_chain<uint32_t, 7>(psi, ga, gb, p, s, rin, rout, want_fixed);
+    else
+      launch_chain<uint64_t, 7>(psi, ga, gb, p, s, rin, rout, want_fixed);
+  }
 }
 
 bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,

@@ -340,6 +340,205 @@ __device__ __forceinline__ int fx_requant(long long y, int shift) {
 }
 
 // Single two-qubit gate per task, groups of 4 amplitudes (complex64).
+// ---- complex128 states in float-float arithmetic (df32.cuh) ---------------------------
+//
+// The plain method's values (complex128 in and out, ~48-bit products and sums, one FP64
+// add per output component) at FP32 speed: gate entries and amplitudes are split into
+// float pairs, products are exact TwoProducts, sums compensated. A gate with entries
+// outside the split range makes its whole task FP64; a group with amplitudes outside it
+// is computed in FP64 (warp-divergent, rare for normalised states).
+
+struct FfGate {
+  df::cf2 u[16];   // U[out * 4 + in], split
+  double2 d[16];   // the same in FP64
+  int ok;
+};
+
+__device__ __forceinline__ void ff_load_gate(const double2* __restrict__ gates, uint32_t gi, FfGate& g, int j) {
+  const double2 v = gates[(uint64_t)gi * 16 + j];
+  g.d[j] = v;
+  const bool ok = df::in_range_gate(v.x) && df::in_range_gate(v.y);
+  g.u[j] = ok ? df::csplit(v.x, v.y) : df::cf2{{0.f, 0.f}, {0.f, 0.f}};
+  if (!ok) g.ok = 0;
+}
+
+// out = sum_i U[o][i] x[i] over four split inputs, as two accumulators.
+__device__ __forceinline__ void ff_row(const df::cf2* u, const df::cf2 (&x)[4], int o, df::acc& re, df::acc& im) {
+  df::cmul_acc(u[o * 4], x[0], re, im);
+#pragma unroll
+  for (int i = 1; i < 4; ++i) {
+    const df::cf2 g = u[o * 4 + i];
+    df::acc_mac(re, g.re, x[i].re);
+    df::acc_mac(re, df::neg(g.im), x[i].im);
+    df::acc_mac(im, g.re, x[i].im);
+    df::acc_mac(im, g.im, x[i].re);
+  }
+}
+
+__device__ __forceinline__ bool ff_in_range(double2 v) {
+  return df::in_range_state(v.x) && df::in_range_state(v.y);
+}
+
+// One two-qubit gate per task (as gate_kernel) in float-float.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) ff_gate_kernel(const GateTask* __restrict__ tasks,
+                                                          const uint64_t* __restrict__ cbeg, uint32_t ntasks,
+                                                          uint64_t total, const double2* __restrict__ gates,
+                                                          uint64_t chunk_groups) {
+  __shared__ FfGate g;
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) {
+      s_task = find_task(cbeg, ntasks, w);
+      g.ok = 1;
+    }
+    __syncthreads();
+    const GateTask t = tasks[s_task];
+    if (threadIdx.x < 16) ff_load_gate(gates, t.gate, g, threadIdx.x);
+    __syncthreads();
+    double2* psi = static_cast<double2*>(t.psi);
+    const uint64_t ngroups = 1ull << (t.n - 2);
+    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
+    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
+    const uint32_t lo = min(t.ba, t.bb), hi = max(t.ba, t.bb);
+    const uint64_t sa = 1ull << t.ba, sb = 1ull << t.bb;
+    const uint64_t off[4] = {0, sb, sa, sa + sb};
+    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
+      const uint64_t x0 = insert_zero(insert_zero(grp, lo), hi);
+      double2 x[4];
+      bool ok = g.ok != 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        x[i] = psi[x0 + off[i]];
+        ok = ok && ff_in_range(x[i]);
+      }
+      if (ok) {
+        df::cf2 xs[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) xs[i] = df::csplit(x[i].x, x[i].y);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+          df::acc re, im;
+          ff_row(g.u, xs, o, re, im);
+          psi[x0 + off[o]] = make_double2(df::to_double(re), df::to_double(im));
+        }
+      } else {
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+          double re = 0, im = 0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cmac(g.d[o * 4 + i], x[i], re, im);
+          psi[x0 + off[o]] = make_double2(re, im);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Two disjoint gates per task (as pair_kernel) in float-float: gate b on the quadruple of
+// each ia, its outputs kept as split pairs, then gate a on each ib, stored as doubles.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) ff_pair_kernel(const PairTask* __restrict__ tasks,
+                                                          const uint64_t* __restrict__ cbeg, uint32_t ntasks,
+                                                          uint64_t total, const double2* __restrict__ gates,
+                                                          uint64_t chunk_groups) {
+  __shared__ FfGate g[2];
+  __shared__ uint32_t s_task;
+  for (uint64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) {
+      s_task = find_task(cbeg, ntasks, w);
+      g[0].ok = g[1].ok = 1;
+    }
+    __syncthreads();
+    const PairTask t = tasks[s_task];
+    if (threadIdx.x < 32) ff_load_gate(gates, threadIdx.x < 16 ? t.ga : t.gb, g[threadIdx.x >> 4], threadIdx.x & 15);
+    __syncthreads();
+    double2* psi = static_cast<double2*>(t.psi);
+    const uint64_t ngroups = 1ull << (t.n - 4);
+    const uint64_t g0 = (w - cbeg[s_task]) * chunk_groups;
+    const uint64_t g1 = min(g0 + chunk_groups, ngroups);
+    uint32_t pos[4] = {t.a0, t.a1, t.b0, t.b1};
+#pragma unroll
+    for (int i = 1; i < 4; ++i)
+#pragma unroll
+      for (int j = 3; j >= i; --j)
+        if (pos[j - 1] > pos[j]) {
+          const uint32_t tmp = pos[j - 1];
+          pos[j - 1] = pos[j];
+          pos[j] = tmp;
+        }
+    uint64_t offa[4], offb[4];
+    offa[0] = 0, offa[1] = 1ull << t.a1, offa[2] = 1ull << t.a0, offa[3] = offa[1] + offa[2];
+    offb[0] = 0, offb[1] = 1ull << t.b1, offb[2] = 1ull << t.b0, offb[3] = offb[1] + offb[2];
+    const bool gok = g[0].ok != 0 && g[1].ok != 0;
+    for (uint64_t grp = g0 + threadIdx.x; grp < g1; grp += THREADS) {
+      uint64_t x0 = grp;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x0 = insert_zero(x0, pos[i]);
+      double2 x[16];
+      bool ok = gok;
+#pragma unroll
+      for (int ia = 0; ia < 4; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < 4; ++ib) {
+          x[ia * 4 + ib] = psi[x0 + offa[ia] + offb[ib]];
+          ok = ok && ff_in_range(x[ia * 4 + ib]);
+        }
+      if (ok) {
+        df::cf2 xs[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) xs[i] = df::csplit(x[i].x, x[i].y);
+#pragma unroll
+        for (int ia = 0; ia < 4; ++ia) {
+          const df::cf2 in[4] = {xs[ia * 4], xs[ia * 4 + 1], xs[ia * 4 + 2], xs[ia * 4 + 3]};
+#pragma unroll
+          for (int o = 0; o < 4; ++o) {
+            df::acc re, im;
+            ff_row(g[1].u, in, o, re, im);
+            xs[ia * 4 + o] = df::cf2{df::renorm(re), df::renorm(im)};
+          }
+        }
+#pragma unroll
+        for (int ib = 0; ib < 4; ++ib) {
+          const df::cf2 in[4] = {xs[ib], xs[4 + ib], xs[8 + ib], xs[12 + ib]};
+#pragma unroll
+          for (int o = 0; o < 4; ++o) {
+            df::acc re, im;
+            ff_row(g[0].u, in, o, re, im);
+            psi[x0 + offa[o] + offb[ib]] = make_double2(df::to_double(re), df::to_double(im));
+          }
+        }
+      } else {
+        // FP64, as pair_kernel<double2>
+#pragma unroll
+        for (int ia = 0; ia < 4; ++ia) {
+          double2 y[4];
+#pragma unroll
+          for (int o = 0; o < 4; ++o) {
+            double re = 0, im = 0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cmac(g[1].d[o * 4 + i], x[ia * 4 + i], re, im);
+            y[o] = make_double2(re, im);
+          }
+#pragma unroll
+          for (int o = 0; o < 4; ++o) x[ia * 4 + o] = y[o];
+        }
+#pragma unroll
+        for (int ib = 0; ib < 4; ++ib)
+#pragma unroll
+          for (int o = 0; o < 4; ++o) {
+            double re = 0, im = 0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cmac(g[0].d[o * 4 + i], x[i * 4 + ib], re, im);
+            psi[x0 + offa[o] + offb[ib]] = make_double2(re, im);
+          }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) fx_gate_kernel(const GateTask* __restrict__ tasks,
                                                           const uint64_t* __restrict__ cbeg, uint32_t ntasks,

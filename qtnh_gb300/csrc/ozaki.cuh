@@ -117,19 +117,28 @@ DF_HD double combine(const float* C, uint32_t K20) {
 // ---- fixed point between the passes of a gate layer (gate_umma.cu) ----
 //
 // Inside one gate layer the state passes from one fused pass to the next as signed 64-bit
-// fixed point at a common scale, y = Y 2^-F (the pass records F and max |Y|). A pass with
-// such an input cuts every element at one right shift sh (max |Y| < 2^(47 + sh)) into six
-// balanced digits, x ~= m48 2^(sh - F), m48 = round(Y 2^-sh) = sum_j d_j 2^(40 - 8j): the
-// digits of a double at group exponent E with E = 1070 + sh - F (the input's equivalent
-// exponent). The level sums C_l of a row o come back as the exact 64-bit integer
-// T = sum_l C_l 2^(40 - 8l) (|C_l| <= 2^22, so |T| < 2^63), and the output at scale F_out =
-// 2100 - E - max_o erow[o] is Y_o = round(T 2^(erow[o] - max erow)): a right shift, and
+// fixed point at a common scale, y = Y 2^-F (each pass records F and max |Y|). Those
+// passes cut the state at ONE scale for all of it, 2^(E - 1030) with E the input's
+// equivalent exponent, into six balanced digits (48 bits of the largest magnitude):
+// m48 = sum_j d_j 2^(40 - 8j), |m48| <= 2^47:
+//   * fixed point: m48 = round(Y 2^-sh), sh = bits(max |Y|) - 47 (a left shift when not
+//     positive: every pass cuts the largest magnitude just below 2^47, so the scale cannot
+//     drift down from pass to pass), E = 1070 + sh - F;
+//   * doubles (the pass after the first, whose largest exponent was recorded): oz::digits
+//     at E.
+// The gate keeps six digits per row; state digit j meets gate digits 0 .. NL - 1 - j, NL = 6
+// or 7 levels kept (for 7, a zero seventh gate digit block lets the first MMA write level
+// 6 too): the level sums C_0 .. C_(NL-1) are exact in FP32 (|C_l| <= 2^22). T = sum_{l<6}
+// C_l 2^(40 - 8l) (+ round(C_6 2^-8) for NL = 7) is an exact 64-bit integer up to that
+// rounding (|T| < 2^63), the value is T 2^(erow + E - 2100), and the output at scale
+// F_out = 2100 - E - max_o erow[o] is Y_o = round(T 2^(erow[o] - max erow)): a right shift,
 // |Y_o| <= |T|.
 
-// The six balanced digits of the fixed-point value x at right shift sh (1 <= sh < 64),
-// |round(x 2^-sh)| <= 2^47.
-DF_HD void digits_fixed(int64_t x, uint32_t sh, float d[NS]) {
-  const uint64_t mb = (uint64_t)(((x >> (sh - 1u)) + 0x1010101010101ll) >> 1);  // round(x 2^-sh) + B >= 0
+// The six balanced digits of the fixed-point value x at shift sh (-32 < sh < 64; a left
+// shift when sh <= 0), |round(x 2^-sh)| <= 2^47.
+DF_HD void digits_fixed(int64_t x, int32_t sh, float d[NS]) {
+  const int64_t m = sh >= 1 ? (((x >> (sh - 1)) + 1) >> 1) : (int64_t)((uint64_t)x << (uint32_t)(-sh));
+  const uint64_t mb = (uint64_t)m + 0x808080808080ull;  // round(x 2^-sh) + B: bytes - 128 are the digits
   const uint32_t h = (uint32_t)(mb >> 32), l = (uint32_t)mb;
   const float off = -8388736.0f;  // -(2^23 + 128)
   d[0] = df::add(df::u2f(byte_perm(h, 0x4B000000u, 0x7621u)), off);  // bits 40..55 (at most 256)
@@ -140,15 +149,17 @@ DF_HD void digits_fixed(int64_t x, uint32_t sh, float d[NS]) {
   d[5] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7650u)), off);
 }
 
-// The right shift of a fixed-point input whose largest |Y| has its highest set bit in the
-// 32-bit word maxhi (max over elements of |hi word|, see fixed_hi_mag), at least 1: the
+// The shift that puts the largest |Y| of a fixed-point input just below 2^47 (right when
+// positive, left when not), from maxhi = the largest |hi word| (fixed_hi_mag): the
 // magnitude bound is taken as 2^(32 + bit length of maxhi).
-DF_HD uint32_t fixed_shift(uint32_t maxhi) {
-  uint32_t len = 0;
+DF_HD int32_t fixed_shift(uint32_t maxhi) {
+  int32_t len = 0;
   while (len < 32 && (maxhi >> len)) ++len;
-  const int sh = 32 + (int)len - 47;
-  return sh < 1 ? 1u : (uint32_t)sh;
+  return 32 + len - 47;
 }
+
+// The input's equivalent exponent E for shift sh and scale F.
+DF_HD int fixed_exponent(int32_t sh, int32_t F) { return 1070 + sh - F; }
 
 // |hi word| of a 64-bit value (one's complement for negatives: an upper bound of |x| >> 32).
 DF_HD uint32_t fixed_hi_mag(int64_t x) {
@@ -156,16 +167,22 @@ DF_HD uint32_t fixed_hi_mag(int64_t x) {
   return (uint32_t)(hi ^ (hi >> 31));
 }
 
-// Exact T = sum_l C_l 2^(40 - 8l) from the six level sums (exact integers of at most 2^22
-// in magnitude, held in floats): each level is read through the 1.5 2^23 bias (the float's
-// bits minus 0x4B400000), pairs of levels combined in 32 bits, the three pairs in 64 bits.
+// A level sum (an exact integer of at most 2^22 in magnitude, held in a float) as an
+// integer, read through the 1.5 2^23 bias: the float's bits minus 0x4B400000.
+DF_HD int32_t level_int(float c) { return (int32_t)(df::f2u(df::add(c, 12582912.0f)) - 0x4B400000u); }
+
+// T = sum_{l<6} C_l 2^(40 - 8l) (+ round(C_6 2^-8) for NL = 7 levels), exact up to that
+// rounding: pairs of levels combined in 32 bits, the three pairs (and level 6) in 64 bits.
+template <int NL>
 DF_HD int64_t fixed_levels(const float C[NL]) {
+  static_assert(NL == 6 || NL == 7, "six or seven levels");
   int32_t v[NL];
-  for (int l = 0; l < NL; ++l) v[l] = (int32_t)(df::f2u(df::add(C[l], 12582912.0f)) - 0x4B400000u);
+  for (int l = 0; l < NL; ++l) v[l] = level_int(C[l]);
   const int64_t X = (int64_t)(int32_t)((uint32_t)v[0] * 256u + (uint32_t)v[1]);
   const int64_t Y = (int64_t)(int32_t)((uint32_t)v[2] * 256u + (uint32_t)v[3]);
   const int64_t Z = (int64_t)(int32_t)((uint32_t)v[4] * 256u + (uint32_t)v[5]);
-  return (int64_t)((uint64_t)X << 32) + (int64_t)((uint64_t)Y << 16) + Z;
+  const int64_t W = NL == 7 ? (int64_t)((v[NL - 1] + 128) >> 8) : 0;
+  return (int64_t)((uint64_t)X << 32) + (int64_t)((uint64_t)Y << 16) + Z + W;
 }
 
 // round(T 2^-k) for 0 <= k <= 62 (ties up).
@@ -173,8 +190,8 @@ DF_HD int64_t fixed_round_shift(int64_t T, uint32_t k) {
   return k ? ((T + ((int64_t)1 << (k - 1))) >> k) : T;
 }
 
-// T 2^(e - 40) as a double (T from fixed_levels; e = erow + E - 2060): one rounding,
-// then an exact scaling while the result stays a normal double (else scalbn).
+// T 2^(e - 40) as a double (e = erow + E - 2060): one rounding, then an exact scaling
+// while the result stays a normal double (else scalbn).
 DF_HD double fixed_to_double(int64_t T, int e) {
   const double v = (double)T;
   if (v == 0.0) return 0.0;

@@ -187,3 +187,21 @@ def test_batch_rejects_invalid_operations():
         b.add_circuit(1, wl.Circuit(12), queries=[2 ** 12])
     with pytest.raises(q.QtnhError):
         q.Batch([10], precision=7)  # no such state precision
+
+
+def test_plain_batch_float_float_gates_match_oracle(small_batch, monkeypatch):
+    # the plain complex128 schedule with float-float gate arithmetic (QTNH_BATCH_GATES=f32x2,
+    # the grouped pair and single-gate kernels in compensated FP32): every final state within
+    # the contraction bar of the oracle
+    circuits, _, _, refs = small_batch
+    monkeypatch.setenv("QTNH_BATCH_GATES", "f32x2")
+    b = q.Batch([c.n for c, _ in circuits], precision=q.STATE_C128)
+    for i, (c, qi) in enumerate(circuits):
+        b.set_state(i, dev(wl.random_state(c.n, seed=100 + i)))
+        b.add_circuit(i, c, qi)
+    b.compile(renorm_every=0, autotune=True)
+    monkeypatch.delenv("QTNH_BATCH_GATES")
+    b.run()
+    for i, ref in enumerate(refs):
+        assert rel(b.state(i).cpu().numpy(), ref) < 1e-12
+    assert q.take_device_errors() == 0
