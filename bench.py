@@ -1006,7 +1006,12 @@ def main_serve(a):
     reqs = serve.request_stream(a.requests, rate=400.0, seed=a.seed)
     warm = serve.request_stream(4, rate=4000.0, seed=a.seed + 99, qubits=(12, 16), depth=(10, 12))
     out = {}
-    for name, prec in (("mixed", serve.C64), ("plain", serve.C128)):
+    # mixed: complex64 states; plain: complex128 states in FP64; plain_f32x2: complex128
+    # states, gates in float-float (QTNH_BATCH_GATES=f32x2, the fastest plain arithmetic of
+    # the grouped kernels)
+    for name, prec in (("mixed", serve.C64), ("plain", serve.C128), ("plain_f32x2", serve.C128)):
+        if name == "plain_f32x2":
+            os.environ["QTNH_BATCH_GATES"] = "f32x2"
         ex = serve.GpuExecutor(prec)
         serve.serve(warm, ex, renorm_every=8 if prec == serve.C64 else 0)
         torch.cuda.synchronize()
@@ -1017,11 +1022,18 @@ def main_serve(a):
         stats["clocks"] = clocks.stop()
         stats["gpu_launches"] = q.launches() - l0
         out[name] = (stats, results)
+        os.environ.pop("QTNH_BATCH_GATES", None)
     errs = []
     for r in reqs:
         a_, b_ = np.asarray(out["mixed"][1][r.rid]), np.asarray(out["plain"][1][r.rid])
         errs.append(float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_)))
     ms, ps = out["mixed"][0], out["plain"][0]
+    # the same stream at an arrival rate the mixed path sustains (3/4 of its measured
+    # request throughput at 400/s): latency without the queueing of an overloaded stream
+    sus_rate = 0.75 * ms["requests_per_s"]
+    sus_reqs = serve.request_stream(a.requests, rate=sus_rate, seed=a.seed)
+    ex = serve.GpuExecutor(serve.C64)
+    _, _, sus = serve.serve(sus_reqs, ex, budget_bytes=150e9, renorm_every=8)
     if rank == 0:
         gate_bytes = sum(16 * 16 * len(layer.gates) for r in reqs for layer in r.circuit.layers)
         answer_bytes = sum(16 * (256 if r.kind == "amps" else 256) for r in reqs)
@@ -1031,7 +1043,8 @@ def main_serve(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 (mixed) vs c128 (plain)",
             "data": "synthetic (seeded Poisson request stream, seeded circuits and states)",
             "config": {"workload": "%d requests, Poisson arrivals at 400/s, qubits log-uniform 12..26, depth 10..60, "
-                                   "Haar two-qubit gates, phase layer every 4th, qubit exchange every 8th layer, "
+                                   "Haar two-qubit gates, phase layer every 4th, every 8th layer the top 3 indices "
+                                   "exchanged with 3 random local ones, "
                                    "256 amplitudes or a 4-qubit reduced density matrix each; 150 GB admission budget; "
                                    "all active requests advance one layer per grouped step" % len(reqs),
                        "requests": len(reqs), "rate_per_s": 400.0, "budget_bytes": 150e9,
@@ -1040,7 +1053,16 @@ def main_serve(a):
                                          "makespan_s", "steps")},
             "plain": {k: ps[k] for k in ("p50_ms", "p99_ms", "mean_ms", "requests_per_s", "gate_layers_per_s",
                                          "makespan_s", "steps")},
+            "plain_f32x2": dict({k: out["plain_f32x2"][0][k] for k in ("p50_ms", "p99_ms", "mean_ms", "requests_per_s",
+                                                                       "gate_layers_per_s", "makespan_s")},
+                                answers_rel_max_vs_fp64=max(
+                                    float(np.linalg.norm(np.asarray(out["plain_f32x2"][1][r.rid]) -
+                                                         np.asarray(out["plain"][1][r.rid])) /
+                                          np.linalg.norm(np.asarray(out["plain"][1][r.rid]))) for r in reqs)),
             "error_mixed_vs_plain": {"rel_max": max(errs), "rel_median": statistics.median(errs)},
+            "mixed_sustainable_load": dict({k: sus[k] for k in ("p50_ms", "p99_ms", "mean_ms", "requests_per_s",
+                                                                "gate_layers_per_s", "makespan_s")},
+                                           rate_per_s=sus_rate),
             "cpu_baseline": cpu,
             "e2e": {"value": ms["p99_ms"], "unit": "ms", "h2d_bytes_per_step": gate_bytes / max(1, ms["steps"]),
                     "d2h_bytes_per_step": answer_bytes / max(1, ms["steps"])},

@@ -10,6 +10,8 @@
 // contraction of the state with its conjugate, src/tensor/contract.cpp:12-201).
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -218,11 +220,23 @@ void group_layer(int32_t ns, void* const* states, const int32_t* nq, const int32
     }
   }
   up.send(s);
+  // complex128 with QTNH_BATCH_GATES=f32x2: gates in float-float (the plain method's values
+  // at FP32 speed)
+  const char* genv = std::getenv("QTNH_BATCH_GATES");
+  const bool ff = !fx && genv && std::strcmp(genv, "f32x2") == 0;
   try {
     for (auto& r : rounds) {
       const uint64_t* cb = reinterpret_cast<const uint64_t*>(up.dev + r.cbeg);
       const grp::FxGate* fxg = reinterpret_cast<const grp::FxGate*>(up.dev + fx_off);
-      if (fx && r.kind == grp::PAIR)
+      if (ff && r.kind == grp::PAIR)
+        grp::ff_pair_kernel<256><<<grid_items(r.total, 256), 256, 0, s>>>(
+            reinterpret_cast<const grp::PairTask*>(up.dev + r.tasks), cb, r.ntasks, r.total,
+            reinterpret_cast<const double2*>(up.dev + gate_off), G_PAIR_CHUNK);
+      else if (ff && r.kind == grp::GATE)
+        grp::ff_gate_kernel<256><<<grid_items(r.total, 256), 256, 0, s>>>(
+            reinterpret_cast<const grp::GateTask*>(up.dev + r.tasks), cb, r.ntasks, r.total,
+            reinterpret_cast<const double2*>(up.dev + gate_off), G_GATE_CHUNK);
+      else if (fx && r.kind == grp::PAIR)
         grp::fx_pair_kernel<256><<<grid_items(r.total, 256), 256, 0, s>>>(
             reinterpret_cast<const grp::PairTask*>(up.dev + r.tasks), cb, r.ntasks, r.total, fxg, G_PAIR_CHUNK);
       else if (fx && r.kind == grp::GATE)

@@ -2,8 +2,9 @@
 
 Requests arrive as a seeded Poisson stream; each is a layered circuit in the shape of
 the headline workload (Haar two-qubit SymmTensor gates on a random pairing per layer, a
-phase DiagTensor layer every 4th layer, every 8th layer an exchange of a top qubit with a
-random other one) and asks for 256 amplitudes or the reduced density matrix of 4 qubits.
+phase DiagTensor layer every 4th layer, every 8th layer the redistribution of the top 3
+indices: a permutation exchanging them with 3 random local indices, i.e. three disjoint
+qubit exchanges) and asks for 256 amplitudes or the reduced density matrix of 4 qubits.
 The loop admits arrived requests in order while their states fit an HBM budget, keeps
 every admitted state resident, and advances all of them together in work-balanced steps:
 the largest active request advances one layer per step, and every other one as many
@@ -60,10 +61,10 @@ def request_stream(count, rate=400.0, seed=2026, qubits=(12, 26), depth=(10, 60)
             if (layer + 1) % 4 == 0:
                 L.phases = rng.uniform(0.0, 2.0 * math.pi, n)
             if (layer + 1) % 8 == 0:
-                a = int(rng.integers(0, 3))
-                b = int(rng.integers(3, n))
+                local = rng.choice(np.arange(3, n), size=3, replace=False)
                 ptup = list(range(n))
-                ptup[a], ptup[b] = b, a
+                for k3 in range(3):
+                    ptup[k3], ptup[int(local[k3])] = int(local[k3]), k3
                 L.ptup = ptup
             c.layers.append(L)
         if rng.random() < 0.5:
@@ -76,13 +77,19 @@ def request_stream(count, rate=400.0, seed=2026, qubits=(12, 26), depth=(10, 60)
     return out
 
 
-def swap_of(layer):
+def swaps_of(layer):
+    """The layer's permutation as disjoint qubit exchanges [(a, b), ...] (empty when none)."""
     if layer.ptup is None:
-        return None
-    moved = [i for i, p in enumerate(layer.ptup) if p != i]
-    if len(moved) != 2 or layer.ptup[moved[0]] != moved[1]:
-        raise ValueError("a layer's permutation must be one qubit exchange")
-    return moved[0], moved[1]
+        return []
+    out, seen = [], set()
+    for i, p in enumerate(layer.ptup):
+        if p == i or i in seen:
+            continue
+        if layer.ptup[p] != i:
+            raise ValueError("a layer's permutation must be disjoint qubit exchanges")
+        out.append((i, p))
+        seen.update((i, p))
+    return out
 
 
 class GpuExecutor:
@@ -110,9 +117,15 @@ class GpuExecutor:
         return st
 
     def step(self, items):
-        """items: [(state, circuit, layer index)] -> applies that layer to each state."""
+        """items: [(state, circuit, layer index)] -> applies that layer to each state: one
+        grouped call for the gates, phases and first qubit exchange, one more grouped call
+        (exchanges only) for each further exchange of a redistribution."""
+        sw = [swaps_of(c.layers[li]) for _, c, li in items]
         self.q.group_layer(self.precision, [(st, c.n, c.layers[li].pairs, c.layers[li].gates, c.layers[li].phases,
-                                             swap_of(c.layers[li])) for st, c, li in items])
+                                             s[0] if s else None) for (st, c, li), s in zip(items, sw)])
+        for k in range(1, max((len(s) for s in sw), default=0)):
+            more = [(st, c.n, [], [], None, s[k]) for (st, c, _), s in zip(items, sw) if len(s) > k]
+            self.q.group_layer(self.precision, more)
 
     def renorm(self, items):
         self.q.group_renorm(self.precision, [(st, c.n) for st, c in items])

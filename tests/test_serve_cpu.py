@@ -26,8 +26,12 @@ def test_request_stream_shape():
             assert len(set(int(x) for x in r.query)) == 4
         for i, layer in enumerate(r.circuit.layers):
             assert (layer.phases is not None) == ((i + 1) % 4 == 0)
+            assert (layer.ptup is not None) == ((i + 1) % 8 == 0)
             if layer.ptup is not None:
-                assert serve.swap_of(layer) is not None
+                # the redistribution of the headline workload: the top 3 indices exchanged
+                # with 3 distinct local ones, three disjoint qubit exchanges
+                sw = serve.swaps_of(layer)
+                assert len(sw) == 3 and sorted(a for a, _ in sw) == [0, 1, 2] and all(b >= 3 for _, b in sw)
 
 
 class FakeExecutor:
