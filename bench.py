@@ -1368,19 +1368,22 @@ def main():
     share = {k: sum(s.elapsed_time(e) for s, e in v) / ms for k, v in events.items()}
 
     # e2e through the C ABI with host buffers: every step copies its input state from
-    # pinned host memory and its result back, on two copy streams, double-buffered so that
-    # step i+1's input copy and step i's result copy overlap the circuits
+    # pinned host memory and its result back, on two copy streams, with three state buffers
+    # in rotation so that step i+1's input copy and step i-1's result copy both run during
+    # step i, in opposite directions at the same time (with two buffers the input copy
+    # would wait for the result copy that frees its buffer)
+    NB = 3
     h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
-    bufs = [(cur, oth), (torch.empty_like(cur), torch.empty_like(cur))]
-    in_ev = [torch.cuda.Event(), torch.cuda.Event()]
-    free_ev = [torch.cuda.Event(), torch.cuda.Event()]
+    bufs = [(cur, oth)] + [(torch.empty_like(cur), torch.empty_like(cur)) for _ in range(NB - 1)]
+    in_ev = [torch.cuda.Event() for _ in range(NB)]
+    free_ev = [torch.cuda.Event() for _ in range(NB)]
     done_ev = torch.cuda.Event()
 
     def copy_in(i):
-        c = bufs[i % 2][0]
-        h2d_s.wait_event(free_ev[i % 2])  # that buffer's previous result has been copied out
+        c = bufs[i % NB][0]
+        h2d_s.wait_event(free_ev[i % NB])  # that buffer's previous result has been copied out
         q.check(q.lib().qtnh_memcpy_h2d(q._ptr(c), q._ptr(host_in), q.ctypes.c_size_t(16 * N), q._stream(h2d_s)))
-        in_ev[i % 2].record(h2d_s)
+        in_ev[i % NB].record(h2d_s)
 
     for e in free_ev:
         e.record(stream)
@@ -1391,21 +1394,21 @@ def main():
     h2d_s.wait_event(f0)
     copy_in(0)
     for i in range(a.steps):
-        c, o = bufs[i % 2]
-        stream.wait_event(in_ev[i % 2])
+        c, o = bufs[i % NB]
+        stream.wait_event(in_ev[i % NB])
         res = dc.run(c, o)
         done_ev.record(stream)
         if i + 1 < a.steps:
             copy_in(i + 1)
         d2h_s.wait_event(done_ev)
         q.check(q.lib().qtnh_memcpy_d2h(q._ptr(host_out), q._ptr(res), q.ctypes.c_size_t(16 * N), q._stream(d2h_s)))
-        free_ev[i % 2].record(d2h_s)
+        free_ev[i % NB].record(d2h_s)
     stream.wait_stream(d2h_s)
     f1.record(stream)
     torch.cuda.synchronize()
     barrier()
     ems = f0.elapsed_time(f1)
-    last_c, last_o = bufs[(a.steps - 1) % 2]
+    last_c, last_o = bufs[(a.steps - 1) % NB]
     cur, oth = (res, last_o) if res is last_c else (res, last_c)
     del bufs
     if dist is not None:

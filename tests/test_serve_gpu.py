@@ -52,6 +52,21 @@ def test_serve_answers_match_oracle(precision, bar):
     assert q.take_device_errors() == 0
 
 
+def test_serve_plain_float_float_gates_match_oracle(monkeypatch):
+    # complex128 states with the grouped gates in float-float (QTNH_BATCH_GATES=f32x2, read
+    # at every grouped call): the plain bar of 1e-12 against the oracle still holds
+    monkeypatch.setenv("QTNH_BATCH_GATES", "f32x2")
+    reqs = serve.request_stream(10, rate=4000.0, seed=31, qubits=(10, 14), depth=(16, 24))
+    lat, results, stats = serve.serve(reqs, serve.GpuExecutor(serve.C128), budget_bytes=4 * 2 ** 20,
+                                      renorm_every=0, realtime=False)
+    assert stats["requests"] == len(reqs)
+    for r in reqs:
+        got, ref = np.asarray(results[r.rid]), reference(r)
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err < 1e-12, (r.rid, r.kind, r.circuit.n, err)
+    assert q.take_device_errors() == 0
+
+
 @pytest.mark.parametrize("precision,bar", [(serve.C128, 1e-13), (serve.C64, 1e-6)], ids=["plain", "mixed"])
 def test_serve_result_same_alone_and_in_mix(precision, bar):
     # a request's answer does not depend on what else is on the GPU: served in a mix of
