@@ -8,6 +8,8 @@
 // j meets gate digits 0 .. 5 - j in one tcgen05.mma (kind::f16, bf16 operands, FP32
 // accumulators) of N = 32 (6 - j) into columns 32 j ..: 6 digits x 2 K-steps = 12 MMAs.
 //
+// First pass (gate_pair_umma_kernel, below; a later pass of a fixed-point chain has its
+// own pipelined kernel, gate_pair_chain_kernel, further down).
 // CTA = a team of eight warps + one MMA warp; two CTAs per SM (persistent; each holds half
 // of the SM's tensor memory and ~97 KB of shared memory):
 //   * the team handles every tile of its CTA; group r of a tile belongs to two threads
@@ -417,24 +419,32 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
 // (QTNH_CHAIN_LEVELS=6).
 constexpr int CH_ND = oz::NS;
 constexpr int CH_NLMAX = 7;
+constexpr int CH_WARPS = 16;                // team warps: four per TMEM lane quarter
+constexpr int CH_TEAM = CH_WARPS * 32;      // two tiles in flight: digits of one, MMAs of the other
+constexpr int CH_THREADS = CH_TEAM + 32;    // + the MMA warp
+constexpr uint32_t CH_ACC = 256;            // TMEM columns of one accumulator set
+constexpr uint32_t CH_TMEM_COLS = 512;      // two accumulator sets: all of an SM's TMEM
 
-// Shared memory of a chain CTA: the state digits (K-major core layout as UmSmem), the six
-// gate digits and, for seven levels, a zero seventh block stacked along N (it makes the
-// first MMA write every level block), the stage, the fused gate.
+// Shared memory of a chain CTA (one per SM): two buffers of state digits (K-major core
+// layout as UmSmem), the six gate digits and, for seven levels, a zero seventh block
+// stacked along N (it makes the first MMA write every level block), the stage, the
+// fused gate.
 struct ChSmem {
-  uint8_t adig[CH_ND][2][UM_M * 32];     // state digits: digit, K-step (4 KB each)
+  uint8_t adig[2][CH_ND][2][UM_M * 32];  // state digits: buffer, digit, K-step (4 KB each)
   uint8_t bdig[2][CH_NLMAX][UM_N * 32];  // gate digits: K-step, digit (1 KB each)
   double2 stage[16][UM_M];              // fetched amplitudes (or fixed-point pairs): amplitude, group
   double2 U16[256];
   int32_t erow[16];
-  uint64_t full;
-  uint64_t done;
+  uint64_t full[2];                     // digits of the tiles using buffer b are ready
+  uint64_t done[2];                     // MMAs into accumulator set b are complete
   uint32_t tmem_base;
   int gate_ok;
   int abort;
+  int no_abort;                         // stays 0: the final wait for in-flight MMAs
 };
-static_assert(CH_NLMAX * UM_N <= UM_COLS, "chain level sums exceed a CTA's TMEM columns");
-static_assert(2 * (sizeof(ChSmem) + 1024) <= 228 * 1024, "two chain CTAs per SM");
+static_assert(CH_NLMAX * UM_N <= (int)CH_ACC, "chain level sums exceed an accumulator set");
+static_assert(2 * CH_ACC <= CH_TMEM_COLS, "two accumulator sets");
+static_assert(sizeof(ChSmem) + 1024 <= 227 * 1024, "chain shared memory");
 //
 // The input is what the previous pass wrote (rin): doubles with the largest group key of
 // all of them, or 64-bit fixed point at scale rin->F with the largest |hi word|. Both are
@@ -444,8 +454,20 @@ static_assert(2 * (sizeof(ChSmem) + 1024) <= 228 * 1024, "two chain CTAs per SM"
 // When the input is doubles whose largest magnitude lies outside 2^-200..2^201 or the gate
 // has entries the digits cannot carry (then gate_ok is 0), every group is computed in FP64
 // (from the converted fixed-point input where that is the input) and doubles are written.
+//
+// Pipeline (persistent, one CTA per SM): group r of a tile belongs to four threads (warps
+// q, q + 4, q + 8, q + 12 of the lane quarter q = r / 32), each owning 4 of its 16
+// amplitudes. In iteration m the team writes the digits of tile m into digit buffer m % 2
+// and arrives on full[m % 2]; then it waits for the MMAs of tile m - 1 (accumulator set
+// (m - 1) % 2) and recombines and stores that tile. The MMA warp issues tile m's MMAs into
+// accumulator set m % 2 as soon as its digits are complete, so the tensor cores work on
+// tile m while the team recombines tile m - 1: the team never waits for its own MMAs
+// unless they take longer than a digit phase. Buffer reuse: digits of tile m overwrite
+// buffer m % 2 after the team waited (in iteration m - 1) for the MMAs of tile m - 2 that
+// read it; the MMAs of tile m overwrite set m % 2 after every thread arrived on full for
+// tile m, i.e. after its reads of tile m - 2's sums (tcgen05.fence before the arrive).
 template <typename IT, uint32_t MODE, int NL>
-__global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __restrict__ psiv,
+__global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __restrict__ psiv,
                                                                         const double2* __restrict__ ga,
                                                                         const double2* __restrict__ gb,
                                                                         const __grid_constant__ PairParams p,
@@ -462,17 +484,20 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
   if (tid == 0) {
     sm.gate_ok = 1;
     sm.abort = 0;
-    mbar_init(&sm.full, UM_TEAM);
-    mbar_init(&sm.done, 1);
+    sm.no_abort = 0;
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.full[b], CH_TEAM);
+      mbar_init(&sm.done[b], 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == UM_WG * 8) {
+  if (warp == CH_WARPS) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
-                 "r"(UM_TMEM_COLS)
+                 "r"(CH_TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  for (int t = tid; t < 256; t += UM_THREADS) sm.U16[t] = fused_entry<MODE>(ga, gb, t);
+  for (int t = tid; t < 256; t += CH_THREADS) sm.U16[t] = fused_entry<MODE>(ga, gb, t);
   __syncthreads();
   if (tid < 16) {
     bool ok;
@@ -535,7 +560,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
     // ---- every group in FP64 (no tensor cores): thread per group, doubles out; the output
     // range is recorded like the first pass's, so a later pass starts no chain on it ----
     uint32_t okey = 0, ominc = 0;
-    for (uint64_t g = (uint64_t)blockIdx.x * UM_THREADS + tid; g < p.ngroups; g += (uint64_t)gridDim.x * UM_THREADS) {
+    for (uint64_t g = (uint64_t)blockIdx.x * CH_THREADS + tid; g < p.ngroups; g += (uint64_t)gridDim.x * CH_THREADS) {
       const IT gbase = pair_base<IT>((IT)g, p);
       double2 x[16];
 #pragma unroll
@@ -564,36 +589,70 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
       if (okey) atomicMax(&rout->maxkey, okey);
       if (ominc) atomicMax(&rout->minc, ominc);
     }
-  } else if (warp < UM_WG * 8) {
-    // ---- team: fetch, digits at the common scale, recombination, store ----
-    const int v = warp & 7, q = v & 3, h = v >> 2;
-    const int r = q * 32 + lane;  // group row of the tile (TMEM lane)
-    const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16);
+  } else if (warp < CH_WARPS) {
+    // ---- team: fetch, digits at the common scale; recombination and store one tile behind ----
+    const int q = warp & 3, h = warp >> 2;  // lane quarter; this thread's amplitudes 4h .. 4h + 3
+    const int r = q * 32 + lane;            // group row of the tile (TMEM lane)
+    const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16 + (h & 1) * 8);
     auto fetch = [&](uint64_t T) {
       if (T < ntiles) {
         const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
 #pragma unroll
-        for (int c = 8 * h; c < 8 * h + 8; ++c) cp_async16(&sm.stage[c][r], psi + (gbase + (IT)p.off[c]));
+        for (int c = 4 * h; c < 4 * h + 4; ++c) cp_async16(&sm.stage[c][r], psi + (gbase + (IT)p.off[c]));
       }
       cp_async_commit();
     };
-    fetch(tile_of(0));
-    uint32_t it = 0, okey = 0, ohi = 0;
-    for (uint64_t m = 0; tile_of(m) < ntiles; ++m, ++it) {
-      const IT gbase = pair_base<IT>((IT)(tile_of(m) * UM_M + r), p);
-      cp_async_wait_all();
-      double2 x[8];
+    uint32_t okey = 0, ohi = 0;
+    // level sums of tile T from accumulator set b -> the outputs 4h .. 4h + 3 of group r
+    auto recombine = [&](uint64_t T, uint32_t b) {
+      const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * CH_ACC + (uint32_t)(4 * h);
+      uint32_t re[NL][4], im[NL][4];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) x[c] = sm.stage[8 * h + c][r];
+      for (int l = 0; l < NL; ++l) {
+        tmem_ld4(tbase + (uint32_t)(32 * l), re[l]);
+        tmem_ld4(tbase + (uint32_t)(32 * l + 16), im[l]);
+      }
+      tmem_wait_ld();
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        float lr[NL], li[NL];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
+        const int64_t Tr = oz::fixed_levels<NL>(lr), Ti = oz::fixed_levels<NL>(li);
+        const int o = 4 * h + a;
+        const IT ix = gbase + (IT)p.off[o];
+        if (out_fixed) {
+          const uint32_t k = (uint32_t)min(62, max_erow - sm.erow[o]);
+          const int64_t Yr = oz::fixed_round_shift(Tr, k), Yi = oz::fixed_round_shift(Ti, k);
+          ohi = max(ohi, max(oz::fixed_hi_mag(Yr), oz::fixed_hi_mag(Yi)));
+          *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
+        } else {
+          const int e = sm.erow[o] + Ein - 2060;
+          const double2 vv = make_double2(oz::fixed_to_double(Tr, e), oz::fixed_to_double(Ti, e));
+          okey = max(okey, amp_key(vv));
+          psi[ix] = vv;
+        }
+      }
+    };
+    fetch(tile_of(0));
+    uint64_t m = 0;
+    bool ok = true;
+    for (; tile_of(m) < ntiles; ++m) {
+      const uint32_t b = (uint32_t)(m & 1);
+      cp_async_wait_all();
+      double2 x[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) x[c] = sm.stage[4 * h + c][r];
       fetch(tile_of(m + 1));  // only this thread reads its stage slots
-      // digits of this thread's 16 reals: K core h (real parts of amplitudes 8h..8h+7)
-      // and K core 2 + h (their imaginary parts)
+      // digits of this thread's 8 reals: the real parts of amplitudes 4h .. 4h + 3 (K core
+      // h / 2, bytes 8 (h % 2) of each row) and their imaginary parts (K core 2 + h / 2)
 #pragma unroll
       for (int part = 0; part < 2; ++part) {
-        const int kc = 2 * part + h;
-        float d[8][CH_ND];
+        const int kc = 2 * part + (h >> 1);
+        float d[4][CH_ND];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
+        for (int e = 0; e < 4; ++e) {
           const double xv = part ? x[e].y : x[e].x;
           if (in_fixed)
             oz::digits_fixed((int64_t)df::d2u(xv), sh, d[e]);
@@ -602,52 +661,33 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
         }
 #pragma unroll
         for (int j = 0; j < CH_ND; ++j) {
-          const uint4 vv = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]),
-                                      oz::pack(d[4][j], d[5][j]), oz::pack(d[6][j], d[7][j]));
-          *reinterpret_cast<uint4*>(&sm.adig[j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
+          const uint2 vv = make_uint2(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]));
+          *reinterpret_cast<uint2*>(&sm.adig[b][j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
         }
       }
       fence_proxy_async();
-      mbar_arrive(&sm.full);
-      if (!mbar_wait_warp(&sm.done, it & 1u, &sm.abort)) {
+      tc_fence_before();  // this thread's reads of set b (tile m - 2) precede the MMAs of tile m
+      mbar_arrive(&sm.full[b]);
+      if (m >= 1) {
+        if (!mbar_wait_warp(&sm.done[b ^ 1u], (uint32_t)(((m - 1) >> 1) & 1), &sm.abort)) {
+          atomicOr(&g_umma_error, 2u);
+          sm.abort = 1;
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        recombine(tile_of(m - 1), b ^ 1u);
+      }
+    }
+    if (ok && m >= 1) {  // the last tile
+      const uint32_t b = (uint32_t)((m - 1) & 1);
+      if (mbar_wait_warp(&sm.done[b], (uint32_t)(((m - 1) >> 1) & 1), &sm.abort)) {
+        tc_fence_after();
+        recombine(tile_of(m - 1), b);
+      } else {
         atomicOr(&g_umma_error, 2u);
         sm.abort = 1;
-        break;
       }
-      tc_fence_after();
-      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
-#pragma unroll
-      for (int c4 = 0; c4 < 2; ++c4) {
-        const int a0 = 8 * h + 4 * c4;
-        uint32_t re[NL][4], im[NL][4];
-#pragma unroll
-        for (int l = 0; l < NL; ++l) {
-          tmem_ld4(tbase + (uint32_t)(32 * l + a0), re[l]);
-          tmem_ld4(tbase + (uint32_t)(32 * l + 16 + a0), im[l]);
-        }
-        tmem_wait_ld();
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          float lr[NL], li[NL];
-#pragma unroll
-          for (int l = 0; l < NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
-          const int64_t Tr = oz::fixed_levels<NL>(lr), Ti = oz::fixed_levels<NL>(li);
-          const int o = a0 + a;
-          const IT ix = gbase + (IT)p.off[o];
-          if (out_fixed) {
-            const uint32_t k = (uint32_t)min(62, max_erow - sm.erow[o]);
-            const int64_t Yr = oz::fixed_round_shift(Tr, k), Yi = oz::fixed_round_shift(Ti, k);
-            ohi = max(ohi, max(oz::fixed_hi_mag(Yr), oz::fixed_hi_mag(Yi)));
-            *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
-          } else {
-            const int e = sm.erow[o] + Ein - 2060;
-            const double2 vv = make_double2(oz::fixed_to_double(Tr, e), oz::fixed_to_double(Ti, e));
-            okey = max(okey, amp_key(vv));
-            psi[ix] = vv;
-          }
-        }
-      }
-      tc_fence_before();
     }
     cp_async_wait_all();
 #pragma unroll
@@ -660,18 +700,19 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
       if (ohi) atomicMax(&rout->maxhi, ohi);
     }
   } else {
-    // ---- MMA warp: one elected thread issues each tile's 12 MMAs ----
+    // ---- MMA warp: one elected thread issues each tile's 12 MMAs into set m % 2 ----
     const uint32_t bbase = smem_u32(&sm.bdig[0][0][0]);
+    uint64_t issued = 0;
     for (uint64_t m = 0; tile_of(m) < ntiles; ++m) {
-      const uint32_t it = (uint32_t)m;
-      if (!mbar_wait_warp(&sm.full, it & 1u, &sm.abort)) {
+      const uint32_t b = (uint32_t)(m & 1);
+      if (!mbar_wait_warp(&sm.full[b], (uint32_t)((m >> 1) & 1), &sm.abort)) {
         atomicOr(&g_umma_error, 1u);
         sm.abort = 1;
         break;
       }
       tc_fence_after();
       if (lane == 0) {
-        const uint32_t abase = smem_u32(&sm.adig[0][0][0]);
+        const uint32_t abase = smem_u32(&sm.adig[b][0][0][0]);
         // state digit j x gate digits 0 .. NL - 1 - j (stacked along N) -> levels j .. NL - 1;
         // the first MMA (j = 0, all levels) overwrites, the rest accumulate
 #pragma unroll
@@ -680,22 +721,26 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_chain_kernel(void* __
           for (int ks = 0; ks < 2; ++ks) {
             const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
             const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * CH_NLMAX * UM_N * 32));
-            umma_bf16(tmem + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (NL - j))),
+            umma_bf16(tmem + b * CH_ACC + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (NL - j))),
                       (j | ks) != 0 ? 1u : 0u);
           }
         }
-        umma_commit(&sm.done);
+        umma_commit(&sm.done[b]);
       }
       __syncwarp();
+      issued = m + 1;
     }
+    // the team may have stopped early: let the last issued MMAs finish before tensor memory
+    // is freed (no commit on that barrier follows, so its phase parity is stable)
+    if (issued) mbar_wait_warp(&sm.done[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), &sm.no_abort);
   }
 
   // ---- teardown: all tensor-memory reads are done; free it ----
   tc_fence_before();
   __syncthreads();
-  if (warp == UM_WG * 8) {
+  if (warp == CH_WARPS) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(CH_TMEM_COLS) : "memory");
   }
 }
 
@@ -726,9 +771,9 @@ void launch_chain(void* psi, const double2* ga, const double2* gb, const PairPar
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
              "gate_pair_chain_kernel shared memory");
   const uint64_t ntiles = p.ngroups / UM_M;
-  const int grid = (int)std::min<uint64_t>(ntiles, 2 * (uint64_t)sm_count());
+  const int grid = (int)std::min<uint64_t>(ntiles, (uint64_t)sm_count());  // one CTA per SM (all its TMEM)
   gate_pair_chain_kernel<IT, PAIR_KRON, NL>
-      <<<grid, UM_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0);
+      <<<grid, CH_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0);
 }
 
 int chain_levels() {
