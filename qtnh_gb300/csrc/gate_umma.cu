@@ -594,18 +594,27 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     const int q = warp & 3, h = warp >> 2;  // lane quarter; this thread's amplitudes 4h .. 4h + 3
     const int r = q * 32 + lane;            // group row of the tile (TMEM lane)
     const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16 + (h & 1) * 8);
-    auto fetch = [&](uint64_t T) {
+    // group base of row r of tile T = pair_base(T * 128) | pair_base(r): zero bits are inserted
+    // into the tile's bits and the row's bits of the group index independently
+    const IT rbase = pair_base<IT>((IT)r, p);
+    auto tile_part = [&](uint64_t T) -> IT { return pair_base<IT>((IT)(T * UM_M), p); };
+    // per output 4h + a: the row shift to the common output scale (fixed point), 8 bits each
+    uint32_t kk = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) kk |= (uint32_t)min(62, max_erow - sm.erow[4 * h + a]) << (8 * a);
+    auto fetch = [&](uint64_t T, IT tb) {
       if (T < ntiles) {
-        const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
+        const IT gbase = tb | rbase;
 #pragma unroll
         for (int c = 4 * h; c < 4 * h + 4; ++c) cp_async16(&sm.stage[c][r], psi + (gbase + (IT)p.off[c]));
       }
       cp_async_commit();
     };
     uint32_t okey = 0, ohi = 0;
-    // level sums of tile T from accumulator set b -> the outputs 4h .. 4h + 3 of group r
-    auto recombine = [&](uint64_t T, uint32_t b) {
-      const IT gbase = pair_base<IT>((IT)(T * UM_M + r), p);
+    // level sums from accumulator set b -> the outputs 4h .. 4h + 3 of group r of the tile
+    // whose tile part is tb
+    auto recombine = [&](IT tb, uint32_t b) {
+      const IT gbase = tb | rbase;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * CH_ACC + (uint32_t)(4 * h);
       uint32_t re[NL][4], im[NL][4];
 #pragma unroll
@@ -616,26 +625,28 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
       tmem_wait_ld();
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        float lr[NL], li[NL];
+        uint32_t br[NL], bi[NL];
 #pragma unroll
-        for (int l = 0; l < NL; ++l) lr[l] = __uint_as_float(re[l][a]), li[l] = __uint_as_float(im[l][a]);
-        const int64_t Tr = oz::fixed_levels<NL>(lr), Ti = oz::fixed_levels<NL>(li);
-        const int o = 4 * h + a;
-        const IT ix = gbase + (IT)p.off[o];
+        for (int l = 0; l < NL; ++l)
+          br[l] = oz::level_bits(__uint_as_float(re[l][a])), bi[l] = oz::level_bits(__uint_as_float(im[l][a]));
+        const int64_t Tr = oz::fixed_levels_bits<NL>(br), Ti = oz::fixed_levels_bits<NL>(bi);
+        const IT ix = gbase + (IT)p.off[4 * h + a];
         if (out_fixed) {
-          const uint32_t k = (uint32_t)min(62, max_erow - sm.erow[o]);
-          const int64_t Yr = oz::fixed_round_shift(Tr, k), Yi = oz::fixed_round_shift(Ti, k);
+          const uint32_t k = (kk >> (8 * a)) & 0xFFu;
+          const int64_t rh = ((int64_t)1 << k) >> 1;  // rounding half (0 for no shift)
+          const int64_t Yr = (Tr + rh) >> k, Yi = (Ti + rh) >> k;
           ohi = max(ohi, max(oz::fixed_hi_mag(Yr), oz::fixed_hi_mag(Yi)));
           *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
         } else {
-          const int e = sm.erow[o] + Ein - 2060;
+          const int e = sm.erow[4 * h + a] + Ein - 2060;
           const double2 vv = make_double2(oz::fixed_to_double(Tr, e), oz::fixed_to_double(Ti, e));
           okey = max(okey, amp_key(vv));
           psi[ix] = vv;
         }
       }
     };
-    fetch(tile_of(0));
+    IT tb_cur = tile_part(tile_of(0)), tb_prev = 0;
+    fetch(tile_of(0), tb_cur);
     uint64_t m = 0;
     bool ok = true;
     for (; tile_of(m) < ntiles; ++m) {
@@ -644,7 +655,8 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
       double2 x[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) x[c] = sm.stage[4 * h + c][r];
-      fetch(tile_of(m + 1));  // only this thread reads its stage slots
+      const IT tb_next = tile_part(tile_of(m + 1));
+      fetch(tile_of(m + 1), tb_next);  // only this thread reads its stage slots
       // digits of this thread's 8 reals: the real parts of amplitudes 4h .. 4h + 3 (K core
       // h / 2, bytes 8 (h % 2) of each row) and their imaginary parts (K core 2 + h / 2)
 #pragma unroll
@@ -676,14 +688,16 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
           break;
         }
         tc_fence_after();
-        recombine(tile_of(m - 1), b ^ 1u);
+        recombine(tb_prev, b ^ 1u);
       }
+      tb_prev = tb_cur;
+      tb_cur = tb_next;
     }
     if (ok && m >= 1) {  // the last tile
       const uint32_t b = (uint32_t)((m - 1) & 1);
       if (mbar_wait_warp(&sm.done[b], (uint32_t)(((m - 1) >> 1) & 1), &sm.abort)) {
         tc_fence_after();
-        recombine(tile_of(m - 1), b);
+        recombine(tb_prev, b);
       } else {
         atomicOr(&g_umma_error, 2u);
         sm.abort = 1;

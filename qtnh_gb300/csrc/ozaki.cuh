@@ -171,18 +171,32 @@ DF_HD uint32_t fixed_hi_mag(int64_t x) {
 // integer, read through the 1.5 2^23 bias: the float's bits minus 0x4B400000.
 DF_HD int32_t level_int(float c) { return (int32_t)(df::f2u(df::add(c, 12582912.0f)) - 0x4B400000u); }
 
+// The biased bits of a level sum c (|c| < 2^22): c + 1.5 2^23 is exact and its bits are
+// 0x4B400000 + c.
+DF_HD uint32_t level_bits(float c) { return df::f2u(df::add(c, 12582912.0f)); }
+
 // T = sum_{l<6} C_l 2^(40 - 8l) (+ round(C_6 2^-8) for NL = 7 levels), exact up to that
-// rounding: pairs of levels combined in 32 bits, the three pairs (and level 6) in 64 bits.
+// rounding, from the biased bits B_l = 0x4B400000 + C_l of the level sums (|C_l| < 2^22).
+// A pair of levels is one multiply-add of the biased bits: B_{2i} 256 + B_{2i+1} =
+// 256 C_{2i} + C_{2i+1} + 0x8B400000 (mod 2^32), which lies in (0, 2^32) for |C| < 2^22,
+// so the three pairs enter the 64-bit sum as unsigned words and one constant,
+// 0x8B400000 (2^32 + 2^16 + 1), removes their biases.
+template <int NL>
+DF_HD int64_t fixed_levels_bits(const uint32_t B[NL]) {
+  static_assert(NL == 6 || NL == 7, "six or seven levels");
+  const uint32_t X = B[0] * 256u + B[1];
+  const uint32_t Y = B[2] * 256u + B[3];
+  const uint32_t Z = B[4] * 256u + B[5];
+  const uint64_t W = NL == 7 ? (uint64_t)(int64_t)((int32_t)(B[NL - 1] - 0x4B3FFF80u) >> 8) : 0;  // round(C_6 / 256)
+  const uint64_t KB = 0x8B400000ull * 0x100010001ull;  // mod 2^64
+  return (int64_t)(((uint64_t)X << 32) + ((uint64_t)Y << 16) + (uint64_t)Z + W - KB);
+}
+
 template <int NL>
 DF_HD int64_t fixed_levels(const float C[NL]) {
-  static_assert(NL == 6 || NL == 7, "six or seven levels");
-  int32_t v[NL];
-  for (int l = 0; l < NL; ++l) v[l] = level_int(C[l]);
-  const int64_t X = (int64_t)(int32_t)((uint32_t)v[0] * 256u + (uint32_t)v[1]);
-  const int64_t Y = (int64_t)(int32_t)((uint32_t)v[2] * 256u + (uint32_t)v[3]);
-  const int64_t Z = (int64_t)(int32_t)((uint32_t)v[4] * 256u + (uint32_t)v[5]);
-  const int64_t W = NL == 7 ? (int64_t)((v[NL - 1] + 128) >> 8) : 0;
-  return (int64_t)((uint64_t)X << 32) + (int64_t)((uint64_t)Y << 16) + Z + W;
+  uint32_t B[NL];
+  for (int l = 0; l < NL; ++l) B[l] = level_bits(C[l]);
+  return fixed_levels_bits<NL>(B);
 }
 
 // round(T 2^-k) for 0 <= k <= 62 (ties up).

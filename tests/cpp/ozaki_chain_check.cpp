@@ -210,7 +210,37 @@ static double chain(std::mt19937_64& rng, int n, int R, double spread, double gs
   return (double)std::sqrt(num / den);
 }
 
+// fixed_levels (biased bits, one constant) against the direct integer formula
+// sum_{l<6} C_l 2^(40 - 8l) + floor((C_6 + 128) / 256) over random and extreme level sums
+template <int NL>
+static void check_levels(std::mt19937_64& rng) {
+  const int64_t lim = (1 << 22) - 1;
+  std::uniform_int_distribution<int64_t> U(-lim, lim);
+  for (int it = 0; it < 200000; ++it) {
+    int64_t C[NL];
+    float F[NL];
+    for (int l = 0; l < NL; ++l) {
+      const int kind = (int)(rng() % 8);
+      C[l] = kind == 0 ? lim : kind == 1 ? -lim : kind == 2 ? 0 : U(rng);
+      F[l] = (float)C[l];
+    }
+    int64_t want = 0;
+    for (int l = 0; l < 6; ++l) want += C[l] * ((int64_t)1 << (40 - 8 * l));
+    if (NL == 7) want += (C[NL - 1] + 128) >> 8;
+    const int64_t got = oz::fixed_levels<NL>(F);
+    if (got != want) {
+      if (fails < 5) std::printf("fixed_levels<%d>: %lld != %lld\n", NL, (long long)got, (long long)want);
+      ++fails;
+    }
+  }
+}
+
 int main() {
+  {
+    std::mt19937_64 lr(99);
+    check_levels<7>(lr);
+    check_levels<6>(lr);
+  }
   std::mt19937_64 rng(4242);
   struct Case {
     const char* what;
