@@ -34,6 +34,8 @@
 #include <cstdlib>
 #include <cstring>
 
+#include <cuda_fp16.h>
+
 #include "gate_pair.cuh"
 
 namespace qtnh_impl {
@@ -127,7 +129,7 @@ __host__ __device__ constexpr uint32_t um_idesc(uint32_t n) {
 static_assert(oz::NS == oz::NL, "state digit j meets gate digits 0 .. NL - 1 - j");
 static_assert(UM_N * oz::NL <= 256, "an MMA's N is at most 256");
 
-__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+__device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -392,7 +394,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) gate_pair_umma_kernel(double2* 
           for (int ks = 0; ks < 2; ++ks) {
             const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
             const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * oz::NS * UM_N * 32));
-            umma_bf16(dcol + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (oz::NL - j))),
+            umma_f16(dcol + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (oz::NL - j))),
                       (j | ks) != 0 ? 1u : 0u);
           }
         }
@@ -424,6 +426,24 @@ constexpr int CH_TEAM = CH_WARPS * 32;      // two tiles in flight: digits of on
 constexpr int CH_THREADS = CH_TEAM + 32;    // + the MMA warp
 constexpr uint32_t CH_ACC = 256;            // TMEM columns of one accumulator set
 constexpr uint32_t CH_TMEM_COLS = 512;      // two accumulator sets: all of an SM's TMEM
+
+// The chain's digits are fp16 (both operands, kind::f16; balanced digits, |d| <= 128, are
+// exact in fp16 as in bf16, and fp16 lets byte permutes build them): instruction
+// descriptor with A and B formats F16.
+__host__ __device__ constexpr uint32_t ch_idesc(uint32_t n) {
+  return (1u << 4) | ((n >> 3) << 17) | ((uint32_t)(UM_M >> 4) << 24);
+}
+// Two floats (exact small integers) as an fp16x2 word: lo in the low half.
+__device__ __forceinline__ uint32_t pack_h(float lo, float hi) {
+  const __half2 v = __floats2half2_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+// Both halves minus 1152: the fp16 words of oz::digit_words_fixed -> balanced digits (exact).
+__device__ __forceinline__ uint32_t unbias_h(uint32_t w) {
+  const uint32_t c = 0x64806480u;
+  const __half2 v = __hsub2(*reinterpret_cast<const __half2*>(&w), *reinterpret_cast<const __half2*>(&c));
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
 
 // Shared memory of a chain CTA (one per SM): two buffers of state digits (K-major core
 // layout as UmSmem), the six gate digits and, for seven levels, a zero seventh block
@@ -514,8 +534,8 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     for (int e = 0; e < 8; ++e) oz::digits(df::words(real_form(sm.U16, o, kc * 8 + e)), E, d[e]);
 #pragma unroll
     for (int j = 0; j < oz::NS; ++j) {
-      const uint4 v = make_uint4(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]), oz::pack(d[4][j], d[5][j]),
-                                 oz::pack(d[6][j], d[7][j]));
+      const uint4 v = make_uint4(pack_h(d[0][j], d[1][j]), pack_h(d[2][j], d[3][j]), pack_h(d[4][j], d[5][j]),
+                                 pack_h(d[6][j], d[7][j]));
       *reinterpret_cast<uint4*>(&sm.bdig[kc >> 1][j][(o >> 3) * 256 + (kc & 1) * 128 + (o & 7) * 16]) = v;
     }
     if (NL > oz::NS)  // the seventh gate digit: zero (the first MMA then writes level 6 too)
@@ -662,20 +682,23 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
 #pragma unroll
       for (int part = 0; part < 2; ++part) {
         const int kc = 2 * part + (h >> 1);
-        float d[4][CH_ND];
+        uint32_t wa[CH_ND], wb[CH_ND];  // digit j of amplitudes (0, 1) and (2, 3) as fp16x2
+        if (in_fixed) {
+          const auto v = [&](int e) { return (int64_t)df::d2u(part ? x[e].y : x[e].x); };
+          oz::digit_words_fixed(v(0), v(1), sh, wa);
+          oz::digit_words_fixed(v(2), v(3), sh, wb);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const double xv = part ? x[e].y : x[e].x;
-          if (in_fixed)
-            oz::digits_fixed((int64_t)df::d2u(xv), sh, d[e]);
-          else
-            oz::digits(df::words(xv), (uint32_t)Ein, d[e]);
+          for (int j = 0; j < CH_ND; ++j) wa[j] = unbias_h(wa[j]), wb[j] = unbias_h(wb[j]);
+        } else {
+          float d[4][CH_ND];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) oz::digits(df::words(part ? x[e].y : x[e].x), (uint32_t)Ein, d[e]);
+#pragma unroll
+          for (int j = 0; j < CH_ND; ++j) wa[j] = pack_h(d[0][j], d[1][j]), wb[j] = pack_h(d[2][j], d[3][j]);
         }
 #pragma unroll
-        for (int j = 0; j < CH_ND; ++j) {
-          const uint2 vv = make_uint2(oz::pack(d[0][j], d[1][j]), oz::pack(d[2][j], d[3][j]));
-          *reinterpret_cast<uint2*>(&sm.adig[b][j][kc >> 1][row_off + (kc & 1) * 128]) = vv;
-        }
+        for (int j = 0; j < CH_ND; ++j)
+          *reinterpret_cast<uint2*>(&sm.adig[b][j][kc >> 1][row_off + (kc & 1) * 128]) = make_uint2(wa[j], wb[j]);
       }
       fence_proxy_async();
       tc_fence_before();  // this thread's reads of set b (tile m - 2) precede the MMAs of tile m
@@ -735,7 +758,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
           for (int ks = 0; ks < 2; ++ks) {
             const uint64_t ad = smem_desc(abase + (uint32_t)((j * 2 + ks) * UM_M * 32));
             const uint64_t bd = smem_desc(bbase + (uint32_t)(ks * CH_NLMAX * UM_N * 32));
-            umma_bf16(tmem + b * CH_ACC + (uint32_t)(j * UM_N), ad, bd, um_idesc((uint32_t)(UM_N * (NL - j))),
+            umma_f16(tmem + b * CH_ACC + (uint32_t)(j * UM_N), ad, bd, ch_idesc((uint32_t)(UM_N * (NL - j))),
                       (j | ks) != 0 ? 1u : 0u);
           }
         }

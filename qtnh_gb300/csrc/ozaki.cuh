@@ -136,8 +136,12 @@ DF_HD double combine(const float* C, uint32_t K20) {
 
 // The six balanced digits of the fixed-point value x at shift sh (-32 < sh < 64; a left
 // shift when sh <= 0), |round(x 2^-sh)| <= 2^47.
+DF_HD int64_t fixed_round(int64_t x, int32_t sh) {
+  return sh >= 1 ? (((x >> (sh - 1)) + 1) >> 1) : (int64_t)((uint64_t)x << (uint32_t)(-sh));
+}
+
 DF_HD void digits_fixed(int64_t x, int32_t sh, float d[NS]) {
-  const int64_t m = sh >= 1 ? (((x >> (sh - 1)) + 1) >> 1) : (int64_t)((uint64_t)x << (uint32_t)(-sh));
+  const int64_t m = fixed_round(x, sh);
   const uint64_t mb = (uint64_t)m + 0x808080808080ull;  // round(x 2^-sh) + B: bytes - 128 are the digits
   const uint32_t h = (uint32_t)(mb >> 32), l = (uint32_t)mb;
   const float off = -8388736.0f;  // -(2^23 + 128)
@@ -147,6 +151,29 @@ DF_HD void digits_fixed(int64_t x, int32_t sh, float d[NS]) {
   d[3] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7652u)), off);
   d[4] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7651u)), off);
   d[5] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7650u)), off);
+}
+
+// The six digits of two K-adjacent fixed-point values x0, x1 at shift sh as fp16x2 words
+// still carrying the fp16 offset: half j of word w[j] is 0x6400 | b_j, the fp16 of 1024 + b_j,
+// where b_j is digit j's byte of round(x 2^-sh) + 0x808080808080 (b_0: bits 40..48, at
+// most 256) -- x0 in the low half, x1 in the high half. Subtracting 1152 (0x6480) from both
+// halves (one packed fp16 subtraction, exact) gives the balanced digits b_j - 128 of
+// digits_fixed. Byte permutes only: one to pair the two values' bytes, one per word to put
+// them under the exponent byte 0x64.
+DF_HD void digit_words_fixed(int64_t x0, int64_t x1, int32_t sh, uint32_t w[NS]) {
+  const uint64_t m0 = (uint64_t)fixed_round(x0, sh) + 0x808080808080ull;
+  const uint64_t m1 = (uint64_t)fixed_round(x1, sh) + 0x808080808080ull;
+  const uint32_t l0 = (uint32_t)m0, l1 = (uint32_t)m1, h0 = (uint32_t)(m0 >> 32), h1 = (uint32_t)(m1 >> 32);
+  const uint32_t E = 0x64646464u;
+  const uint32_t pa = byte_perm(l0, l1, 0x5140u);  // bytes 0 and 1 of both: digits 5 and 4
+  const uint32_t pb = byte_perm(l0, l1, 0x7362u);  // bytes 2 and 3: digits 3 and 2
+  const uint32_t pc = byte_perm(h0, h1, 0x5140u);  // bytes 4 and 5: digits 1 and 0 (its low 8 bits)
+  w[5] = byte_perm(pa, E, 0x4140u);
+  w[4] = byte_perm(pa, E, 0x4342u);
+  w[3] = byte_perm(pb, E, 0x4140u);
+  w[2] = byte_perm(pb, E, 0x4342u);
+  w[1] = byte_perm(pc, E, 0x4140u);
+  w[0] = byte_perm(pc, E, 0x4342u) | ((h0 >> 8) & 0x100u) | ((h1 << 8) & 0x1000000u);  // + bit 48 of each
 }
 
 // The shift that puts the largest |Y| of a fixed-point input just below 2^47 (right when

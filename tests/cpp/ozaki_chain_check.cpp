@@ -235,11 +235,44 @@ static void check_levels(std::mt19937_64& rng) {
   }
 }
 
+// digit_words_fixed (fp16 words of two values, before the packed subtraction of 1152)
+// against digits_fixed: every half must be the fp16 of 1024 + (digit + 128)
+static void check_digit_words(std::mt19937_64& rng) {
+  for (int it = 0; it < 200000; ++it) {
+    const int32_t sh = (int32_t)(rng() % 40) - 8;
+    const int64_t lim = (int64_t)1 << 47;  // |round(x 2^-sh)| <= 2^47
+    int64_t x[2];
+    for (int k = 0; k < 2; ++k) {
+      const int kind = (int)(rng() % 6);
+      int64_t m = kind == 0 ? lim : kind == 1 ? -lim : kind == 2 ? lim - 1 : (int64_t)(rng() % (2 * (uint64_t)lim)) - lim;
+      if (sh <= 0) m >>= -sh;  // a left shift must not overflow: x 2^-sh = m
+      x[k] = sh >= 1 ? (int64_t)((uint64_t)m << sh) + (int64_t)(rng() % ((uint64_t)1 << sh)) - ((int64_t)1 << (sh - 1))
+                     : m;
+      if (std::llabs(oz::fixed_round(x[k], sh)) > lim) x[k] = 0;
+    }
+    uint32_t w[oz::NS];
+    oz::digit_words_fixed(x[0], x[1], sh, w);
+    for (int k = 0; k < 2; ++k) {
+      float d[oz::NS];
+      oz::digits_fixed(x[k], sh, d);
+      for (int j = 0; j < oz::NS; ++j) {
+        const uint32_t hbits = (w[j] >> (16 * k)) & 0xFFFFu;
+        const bool ok = (hbits & 0xFC00u) == 0x6400u && (double)(1024 + (int)(hbits & 0x3FFu)) - 1152.0 == (double)d[j];
+        if (!ok) {
+          if (fails < 5) std::printf("digit_words_fixed: x=%lld sh=%d digit %d half %04x vs %g\n", (long long)x[k], sh, j, hbits, d[j]);
+          ++fails;
+        }
+      }
+    }
+  }
+}
+
 int main() {
   {
     std::mt19937_64 lr(99);
     check_levels<7>(lr);
     check_levels<6>(lr);
+    check_digit_words(lr);
   }
   std::mt19937_64 rng(4242);
   struct Case {
