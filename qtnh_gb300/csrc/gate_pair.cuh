@@ -116,7 +116,8 @@ bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const 
 // the chain's records before its first pass).
 struct ChainRec {
   uint32_t maxkey;  // doubles written: the largest oz::group_key of the outputs
-  uint32_t maxhi;   // fixed point written: the largest |hi word| of the outputs
+  uint32_t maxhi;   // fixed point written: a value with the bit length of the largest |hi
+                    // word| of the outputs (an OR of them)
   int32_t F;        // fixed point written: value = Y 2^-F
   int32_t fmt;      // 1: fixed point written, 0: doubles
   uint32_t minc;    // doubles written by the first pass: 2047 - the smallest exponent of a

@@ -148,6 +148,12 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&v)[4]) {
                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
                : "r"(taddr));
 }
+// 8 consecutive 32-bit TMEM columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Largest group key (oz::group_key) of an amplitude's two parts.
@@ -527,11 +533,19 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
   }
   __syncthreads();
   if (tid < 128) {
+    // B row n = output real (amplitude n / 2, real or imaginary part n % 2), K column k = input
+    // real (amplitude k / 2, part k % 2): real and imaginary parts interleaved, so that the
+    // 8 reals of 4 amplitudes are one core-matrix row (state digits) and 8 adjacent columns
+    // (level sums)
     const int o = tid >> 2, kc = tid & 3;
-    const uint32_t E = oz::digit_scale((uint32_t)sm.erow[o & 15]);
+    const int ro = (o & 1) * 16 + (o >> 1);  // the row of the real form R
+    const uint32_t E = oz::digit_scale((uint32_t)sm.erow[o >> 1]);
     float d[8][oz::NS];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) oz::digits(df::words(real_form(sm.U16, o, kc * 8 + e)), E, d[e]);
+    for (int e = 0; e < 8; ++e) {
+      const int k = kc * 8 + e;
+      oz::digits(df::words(real_form(sm.U16, ro, (k & 1) * 16 + (k >> 1))), E, d[e]);
+    }
 #pragma unroll
     for (int j = 0; j < oz::NS; ++j) {
       const uint4 v = make_uint4(pack_h(d[0][j], d[1][j]), pack_h(d[2][j], d[3][j]), pack_h(d[4][j], d[5][j]),
@@ -564,6 +578,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     in_ok = tc_scale_ok(E) && (ri.minc == 0 || (int)E - (2047 - (int)ri.minc) <= CHAIN_RANGE);
     Ein = (int)oz::digit_scale(E);
   }
+  if (in_fixed && sh > 15) in_ok = false;  // (not reached: outputs stay below 2^62, sh <= 15)
   const bool uni = in_ok && sm.gate_ok != 0;
   const bool out_fixed = uni && want_fixed != 0;
   int max_erow = 0;
@@ -613,7 +628,10 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     // ---- team: fetch, digits at the common scale; recombination and store one tile behind ----
     const int q = warp & 3, h = warp >> 2;  // lane quarter; this thread's amplitudes 4h .. 4h + 3
     const int r = q * 32 + lane;            // group row of the tile (TMEM lane)
-    const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16 + (h & 1) * 8);
+    // this thread's 8 reals (amplitudes 4h .. 4h + 3, real and imaginary parts interleaved)
+    // are row r of K core h: K-step h / 2, core h % 2
+    const uint32_t row_off = (uint32_t)((r >> 3) * 256 + (r & 7) * 16 + (h & 1) * 128);
+    const uint64_t cadd = oz::fixed_addend(sh);
     // group base of row r of tile T = pair_base(T * 128) | pair_base(r): zero bits are inserted
     // into the tile's bits and the row's bits of the group index independently
     const IT rbase = pair_base<IT>((IT)r, p);
@@ -635,27 +653,24 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     // whose tile part is tb
     auto recombine = [&](IT tb, uint32_t b) {
       const IT gbase = tb | rbase;
-      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * CH_ACC + (uint32_t)(4 * h);
-      uint32_t re[NL][4], im[NL][4];
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * CH_ACC + (uint32_t)(8 * h);
+      uint32_t v[NL][8];  // level l, output real 8h + 2a + part
 #pragma unroll
-      for (int l = 0; l < NL; ++l) {
-        tmem_ld4(tbase + (uint32_t)(32 * l), re[l]);
-        tmem_ld4(tbase + (uint32_t)(32 * l + 16), im[l]);
-      }
+      for (int l = 0; l < NL; ++l) tmem_ld8(tbase + (uint32_t)(32 * l), v[l]);
       tmem_wait_ld();
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         uint32_t br[NL], bi[NL];
 #pragma unroll
         for (int l = 0; l < NL; ++l)
-          br[l] = oz::level_bits(__uint_as_float(re[l][a])), bi[l] = oz::level_bits(__uint_as_float(im[l][a]));
+          br[l] = oz::level_bits(__uint_as_float(v[l][2 * a])), bi[l] = oz::level_bits(__uint_as_float(v[l][2 * a + 1]));
         const int64_t Tr = oz::fixed_levels_bits<NL>(br), Ti = oz::fixed_levels_bits<NL>(bi);
         const IT ix = gbase + (IT)p.off[4 * h + a];
         if (out_fixed) {
           const uint32_t k = (kk >> (8 * a)) & 0xFFu;
           const int64_t rh = ((int64_t)1 << k) >> 1;  // rounding half (0 for no shift)
           const int64_t Yr = (Tr + rh) >> k, Yi = (Ti + rh) >> k;
-          ohi = max(ohi, max(oz::fixed_hi_mag(Yr), oz::fixed_hi_mag(Yi)));
+          ohi |= oz::fixed_hi_mag(Yr) | oz::fixed_hi_mag(Yi);  // its bit length is the largest's
           *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
         } else {
           const int e = sm.erow[4 * h + a] + Ein - 2060;
@@ -677,29 +692,30 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
       for (int c = 0; c < 4; ++c) x[c] = sm.stage[4 * h + c][r];
       const IT tb_next = tile_part(tile_of(m + 1));
       fetch(tile_of(m + 1), tb_next);  // only this thread reads its stage slots
-      // digits of this thread's 8 reals: the real parts of amplitudes 4h .. 4h + 3 (K core
-      // h / 2, bytes 8 (h % 2) of each row) and their imaginary parts (K core 2 + h / 2)
+      // digits of this thread's 8 reals: digit j of amplitude 4h + a as one fp16x2 word (real,
+      // imaginary); the four words of digit j fill the thread's core-matrix row
+      uint32_t w[4][CH_ND];
+      if (in_fixed) {
 #pragma unroll
-      for (int part = 0; part < 2; ++part) {
-        const int kc = 2 * part + (h >> 1);
-        uint32_t wa[CH_ND], wb[CH_ND];  // digit j of amplitudes (0, 1) and (2, 3) as fp16x2
-        if (in_fixed) {
-          const auto v = [&](int e) { return (int64_t)df::d2u(part ? x[e].y : x[e].x); };
-          oz::digit_words_fixed(v(0), v(1), sh, wa);
-          oz::digit_words_fixed(v(2), v(3), sh, wb);
+        for (int a = 0; a < 4; ++a) {
+          oz::digit_words_biased(oz::fixed_biased((int64_t)df::d2u(x[a].x), sh, cadd),
+                                 oz::fixed_biased((int64_t)df::d2u(x[a].y), sh, cadd), w[a]);
 #pragma unroll
-          for (int j = 0; j < CH_ND; ++j) wa[j] = unbias_h(wa[j]), wb[j] = unbias_h(wb[j]);
-        } else {
-          float d[4][CH_ND];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) oz::digits(df::words(part ? x[e].y : x[e].x), (uint32_t)Ein, d[e]);
-#pragma unroll
-          for (int j = 0; j < CH_ND; ++j) wa[j] = pack_h(d[0][j], d[1][j]), wb[j] = pack_h(d[2][j], d[3][j]);
+          for (int j = 0; j < CH_ND; ++j) w[a][j] = unbias_h(w[a][j]);
         }
+      } else {
 #pragma unroll
-        for (int j = 0; j < CH_ND; ++j)
-          *reinterpret_cast<uint2*>(&sm.adig[b][j][kc >> 1][row_off + (kc & 1) * 128]) = make_uint2(wa[j], wb[j]);
+        for (int a = 0; a < 4; ++a) {
+          float dr[CH_ND], di[CH_ND];
+          oz::digits(df::words(x[a].x), (uint32_t)Ein, dr);
+          oz::digits(df::words(x[a].y), (uint32_t)Ein, di);
+#pragma unroll
+          for (int j = 0; j < CH_ND; ++j) w[a][j] = pack_h(dr[j], di[j]);
+        }
       }
+#pragma unroll
+      for (int j = 0; j < CH_ND; ++j)
+        *reinterpret_cast<uint4*>(&sm.adig[b][j][h >> 1][row_off]) = make_uint4(w[0][j], w[1][j], w[2][j], w[3][j]);
       fence_proxy_async();
       tc_fence_before();  // this thread's reads of set b (tile m - 2) precede the MMAs of tile m
       mbar_arrive(&sm.full[b]);

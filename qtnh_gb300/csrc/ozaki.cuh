@@ -153,16 +153,26 @@ DF_HD void digits_fixed(int64_t x, int32_t sh, float d[NS]) {
   d[5] = df::add(df::u2f(byte_perm(l, 0x4B000000u, 0x7650u)), off);
 }
 
-// The six digits of two K-adjacent fixed-point values x0, x1 at shift sh as fp16x2 words
-// still carrying the fp16 offset: half j of word w[j] is 0x6400 | b_j, the fp16 of 1024 + b_j,
-// where b_j is digit j's byte of round(x 2^-sh) + 0x808080808080 (b_0: bits 40..48, at
-// most 256) -- x0 in the low half, x1 in the high half. Subtracting 1152 (0x6480) from both
-// halves (one packed fp16 subtraction, exact) gives the balanced digits b_j - 128 of
-// digits_fixed. Byte permutes only: one to pair the two values' bytes, one per word to put
-// them under the exponent byte 0x64.
-DF_HD void digit_words_fixed(int64_t x0, int64_t x1, int32_t sh, uint32_t w[NS]) {
-  const uint64_t m0 = (uint64_t)fixed_round(x0, sh) + 0x808080808080ull;
-  const uint64_t m1 = (uint64_t)fixed_round(x1, sh) + 0x808080808080ull;
+// round(x 2^-sh) + 0x808080808080 (the biased value whose bytes minus 128 are the six
+// balanced digits) with the rounding half and the bias folded into one 64-bit addend
+// c = fixed_addend(sh): ((x + c) >> sh) for 1 <= sh <= 15 (x + c then lies in (0, 2^64)
+// while |round(x 2^-sh)| <= 2^47), (x << -sh) + c for sh <= 0.
+DF_HD uint64_t fixed_addend(int32_t sh) {
+  const uint64_t B = 0x808080808080ull;
+  return sh >= 1 ? ((uint64_t)1 << (sh - 1)) + (B << sh) : B;
+}
+DF_HD uint64_t fixed_biased(int64_t x, int32_t sh, uint64_t c) {
+  return sh >= 1 ? ((uint64_t)x + c) >> sh : ((uint64_t)x << (uint32_t)(-sh)) + c;
+}
+
+// The six digits of two K-adjacent values as fp16x2 words still carrying the fp16 offset,
+// from their biased values m0, m1 (fixed_biased): half j of word w[j] is 0x6400 | b_j, the
+// fp16 of 1024 + b_j, where b_j is digit j's byte of m (b_0: bits 40..48, at most 256) --
+// the first value in the low half, the second in the high half. Subtracting 1152 (0x6480)
+// from both halves (one packed fp16 subtraction, exact) gives the balanced digits
+// b_j - 128 of digits_fixed. Byte permutes only: one to pair the two values' bytes, one per
+// word to put them under the exponent byte 0x64.
+DF_HD void digit_words_biased(uint64_t m0, uint64_t m1, uint32_t w[NS]) {
   const uint32_t l0 = (uint32_t)m0, l1 = (uint32_t)m1, h0 = (uint32_t)(m0 >> 32), h1 = (uint32_t)(m1 >> 32);
   const uint32_t E = 0x64646464u;
   const uint32_t pa = byte_perm(l0, l1, 0x5140u);  // bytes 0 and 1 of both: digits 5 and 4
@@ -176,9 +186,15 @@ DF_HD void digit_words_fixed(int64_t x0, int64_t x1, int32_t sh, uint32_t w[NS])
   w[0] = byte_perm(pc, E, 0x4342u) | ((h0 >> 8) & 0x100u) | ((h1 << 8) & 0x1000000u);  // + bit 48 of each
 }
 
+// The same from two fixed-point values x0, x1 at shift sh (1 <= sh <= 15 or sh <= 0).
+DF_HD void digit_words_fixed(int64_t x0, int64_t x1, int32_t sh, uint32_t w[NS]) {
+  const uint64_t c = fixed_addend(sh);
+  digit_words_biased(fixed_biased(x0, sh, c), fixed_biased(x1, sh, c), w);
+}
+
 // The shift that puts the largest |Y| of a fixed-point input just below 2^47 (right when
-// positive, left when not), from maxhi = the largest |hi word| (fixed_hi_mag): the
-// magnitude bound is taken as 2^(32 + bit length of maxhi).
+// positive, left when not), from maxhi, a value with the bit length of the largest |hi
+// word| (fixed_hi_mag): the magnitude bound is taken as 2^(32 + bit length of maxhi).
 DF_HD int32_t fixed_shift(uint32_t maxhi) {
   int32_t len = 0;
   while (len < 32 && (maxhi >> len)) ++len;
