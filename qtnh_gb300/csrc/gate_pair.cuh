@@ -130,6 +130,7 @@ struct ChainRec {
 // magnitude, so every group keeps ~40 bits of its own.
 constexpr int CHAIN_RANGE = 6;
 
+
 // Whether the chain kernel takes a pair of this shape (the tcgen05 tile shape).
 bool chain_applies(const PairParams& p);
 // A later pass of a chain (two disjoint two-qubit gates): reads what rin describes, writes

@@ -532,6 +532,10 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     if (!ok) sm.gate_ok = 0;
   }
   __syncthreads();
+  int max_erow = 0, min_erow = 0x7FFFFFFF;
+#pragma unroll
+  for (int o = 0; o < 16; ++o) max_erow = max(max_erow, sm.erow[o]), min_erow = min(min_erow, sm.erow[o]);
+  const bool common = max_erow - min_erow <= oz::CHAIN_COMMON_SPAN;  // one digit scale for all rows
   if (tid < 128) {
     // B row n = output real (amplitude n / 2, real or imaginary part n % 2), K column k = input
     // real (amplitude k / 2, part k % 2): real and imaginary parts interleaved, so that the
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     // (level sums)
     const int o = tid >> 2, kc = tid & 3;
     const int ro = (o & 1) * 16 + (o >> 1);  // the row of the real form R
-    const uint32_t E = oz::digit_scale((uint32_t)sm.erow[o >> 1]);
+    const uint32_t E = oz::digit_scale((uint32_t)(common ? max_erow : sm.erow[o >> 1]));
     float d[8][oz::NS];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
@@ -581,9 +585,6 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
   if (in_fixed && sh > 15) in_ok = false;  // (not reached: outputs stay below 2^62, sh <= 15)
   const bool uni = in_ok && sm.gate_ok != 0;
   const bool out_fixed = uni && want_fixed != 0;
-  int max_erow = 0;
-#pragma unroll
-  for (int o = 0; o < 16; ++o) max_erow = max(max_erow, sm.erow[o]);
   const int F_out = 2100 - Ein - max_erow;
   if (blockIdx.x == 0 && tid == 0) {
     rout->fmt = out_fixed ? 1 : 0;
@@ -636,10 +637,11 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     // into the tile's bits and the row's bits of the group index independently
     const IT rbase = pair_base<IT>((IT)r, p);
     auto tile_part = [&](uint64_t T) -> IT { return pair_base<IT>((IT)(T * UM_M), p); };
-    // per output 4h + a: the row shift to the common output scale (fixed point), 8 bits each
+    // per output 4h + a: the row shift to the common output scale (fixed point), 8 bits
+    // each, and the row's scale exponent (0 and max_erow when all rows share one scale)
     uint32_t kk = 0;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) kk |= (uint32_t)min(62, max_erow - sm.erow[4 * h + a]) << (8 * a);
+    for (int a = 0; a < 4; ++a) kk |= (common ? 0u : (uint32_t)min(62, max_erow - sm.erow[4 * h + a])) << (8 * a);
     auto fetch = [&](uint64_t T, IT tb) {
       if (T < ntiles) {
         const IT gbase = tb | rbase;
@@ -660,20 +662,27 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
       tmem_wait_ld();
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        uint32_t br[NL], bi[NL];
+        float cr[NL], ci[NL];
 #pragma unroll
-        for (int l = 0; l < NL; ++l)
-          br[l] = oz::level_bits(__uint_as_float(v[l][2 * a])), bi[l] = oz::level_bits(__uint_as_float(v[l][2 * a + 1]));
-        const int64_t Tr = oz::fixed_levels_bits<NL>(br), Ti = oz::fixed_levels_bits<NL>(bi);
+        for (int l = 0; l < NL; ++l) cr[l] = __uint_as_float(v[l][2 * a]), ci[l] = __uint_as_float(v[l][2 * a + 1]);
+        int64_t Tr, Ti;
+        if constexpr (NL == 7) {
+          Tr = oz::fixed_levels_merged(cr), Ti = oz::fixed_levels_merged(ci);
+        } else {
+          Tr = oz::fixed_levels<NL>(cr), Ti = oz::fixed_levels<NL>(ci);
+        }
         const IT ix = gbase + (IT)p.off[4 * h + a];
         if (out_fixed) {
-          const uint32_t k = (kk >> (8 * a)) & 0xFFu;
-          const int64_t rh = ((int64_t)1 << k) >> 1;  // rounding half (0 for no shift)
-          const int64_t Yr = (Tr + rh) >> k, Yi = (Ti + rh) >> k;
+          int64_t Yr = Tr, Yi = Ti;
+          if (!common) {
+            const uint32_t k = (kk >> (8 * a)) & 0xFFu;
+            const int64_t rh = ((int64_t)1 << k) >> 1;  // rounding half (0 for no shift)
+            Yr = (Tr + rh) >> k, Yi = (Ti + rh) >> k;
+          }
           ohi |= oz::fixed_hi_mag(Yr) | oz::fixed_hi_mag(Yi);  // its bit length is the largest's
           *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
         } else {
-          const int e = sm.erow[4 * h + a] + Ein - 2060;
+          const int e = (common ? max_erow : sm.erow[4 * h + a]) + Ein - 2060;
           const double2 vv = make_double2(oz::fixed_to_double(Tr, e), oz::fixed_to_double(Ti, e));
           okey = max(okey, amp_key(vv));
           psi[ix] = vv;

@@ -242,6 +242,24 @@ DF_HD int64_t fixed_levels(const float C[NL]) {
   return fixed_levels_bits<NL>(B);
 }
 
+// A chain pass cuts the gate's digits at one scale for all rows (that of its largest row)
+// when the rows' largest exponents differ by at most CHAIN_COMMON_SPAN: the outputs then
+// come out at the common scale without a per-row shift, and a row keeps at least
+// 48 - CHAIN_COMMON_SPAN bits of its own largest entry. Otherwise each row has its own
+// scale and its outputs are shifted (rounded) to the common one.
+constexpr int CHAIN_COMMON_SPAN = 2;
+
+// Seven level sums with level 6 folded into level 5 in FP32 before the conversion:
+// fma(C_6, 2^-8, C_5) rounded to an integer by the bias addition (|C_5 + C_6 2^-8| < 2^22):
+// T = sum_{l<6} C_l 2^(40 - 8l) + C_6 2^-8 to within one unit of level 5 (2^-40 of level
+// 0; the unmerged form rounds only C_6 2^-8), with six level conversions instead of seven.
+DF_HD int64_t fixed_levels_merged(const float C[7]) {
+  uint32_t B[6];
+  for (int l = 0; l < 5; ++l) B[l] = level_bits(C[l]);
+  B[5] = level_bits(df::fma(C[6], 0.00390625f, C[5]));
+  return fixed_levels_bits<6>(B);
+}
+
 // round(T 2^-k) for 0 <= k <= 62 (ties up).
 DF_HD int64_t fixed_round_shift(int64_t T, uint32_t k) {
   return k ? ((T + ((int64_t)1 << (k - 1))) >> k) : T;

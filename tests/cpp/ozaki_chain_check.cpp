@@ -75,8 +75,13 @@ static State pass(const State& in, int n, const int t[4], const std::vector<cd>&
     erow[o] = (int)e;
     max_erow = std::max(max_erow, (int)e);
   }
+  int min_erow = max_erow;
+  for (int o = 0; o < 16; ++o) min_erow = std::min(min_erow, erow[o]);
+  // chain passes: one digit scale for all rows when their exponents are within the span
+  const bool common = in_mode != 0 && max_erow - min_erow <= oz::CHAIN_COMMON_SPAN;
   for (int r = 0; r < 32; ++r)
-    for (int k = 0; k < 32; ++k) oz::digits(df::words(R[r][k]), oz::digit_scale((uint32_t)erow[r & 15]), rd[r][k]);
+    for (int k = 0; k < 32; ++k)
+      oz::digits(df::words(R[r][k]), oz::digit_scale((uint32_t)(common ? max_erow : erow[r & 15])), rd[r][k]);
   int32_t sh = 0;
   int Ein = 0;
   if (in_mode == 2) {
@@ -144,14 +149,14 @@ static State pass(const State& in, int n, const int t[4], const std::vector<cd>&
       if (in_mode == 0) {
         v = oz::combine(C, oz::scale_bits(erow[o] + Eg));
       } else {
-        const int64_t T = oz::fixed_levels<NL>(C);
+        const int64_t T = NL == 7 ? oz::fixed_levels_merged(C) : oz::fixed_levels<NL>(C);
         if (out_fixed) {
-          const int64_t Y = oz::fixed_round_shift(T, (uint32_t)(max_erow - erow[o]));
+          const int64_t Y = common ? T : oz::fixed_round_shift(T, (uint32_t)(max_erow - erow[o]));
           out.y[2 * idx[o] + (r >= 16)] = Y;
           out.maxhi = std::max(out.maxhi, oz::fixed_hi_mag(Y));
           continue;
         }
-        v = oz::fixed_to_double(T, erow[o] + Ein - 2060);
+        v = oz::fixed_to_double(T, (common ? max_erow : erow[o]) + Ein - 2060);
       }
       if (r < 16) out.d[idx[o]].real(v);
       else out.d[idx[o]].imag(v);
