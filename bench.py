@@ -576,33 +576,39 @@ def main_contract(a):
             t2.data.copy_(hb, non_blocking=True)
         in_ev[j].record(h2d_s)
 
-    barrier()
-    torch.cuda.synchronize()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    h2d_s.wait_event(f0)
-    copy_in(0)
-    k = 0
-    for st in range(a.steps):
-        for j, ((t1, t2, wires), (_, _, _, M, N, _)) in enumerate(zip(tens, pairs)):
-            o = outs[k % 2]
-            stream.wait_event(in_ev[j])
-            stream.wait_event(free_out[k % 2])
-            q.contract(t1, t2, wires, out=o[:M * N])
-            done_ev[j].record(stream)
-            nj = (j + 1) % len(tens)
-            if not (st == a.steps - 1 and nj == 0):
-                copy_in(nj)
-            d2h_s.wait_event(done_ev[j])
-            with torch.cuda.stream(d2h_s):
-                host_out[:M * N].copy_(o[:M * N], non_blocking=True)
-            free_out[k % 2].record(d2h_s)
-            k += 1
-    stream.wait_stream(d2h_s)
-    f1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    ems = f0.elapsed_time(f1)
+    def e2e_run(steps):
+        for e in done_ev + free_out:
+            e.record(stream)
+        barrier()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        h2d_s.wait_event(f0)
+        copy_in(0)
+        k = 0
+        for st in range(steps):
+            for j, ((t1, t2, wires), (_, _, _, M, N, _)) in enumerate(zip(tens, pairs)):
+                o = outs[k % 2]
+                stream.wait_event(in_ev[j])
+                stream.wait_event(free_out[k % 2])
+                q.contract(t1, t2, wires, out=o[:M * N])
+                done_ev[j].record(stream)
+                nj = (j + 1) % len(tens)
+                if not (st == steps - 1 and nj == 0):
+                    copy_in(nj)
+                d2h_s.wait_event(done_ev[j])
+                with torch.cuda.stream(d2h_s):
+                    host_out[:M * N].copy_(o[:M * N], non_blocking=True)
+                free_out[k % 2].record(d2h_s)
+                k += 1
+        stream.wait_stream(d2h_s)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return f0.elapsed_time(f1)
+
+    e2e_run(1)  # warm-up of the copy path (the first large host copies after idle run slower)
+    ems = e2e_run(a.steps)
     if dist is not None:
         t = torch.tensor([ems], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)

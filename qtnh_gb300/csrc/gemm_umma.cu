@@ -405,24 +405,40 @@ __global__ void split_b_kernel(const double2* __restrict__ B, uint64_t K, uint64
 }
 
 // C[m][n] = sum over the S slices of the partials of rows 2m (Re) and 2m + 1 (Im) of
-// C^, with compensated FP32 additions (TwoSum), rounded once to double.
-__global__ void reduce_partials_kernel(const float* __restrict__ P, uint32_t S, uint64_t rows, uint64_t ldp,
-                                       double2* __restrict__ C, uint64_t M, uint64_t N) {
-  const uint64_t total = M * N;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t m = i / N, n = i % N;
-    float sr = 0.0f, er = 0.0f, si = 0.0f, ei = 0.0f;
-    for (uint32_t s = 0; s < S; ++s) {
-      const float* ps = P + (uint64_t)s * rows * ldp;
-      float t, e;
-      df::two_sum(sr, ps[(2 * m) * ldp + n], t, e);
-      sr = t;
-      er = __fadd_rn(er, e);
-      df::two_sum(si, ps[(2 * m + 1) * ldp + n], t, e);
-      si = t;
-      ei = __fadd_rn(ei, e);
+// C^, with compensated FP32 additions (TwoSum), rounded once to double. Thread per (row m,
+// four consecutive columns): 16-byte loads of both rows from every slice (the partial rows
+// are padded to a multiple of 256 columns), rows over blockIdx.y (no index division).
+__global__ void __launch_bounds__(256) reduce_partials_kernel(const float* __restrict__ P, uint32_t S, uint64_t rows,
+                                                              uint64_t ldp, double2* __restrict__ C, uint64_t M,
+                                                              uint64_t N) {
+  const uint64_t nq = (N + 3) / 4;
+  for (uint64_t m = blockIdx.y; m < M; m += gridDim.y) {
+    for (uint64_t qd = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; qd < nq; qd += (uint64_t)gridDim.x * blockDim.x) {
+      float sr[4] = {0.f, 0.f, 0.f, 0.f}, er[4] = {0.f, 0.f, 0.f, 0.f};
+      float si[4] = {0.f, 0.f, 0.f, 0.f}, ei[4] = {0.f, 0.f, 0.f, 0.f};
+      const float* pr = P + (2 * m) * ldp + 4 * qd;
+#pragma unroll 2
+      for (uint32_t sl = 0; sl < S; ++sl, pr += rows * ldp) {
+        const float4 a = *reinterpret_cast<const float4*>(pr);
+        const float4 b = *reinterpret_cast<const float4*>(pr + ldp);
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int x = 0; x < 4; ++x) {
+          float t, e;
+          df::two_sum(sr[x], av[x], t, e);
+          sr[x] = t;
+          er[x] = __fadd_rn(er[x], e);
+          df::two_sum(si[x], bv[x], t, e);
+          si[x] = t;
+          ei[x] = __fadd_rn(ei[x], e);
+        }
+      }
+#pragma unroll
+      for (int x = 0; x < 4; ++x) {
+        const uint64_t n = 4 * qd + (uint64_t)x;
+        if (n < N) C[m * N + n] = make_double2((double)sr[x] + (double)er[x], (double)si[x] + (double)ei[x]);
+      }
     }
-    C[i] = make_double2((double)sr + (double)er, (double)si + (double)ei);
   }
 }
 
@@ -508,8 +524,11 @@ static void gemm_core(const Prep& pa, const Prep& pb, void* Cv, uint64_t M, uint
     }
     count_launch();
     if (p.S > 1) {
-      reduce_partials_kernel<<<grid_for((M * N + 255) / 256, 8), 256, 0, s>>>(
-          p.partial, p.S, (uint64_t)p.MT * GM_M, (uint64_t)p.NT * GM_N, C, M, N);
+      // about 8 blocks of 256 threads per SM: column blocks along x, rows along y
+      const uint64_t gx = std::min<uint64_t>(((N + 3) / 4 + 255) / 256, 64);
+      const dim3 rgrid((unsigned)gx, (unsigned)std::min<uint64_t>(M, std::max<uint64_t>(1, 8ull * sm_count() / gx)));
+      reduce_partials_kernel<<<rgrid, 256, 0, s>>>(p.partial, p.S, (uint64_t)p.MT * GM_M, (uint64_t)p.NT * GM_N, C, M,
+                                                   N);
       count_launch();
     }
     check_cuda(cudaGetLastError(), "split GEMM launch");

@@ -8,7 +8,10 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "cuda_common.cuh"
@@ -76,8 +79,30 @@ void check_cuda(cudaError_t e, const char* what) {
 
 static std::atomic<uint64_t> g_workspace_allocs{0};
 
+// The workspace comes from the device's default stream-ordered pool. By default the pool
+// returns freed memory to the device at every synchronization, so the next large
+// workspace maps physical memory again (milliseconds per GB); the engine lets the pool
+// keep up to an eighth of the device memory (at most 32 GiB) cached instead, set once per
+// device on its first workspace.
+static void keep_pool_memory() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 0 || dev >= 64 || done[dev]) return;
+  done[dev] = true;
+  size_t free_b = 0, total_b = 0;
+  check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  cudaMemPool_t pool;
+  check_cuda(cudaDeviceGetDefaultMemPool(&pool, dev), "cudaDeviceGetDefaultMemPool");
+  unsigned long long keep = std::min<unsigned long long>(total_b / 8, 32ull << 30);
+  check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+}
+
 void* workspace_alloc(size_t bytes, void* stream) {
   if (bytes == 0) return nullptr;
+  keep_pool_memory();
   g_workspace_allocs.fetch_add(1, std::memory_order_relaxed);
   void* p = nullptr;
   check_cuda(cudaMallocAsync(&p, bytes, (cudaStream_t)stream), "cudaMallocAsync");
