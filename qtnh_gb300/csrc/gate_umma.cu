@@ -458,7 +458,7 @@ __device__ __forceinline__ uint32_t unbias_h(uint32_t w) {
 struct ChSmem {
   uint8_t adig[2][CH_ND][2][UM_M * 32];  // state digits: buffer, digit, K-step (4 KB each)
   uint8_t bdig[2][CH_NLMAX][UM_N * 32];  // gate digits: K-step, digit (1 KB each)
-  double2 stage[16][UM_M];              // fetched amplitudes (or fixed-point pairs): amplitude, group
+  double2 stage[2][16][UM_M];           // fetched amplitudes (or fixed-point pairs), two tiles ahead
   double2 U16[256];
   int32_t erow[16];
   uint64_t full[2];                     // digits of the tiles using buffer b are ready
@@ -642,11 +642,12 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     uint32_t kk = 0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) kk |= (common ? 0u : (uint32_t)min(62, max_erow - sm.erow[4 * h + a])) << (8 * a);
-    auto fetch = [&](uint64_t T, IT tb) {
+    // tile T into stage slot `slot` (its iteration % 2; one commit group per tile, empty past the end)
+    auto fetch = [&](uint64_t T, IT tb, uint32_t slot) {
       if (T < ntiles) {
         const IT gbase = tb | rbase;
 #pragma unroll
-        for (int c = 4 * h; c < 4 * h + 4; ++c) cp_async16(&sm.stage[c][r], psi + (gbase + (IT)p.off[c]));
+        for (int c = 4 * h; c < 4 * h + 4; ++c) cp_async16(&sm.stage[slot][c][r], psi + (gbase + (IT)p.off[c]));
       }
       cp_async_commit();
     };
@@ -689,18 +690,20 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
         }
       }
     };
-    IT tb_cur = tile_part(tile_of(0)), tb_prev = 0;
-    fetch(tile_of(0), tb_cur);
+    // tile parts of tiles m - 1 .. m + 2; the loads run two tiles ahead
+    IT tb_prev = 0, tb_cur = tile_part(tile_of(0)), tb_next = tile_part(tile_of(1));
+    fetch(tile_of(0), tb_cur, 0);
+    fetch(tile_of(1), tb_next, 1);
     uint64_t m = 0;
     bool ok = true;
     for (; tile_of(m) < ntiles; ++m) {
       const uint32_t b = (uint32_t)(m & 1);
-      cp_async_wait_all();
+      cp_async_wait_one();  // tile m has landed (tile m + 1 may still be in flight)
       double2 x[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) x[c] = sm.stage[4 * h + c][r];
-      const IT tb_next = tile_part(tile_of(m + 1));
-      fetch(tile_of(m + 1), tb_next);  // only this thread reads its stage slots
+      for (int c = 0; c < 4; ++c) x[c] = sm.stage[b][4 * h + c][r];
+      const IT tb_next2 = tile_part(tile_of(m + 2));
+      fetch(tile_of(m + 2), tb_next2, b);  // only this thread reads its stage slots
       // digits of this thread's 8 reals: digit j of amplitude 4h + a as one fp16x2 word (real,
       // imaginary); the four words of digit j fill the thread's core-matrix row
       uint32_t w[4][CH_ND];
@@ -740,6 +743,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
       }
       tb_prev = tb_cur;
       tb_cur = tb_next;
+      tb_next = tb_next2;
     }
     if (ok && m >= 1) {  // the last tile
       const uint32_t b = (uint32_t)((m - 1) & 1);
