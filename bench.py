@@ -125,6 +125,30 @@ def _traffic(kernel, n):
         return None
 
 
+def _host_link(host, dev):
+    """This machine's host link: a copy of `host` (pinned) to `dev` and one back, each alone on
+    its own stream after an untimed copy in the same direction (the first large copy after
+    idle runs slower), timed with CUDA events (GB/s); the e2e number depends on it."""
+    import torch
+    s = torch.cuda.Stream()
+    out = {}
+    for name in ("h2d", "d2h"):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            for timed in (False, True):
+                if timed:
+                    e0.record(s)
+                if name == "h2d":
+                    dev.copy_(host, non_blocking=True)
+                else:
+                    host.copy_(dev, non_blocking=True)
+        e1.record(s)
+        torch.cuda.synchronize()
+        out[name] = host.numel() * host.element_size() / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    return out
+
+
 class _Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -557,15 +581,15 @@ def main_contract(a):
     host_out = torch.empty(max_out, dtype=torch.complex128, pin_memory=True)
     h2d = sum(16 * (t1.data.numel() + t2.data.numel()) for t1, t2, _ in tens)
     d2h = sum(16 * M * N for _, _, _, M, N, _ in pairs)
-    # copies on two copy streams: the next pair's operands go in while this pair contracts,
-    # results come out of two alternating output buffers
+    # copies on two copy streams: the operands of the pairs LOOK ahead go in while this pair
+    # contracts (the host link, not the contractions, is the bound of this arm), results come
+    # out of NOUT output buffers in rotation
+    LOOK, NOUT = 8, 4
     h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
-    outs = [out, torch.empty_like(out)]
+    outs = [out] + [torch.empty_like(out) for _ in range(NOUT - 1)]
     in_ev = [torch.cuda.Event() for _ in tens]
     done_ev = [torch.cuda.Event() for _ in tens]
-    free_out = [torch.cuda.Event(), torch.cuda.Event()]
-    for e in done_ev + free_out:
-        e.record(stream)
+    free_out = [torch.cuda.Event() for _ in range(NOUT)]
 
     def copy_in(j):
         t1, t2, _ = tens[j]
@@ -584,23 +608,26 @@ def main_contract(a):
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         h2d_s.wait_event(f0)
-        copy_in(0)
-        k = 0
-        for st in range(steps):
-            for j, ((t1, t2, wires), (_, _, _, M, N, _)) in enumerate(zip(tens, pairs)):
-                o = outs[k % 2]
-                stream.wait_event(in_ev[j])
-                stream.wait_event(free_out[k % 2])
-                q.contract(t1, t2, wires, out=o[:M * N])
-                done_ev[j].record(stream)
-                nj = (j + 1) % len(tens)
-                if not (st == steps - 1 and nj == 0):
-                    copy_in(nj)
-                d2h_s.wait_event(done_ev[j])
-                with torch.cuda.stream(d2h_s):
-                    host_out[:M * N].copy_(o[:M * N], non_blocking=True)
-                free_out[k % 2].record(d2h_s)
-                k += 1
+        P = len(tens)
+        total = steps * P
+        look = max(1, min(LOOK, P - 1))  # never ahead of the pair's own previous contraction
+        for f in range(min(look, total)):
+            copy_in(f % P)
+        for f in range(total):
+            j = f % P
+            (t1, t2, wires), (_, _, _, M, N, _) = tens[j], pairs[j]
+            o = outs[f % NOUT]
+            stream.wait_event(in_ev[j])
+            stream.wait_event(free_out[f % NOUT])
+            q.contract(t1, t2, wires, out=o[:M * N])
+            done_ev[j].record(stream)
+            # pair f + look: its previous contraction (f + look - P < f, or f itself) is queued
+            if f + look < total:
+                copy_in((f + look) % P)
+            d2h_s.wait_event(done_ev[j])
+            with torch.cuda.stream(d2h_s):
+                host_out[:M * N].copy_(o[:M * N], non_blocking=True)
+            free_out[f % NOUT].record(d2h_s)
         stream.wait_stream(d2h_s)
         f1.record(stream)
         torch.cuda.synchronize()
@@ -823,24 +850,29 @@ def main_batch(a):
             dev_stage.copy_(host_all, non_blocking=True)
         in_ev.record(h2d_s)
 
-    torch.cuda.synchronize()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    h2d_s.wait_event(f0)
-    copy_in()
-    for st in range(a.steps):
-        stream.wait_event(in_ev)
-        for i in range(len(circuits)):
-            b.set_state(i, dev_stage[offs[i]:offs[i + 1]])
+    def e2e_run(steps):
         free_ev.record(stream)
-        if st + 1 < a.steps:
-            copy_in()
-        b.run()
-        b.results(out=dres)
-        host_res.copy_(dres, non_blocking=True)
-    f1.record(stream)
-    torch.cuda.synchronize()
-    ems = f0.elapsed_time(f1)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        h2d_s.wait_event(f0)
+        copy_in()
+        for st in range(steps):
+            stream.wait_event(in_ev)
+            for i in range(len(circuits)):
+                b.set_state(i, dev_stage[offs[i]:offs[i + 1]])
+            free_ev.record(stream)
+            if st + 1 < steps:
+                copy_in()
+            b.run()
+            b.results(out=dres)
+            host_res.copy_(dres, non_blocking=True)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        return f0.elapsed_time(f1)
+
+    e2e_run(1)  # warm-up of the copy path (the first large host copy after idle runs slower)
+    ems = e2e_run(a.steps)
     e2e = world * layers / (ems / a.steps * 1e-3)
     h2d = 16 * offs[-1]
     del dev_stage
@@ -1429,6 +1461,7 @@ def main():
         ems = float(t.item())
     e2e = world * a.depth * a.steps / (ems / 1e3)
     norm = q.norm2(cur)
+    link = _host_link(host_in, oth)  # (oth: a scratch state buffer)
 
     # circuit-level cross-check of the timed arithmetic against native FP64 on the same input
     arith_check = None
@@ -1461,7 +1494,8 @@ def main():
                          "launch_ms": gate_launch_ms, "time_share": share,
                          "layer_frac": value / world * 2 * 16 * N / (peak * 1e9)},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
+                    "host_link_gbs": link},
             "clocks": ck,
             "gpu_launches": launches,
             "final_norm2": norm,

@@ -582,6 +582,26 @@ def test_gate_layer_chain_keeps_regions_of_very_different_scale(bf16x6):
     assert rel_l2(out[4096:], ref[4096:]) < REL_TOL
 
 
+@pytest.mark.parametrize("rows", [[8.0, 8.0, 8.0, 8.0], [1.0, 2.0 ** -9, 2.0 ** 4, 0.75]], ids=["scaled", "rows_apart"])
+def test_gate_layer_chain_non_unitary_gates(rows, bf16x6):
+    # non-unitary gates: scaled by 8 (the rows of the fused operator stay within 2 bits of
+    # each other: the chain passes cut every row's digits at one scale, no output shift), or
+    # with rows 2^-9 .. 2^4 (each row has its own scale and its outputs are shifted to the
+    # common one)
+    nrng = np.random.default_rng(40 + int(rows[1] < 1))
+    n = 16
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    psi /= np.linalg.norm(psi)
+    rows = np.array(rows)
+    gates = [(t, (rows[:, None] * g.reshape(4, 4).T).T.reshape(-1)) for t, g in _disjoint_pairs(nrng, n, 4)]
+    st = dev(psi)
+    q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in gates])
+    out, ref = host(st), _oracle_layer(psi, n, gates)
+    assert rel_l2(out, ref) < REL_TOL
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < REL_TOL
+    assert q.take_device_errors() == 0
+
+
 def test_gate_layer_chain_zero_state_and_nonfinite_gate(bf16x6):
     nrng = np.random.default_rng(32)
     n = 13
