@@ -92,14 +92,18 @@ def _args():
 
 def _config(a, cpu_cores=None):
     return {
-        "workload": "random layered circuit, n=%d qubits, depth %d, 14 Haar 2-qubit SymmTensor gates/layer, "
-                    "phase DiagTensor layer every 4th, rescatter+permute of top 3 indices every 8th" % (a.n, a.depth),
+        "workload": "random layered circuit, n=%d qubits, depth %d, %d Haar 2-qubit SymmTensor gates/layer, "
+                    "phase DiagTensor layer every 4th, rescatter+permute of top 3 indices every 8th"
+                    % (a.n, a.depth, a.n // 2),
         "qubits": a.n,
         "depth": a.depth,
         "gates_per_layer": a.n // 2,
         "element": "complex128",
         "state_bytes": 16 * (2 ** a.n),
-        "l2_flush": "not needed: 4 GiB state is larger than the 129 MB L2",
+        "l2_flush": "not needed: the %s state is larger than the 129 MB L2" % (
+            "%d GiB" % (2 ** a.n // 2 ** 26) if a.n >= 26 else "%d MiB" % (2 ** a.n // 2 ** 16)),
+        "execution": "the gates of consecutive layers between redistributions as fused pairs in one fixed-point chain; "
+                     "each phase layer folded into the gates just before it ((D_a x D_b) U per gate on qubits a, b)",
         "parallelism": "replicas" if a.gpus > 1 else "single GPU",
     }
 

@@ -271,6 +271,15 @@ int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32
 int qtnh_apply_diag(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
                     const void* diag, void* stream);
 
+/* The product of a gate and a diagonal on one of its outputs, for queues of in-place
+ * contractions: out[in, o] = gate[in, o] * diag[o_p] (SymmTensor layout, k targets of dims
+ * tdims, o_p the output's digit at target position p; diag tdims[p] long). Applying the
+ * gate and then the diagonal on its p-th target (two in-place contractions,
+ * src/tensor/contract.cpp:250-289) equals applying this product once. out may be gate
+ * (in place). Device pointers gate, diag, out. */
+int qtnh_symm_diag_product(const void* gate, int32_t k, const uint64_t* tdims, int32_t p, const void* diag,
+                           void* out, void* stream);
+
 /* A layer of single-index diagonals in one streaming pass:
  * psi[x] *= prod_f d_f[x_{axes[f]}], d_f = factors + offset_f (each dims[axes[f]] long,
  * concatenated in f order). Device pointer `factors`. */

@@ -10,6 +10,11 @@ qtnh_permute); rescatter is metadata-only with all slabs resident. The gates of
 consecutive layers with nothing else between them go into one qtnh_apply_gate_layer
 call (in order), as the C++ API's queue of in-place contractions does, so their fused
 passes form one fixed-point chain.
+A phase layer directly after a layer's gates is folded into those gates: the diagonal
+on the qubits (a, b) of gate U follows it, so (D_a (x) D_b) U replaces U (elementwise,
+exact up to one rounding of each product); qubits that no gate of the layer covers keep
+a diagonal layer of their own. The phases then cost no pass over the state, and the gate
+runs on both sides of them form one chain.
 All argument arrays are built once so the timed loop is only library calls.
 """
 import ctypes
@@ -26,7 +31,22 @@ class DeviceCircuit:
         self.n = circuit.n
         self.dims = _u64(circuit.dims)
         self.rank = ctypes.c_int32(circuit.n)
-        all_gates = [g for l in circuit.layers for g in l.gates]
+        all_gates = []
+        residual = []  # per layer: the qubits whose phases stay a diagonal layer
+        for layer in circuit.layers:
+            gates = [np.asarray(g, dtype=np.complex128) for g in layer.gates]
+            rest = []
+            if layer.phases is not None:
+                covered = set()
+                for j, (a, b) in enumerate(layer.pairs):
+                    da, db = np.exp(1j * layer.phases[a]), np.exp(1j * layer.phases[b])
+                    # els[in * 4 + out] = U[out][in], out = 2 o_a + o_b: scale output o by d_a(o_a) d_b(o_b)
+                    scale = np.array([1.0, db, da, da * db], dtype=np.complex128)
+                    gates[j] = (gates[j].reshape(4, 4) * scale[None, :]).reshape(-1)
+                    covered.update((a, b))
+                rest = [qb for qb in range(circuit.n) if qb not in covered]
+            residual.append(rest)
+            all_gates.extend(gates)
         self.gates = torch.from_numpy(np.concatenate(all_gates) if all_gates else np.zeros(1, np.complex128)).to(device)
         base = self.gates.data_ptr()
         self.steps = []
@@ -42,16 +62,15 @@ class DeviceCircuit:
                 self.steps.append(("gates", (ctypes.c_int32(ng), ks, tg, ptrs)))
                 pending.clear()
 
-        for layer in circuit.layers:
+        for layer, rest in zip(circuit.layers, residual):
             for j, pr in enumerate(layer.pairs):
                 pending.append((pr, gi + j))
             gi += len(layer.gates)
-            if layer.phases is not None or layer.ptup is not None:
+            if rest or layer.ptup is not None:
                 flush()
-            if layer.phases is not None:
-                f = torch.from_numpy(phase_factors(layer.phases)).to(device)
-                axes = _u16(range(self.n))
-                self.steps.append(("diag", (ctypes.c_int32(self.n), axes, f)))
+            if rest:
+                f = torch.from_numpy(phase_factors(np.asarray(layer.phases)[rest])).to(device)
+                self.steps.append(("diag", (ctypes.c_int32(len(rest)), _u16(rest), f)))
             if layer.ptup is not None:
                 self.steps.append(("perm", _u16(layer.ptup)))
         flush()

@@ -73,7 +73,43 @@ static void drop_queue(const void* dev) {
   }
 }
 
+// A one-index diagonal whose index was last touched, in queue order, by a gate is folded
+// into that gate (qtnh_symm_diag_product, in place on the queued gate, which the
+// contraction consumed): the diagonal commutes with everything between them, and the
+// gate runs on both sides of it join into one fused run. Diagonals on an index whose
+// last toucher is not a gate, or that no earlier queued operation touches, stay.
+static void fold_diagonals(DeferredQueue& q) {
+  void* st = q.env->stream;
+  std::vector<char> gone(q.ops.size(), 0);
+  for (std::size_t i = 0; i < q.ops.size(); ++i) {
+    if (q.ops[i].kind != QTNH_KIND_DIAG || q.ops[i].targets.size() != 1) continue;
+    const uint16_t x = q.ops[i].targets[0];
+    for (std::size_t j = i; j-- > 0;) {
+      if (gone[j]) continue;
+      const auto& tg = q.ops[j].targets;
+      const auto it = std::find(tg.begin(), tg.end(), x);
+      if (it == tg.end()) continue;
+      if (q.ops[j].kind == QTNH_KIND_SYMM) {
+        std::vector<uint64_t> td;
+        for (uint16_t t : tg) td.push_back(q.dims[t]);
+        check(qtnh_symm_diag_product(q.ops[j].op.read(), (int32_t)tg.size(), td.data(), (int32_t)(it - tg.begin()),
+                                     q.ops[i].op.read(), q.ops[j].op.write(), st));
+        gone[i] = 1;
+      }
+      break;
+    }
+  }
+  std::size_t k = 0;
+  for (std::size_t i = 0; i < q.ops.size(); ++i)
+    if (!gone[i]) {
+      if (k != i) q.ops[k] = std::move(q.ops[i]);
+      ++k;
+    }
+  q.ops.resize(k);
+}
+
 static void apply_queue(void* dev, DeferredQueue& q) {
+  fold_diagonals(q);
   const int32_t rank = (int32_t)q.dims.size();
   void* st = q.env->stream;
   std::size_t i = 0;

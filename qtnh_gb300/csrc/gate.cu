@@ -300,6 +300,16 @@ __global__ void __launch_bounds__(256) layer_apply_kernel(c128* __restrict__ psi
   }
 }
 
+// out[e] = gate[e] * diag[digit p of e's output index] (elements [in * D + o], the digit at
+// stride `stride` and radix `dp`); one thread per element, in place allowed.
+__global__ void diag_product_kernel(const c128* gate, const c128* __restrict__ diag, c128* out, uint64_t n, uint64_t D,
+                                    uint64_t stride, uint64_t dp) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t o = e % D;
+    out[e] = cmul(gate[e], diag[(o / stride) % dp]);
+  }
+}
+
 // Split copy of a phase table (float pairs) plus a per-entry range flag in the sign of
 // nothing: entries out of the gate range are kept as FP64 and flagged with NaN hi parts.
 __global__ void table_split_kernel(const c128* __restrict__ t, df::cf2* __restrict__ ts, uint64_t n) {
@@ -622,6 +632,26 @@ int qtnh_apply_diag(void* state, int32_t rank, const uint64_t* dims, int32_t k, 
   return QTNH_API([&]() -> int {
     if (rank < 0 || rank > QTNH_MAX_RANK || k < 0 || k > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
     apply_diag_device(state, dims_t(dims, dims + rank), std::vector<uint16_t>(targets, targets + k), diag, stream);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_symm_diag_product(const void* gate, int32_t k, const uint64_t* tdims, int32_t p, const void* diag,
+                           void* out, void* stream) {
+  return QTNH_API([&]() -> int {
+    if (k < 1 || k > QTNH_MAX_RANK || p < 0 || p >= k) throw Error(QTNH_ERR_INVALID_ARGUMENT, "target out of range");
+    if (!gate || !diag || !out || !tdims) throw Error(QTNH_ERR_INVALID_ARGUMENT, "null pointer");
+    uint64_t D = 1, stride = 1;
+    for (int32_t j = 0; j < k; ++j) {
+      if (tdims[j] == 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "zero dimension");
+      D *= tdims[j];
+      if (j > p) stride *= tdims[j];
+    }
+    const uint64_t n = D * D;
+    diag_product_kernel<<<grid_for((n + 255) / 256, 1), 256, 0, (cudaStream_t)stream>>>(
+        static_cast<const c128*>(gate), static_cast<const c128*>(diag), static_cast<c128*>(out), n, D, stride, tdims[p]);
+    count_launch();
+    check_cuda(cudaGetLastError(), "diag product launch");
     return QTNH_OK;
   });
 }

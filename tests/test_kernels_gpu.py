@@ -3,6 +3,7 @@
 Data movement (permute, swap, delta contractions) must be bit-exact; contractions
 within 1e-12 relative L2 (the plain complex128 bar), goldens within the
 reference's own 1e-5 (tests/c2-tensor.cpp:157)."""
+import ctypes
 import json
 import math
 import os
@@ -266,6 +267,26 @@ def test_diagonal_in_place_and_layer(arith):
     for j in range(n):
         cur, _, _ = orc.contract(cur, orc.Tensor(orc.DIAG, [], [2, 2], factors[2 * j:2 * j + 2]), [(j, 0)])
     assert rel_l2(host(st), cur.els) < REL_TOL
+
+
+@pytest.mark.parametrize("tdims,p", [([2, 2], 0), ([2, 2], 1), ([3], 0), ([2, 3, 2], 1)])
+def test_symm_diag_product(tdims, p):
+    # out[in, o] = gate[in, o] * diag[o_p]: the gate then the diagonal on its p-th target,
+    # as one gate (what the C++ queue folds); also in place
+    rng = np.random.default_rng(60 + p + len(tdims))
+    D = int(np.prod(tdims))
+    g = crandn(rng, [D * D]).reshape(-1)
+    d = crandn(rng, [tdims[p]]).reshape(-1)
+    odig = (np.arange(D) // int(np.prod(tdims[p + 1:]))) % tdims[p]
+    want = (g.reshape(D, D) * d[odig][None, :]).reshape(-1)
+    gd, dd, od = dev(g), dev(d), dev(np.zeros_like(g))
+    td = (ctypes.c_uint64 * len(tdims))(*tdims)
+    for out in (od, gd):
+        q.check(q.lib().qtnh_symm_diag_product(q._ptr(gd), len(tdims), td, p, q._ptr(dd), q._ptr(out), q._stream()))
+        assert np.max(np.abs(host(out) - want)) <= 1e-15 * np.max(np.abs(want))  # one complex product each
+    with pytest.raises(q.InvalidArgument):
+        q.check(q.lib().qtnh_symm_diag_product(q._ptr(gd), len(tdims), td, len(tdims), q._ptr(dd), q._ptr(od),
+                                                q._stream()))
 
 
 def test_diagonals_default_mode_out_of_range(bf16x6):
