@@ -449,7 +449,9 @@ static void test_queued_contractions(QTNHEnv& env) {
     return ok;
   };
   // four two-qubit gates (two disjoint pairs, then overlapping), a one-index diagonal run
-  // and a two-index diagonal, read back through at()
+  // (the diagonals on 1, 6 and 3 are folded into the queued gates on them, as their second,
+  // second and first target; the one on 4 follows no gate and stays) and a two-index
+  // diagonal, read back through at()
   const std::vector<std::vector<int>> qs = {{0, 5}, {2, 3}, {5, 1}, {7, 6}, {3, 0}};
   tptr st = DenseTensor::make(env, {}, tidx_tup(n, 2), std::vector<tel>(psi));
   std::vector<tel> ref = psi;
@@ -458,7 +460,7 @@ static void test_queued_contractions(QTNHEnv& env) {
                           {{(tidx_tup_st)qs[g][0], 0}, {(tidx_tup_st)qs[g][1], 1}});
     ref = apply_plain(ref, n, qs[g], gate((int)g));
   }
-  for (int q : {1, 4, 6}) {
+  for (int q : {1, 4, 6, 3}) {
     const std::vector<tel> d = {std::exp(0.3i * (double)q), std::exp(-1.1i * (double)q)};
     st = Tensor::contract(std::move(st), DiagTensor::make(env, {}, {2, 2}, 0, false, std::vector<tel>(d)),
                           {{(tidx_tup_st)q, 0}});
