@@ -1380,6 +1380,7 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     l0 = q.launches()
+    q.gate_timing(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(a.steps):
@@ -1391,23 +1392,31 @@ def main():
     barrier()
     ck = clocks.stop()
     launches = q.launches() - l0
+    pass_ms, pass_launches = q.gate_timing(False)
     ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     ms_per_step = ms / a.steps
     value = world * a.depth * a.steps / (ms / 1e3)
 
     # roofline of the dominant kernel (two-qubit gate kernel; with bf16x6 the fused
-    # gate-pair passes, one launch per pair of gates: the first pass of a run of pairs by
-    # the pair kernel, the others by the fixed-point chain kernel)
-    gate_ms = [s.elapsed_time(e) for s, e in events.get("gates", [])]
-    launches_per_step = sum(((args[0].value + 1) // 2 if a.arith == "bf16x6" else args[0].value)
-                            for kind, args in dc.steps if kind == "gates")
+    # gate-pair passes, one launch per pair of gates: the first pass of a chain by the
+    # pair kernel, the others by the fixed-point chain kernel). With bf16x6 the library
+    # times every pass with CUDA events on the launch stream (qtnh_gate_timing); the
+    # other arithmetics take the span of the gate calls over their gate count.
+    runs_ms = sum(s.elapsed_time(e) for s, e in events.get("runs", []))
+    diag_ms = sum(s.elapsed_time(e) for s, e in events.get("diag", []))
     kernel = {"f32x2": "gate_kernel_f32x2<4>", "fp64": "gate_kernel<4>",
               "bf16x6": "gate_pair_chain_kernel + gate_pair_umma_kernel"}[a.arith]
-    gate_launch_ms = sum(gate_ms) / (a.steps * launches_per_step) if gate_ms else None
+    if a.arith == "bf16x6" and pass_launches:
+        gate_launch_ms = pass_ms / pass_launches
+        gates_ms = pass_ms
+    else:
+        gate_launch_ms = runs_ms / (a.steps * dc.gate_count) if dc.gate_count else None
+        gates_ms = runs_ms
     alg_bytes = 32.0 * N
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (gate_launch_ms * 1e-3) / 1e9 if gate_launch_ms else None
-    share = {k: sum(s.elapsed_time(e) for s, e in v) / ms for k, v in events.items()}
+    # perm: the rest of the gate-run calls (the permutations and the gaps between launches)
+    share = {"gates": gates_ms / ms, "diag": diag_ms / ms, "perm": max(0.0, runs_ms - gates_ms) / ms}
 
     # e2e through the C ABI with host buffers: every step copies its input state from
     # pinned host memory and its result back, on two copy streams, with three state buffers

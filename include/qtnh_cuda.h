@@ -256,7 +256,10 @@ int qtnh_contract_dense_noalloc(const void* a, int32_t rank_a, const uint64_t* d
 /* psi'[.., o_j at targets[j], ..] = sum_in G[in, o] psi[.., in_j at targets[j], ..] where
  * G = gate elements in SymmTensor layout [in_0..in_{k-1}, out_0..out_{k-1}] row-major
  * (include/tensor/symm.hpp:22-45). All target dims must be equal to the gate's.
- * In place (state is read and overwritten). Device pointer `gate`. */
+ * In place (state is read and overwritten). Device pointer `gate`. Gate sizes D (product
+ * of the target dims) of 1, 2, 3, 4, 8, 9 and 16 run register-blocked kernels; any other
+ * size runs a general FP64 kernel that reads a copy of the state (workspace of the
+ * state's size). */
 int qtnh_apply_gate(void* state, int32_t rank, const uint64_t* dims, int32_t k, const uint16_t* targets,
                     const void* gate, void* stream);
 
@@ -265,6 +268,28 @@ int qtnh_apply_gate(void* state, int32_t rank, const uint64_t* dims, int32_t k, 
  * targets: concatenated target lists, gates: device pointers (one per gate). */
 int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32_t ngates, const int32_t* gate_k,
                           const uint16_t* targets, const void* const* gates, void* stream);
+
+/* Runs of in-place gate contractions with a permutation between consecutive runs: the
+ * sequence qtnh_apply_gate_layer(run 0), Tensor::permute (src/tensor/dense.cpp:152-169,
+ * ptups[0]), qtnh_apply_gate_layer(run 1), ... as one call. Run r holds run_ngates[r]
+ * gates (gate_k, targets and gates concatenated over the runs, targets naming the axes
+ * of the state as it is when the run starts); ptups holds nruns - 1 permutation tuples
+ * of rank entries each (the qtnh_permute convention). Permutations go out of place
+ * between state and scratch (same size, no overlap; unused when nruns == 1), so the
+ * result is in scratch when nruns - 1 is odd and in state otherwise; the other buffer's
+ * contents are undefined afterwards. With QTNH_ARITH_BF16X6 the fused gate-pair passes
+ * of all runs form one fixed-point chain (the permutations move the fixed-point
+ * elements), so a permutation does not end the chain. All arguments are checked before
+ * the first launch. Device pointers state, scratch and gates. */
+int qtnh_apply_gate_runs(void* state, void* scratch, int32_t rank, const uint64_t* dims, int32_t nruns,
+                         const int32_t* run_ngates, const int32_t* gate_k, const uint16_t* targets,
+                         const void* const* gates, const uint16_t* ptups, void* stream);
+
+/* CUDA-event timing of the fused gate-pair passes (QTNH_ARITH_BF16X6; measurement
+ * support): returns the summed duration (ms) and count of the passes recorded since the
+ * previous call (synchronizing on them), then enables (enable != 0) or disables
+ * recording. */
+int qtnh_gate_timing(int enable, double* ms, uint64_t* launches);
 
 /* DiagTensor contraction in place: psi[x] *= d[x restricted to targets] with d the
  * diagonal (row-major over the target dims). Device pointer `diag`. */

@@ -209,6 +209,28 @@ def apply_gate_layer(state, dims, gates, stream=None):
     return state
 
 
+def apply_gate_runs(state, scratch, dims, runs, stream=None):
+    """runs: list of (gates, ptup) -- gates a list of (targets, device gate tensor) as in
+    apply_gate_layer, ptup the permutation after the run (None for the last run). Returns
+    the buffer holding the result (scratch after an odd number of permutations)."""
+    _check_c128(state)
+    if len(runs) > 1:
+        _check_c128(scratch)
+    for j, (_, pt) in enumerate(runs):
+        if (pt is None) != (j + 1 == len(runs)):
+            raise ValueError("every run but the last is followed by a permutation")
+    gates = [g for gl, _ in runs for g in gl]
+    ng = (ctypes.c_int32 * len(runs))(*[len(gl) for gl, _ in runs])
+    ks = (ctypes.c_int32 * max(1, len(gates)))(*[len(t) for t, _ in gates])
+    tg = _u16([x for t, _ in gates for x in t])
+    ptrs = (ctypes.c_void_p * max(1, len(gates)))(*[g.data_ptr() for _, g in gates])
+    pts = _u16([x for _, pt in runs[:-1] for x in pt])
+    check(lib().qtnh_apply_gate_runs(_ptr(state), _ptr(scratch),
+                                     ctypes.c_int32(len(dims)), _u64(dims), ctypes.c_int32(len(runs)), ng, ks, tg,
+                                     ptrs, pts, _stream(stream)))
+    return scratch if (len(runs) - 1) % 2 else state
+
+
 def apply_diag(state, dims, targets, diag, stream=None):
     _check_c128(state)
     _check_c128(diag)
@@ -271,6 +293,13 @@ def gemm_timing(enable):
     """(ms, launches) of the tcgen05 GEMM kernel since the last call; then (dis)arm recording."""
     ms, n = ctypes.c_double(), ctypes.c_uint64()
     check(lib().qtnh_gemm_timing(ctypes.c_int(1 if enable else 0), ctypes.byref(ms), ctypes.byref(n)))
+    return ms.value, int(n.value)
+
+
+def gate_timing(enable):
+    """(ms, launches) of the fused gate-pair passes since the last call; then (dis)arm recording."""
+    ms, n = ctypes.c_double(), ctypes.c_uint64()
+    check(lib().qtnh_gate_timing(ctypes.c_int(1 if enable else 0), ctypes.byref(ms), ctypes.byref(n)))
     return ms.value, int(n.value)
 
 

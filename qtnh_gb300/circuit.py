@@ -5,11 +5,12 @@ Each layer is the sequence of contractions a qtnh user would write:
 rule, src/tensor/contract.cpp:250-289), one rank-2 DiagTensor contraction per
 qubit for a phase layer, and ``Tensor::rescatter`` / ``Tensor::permute`` /
 ``Tensor::rescatter`` for a redistribution. The runner issues them as the
-batched entry points of the C ABI (qtnh_apply_gate_layer, qtnh_apply_diag_layer,
-qtnh_permute); rescatter is metadata-only with all slabs resident. The gates of
-consecutive layers with nothing else between them go into one qtnh_apply_gate_layer
-call (in order), as the C++ API's queue of in-place contractions does, so their fused
-passes form one fixed-point chain.
+batched entry points of the C ABI (qtnh_apply_gate_runs, qtnh_apply_diag_layer);
+rescatter is metadata-only with all slabs resident. The gates of consecutive layers go
+into one call (in order), as the C++ API's queue of in-place contractions does, with
+the permutations between them: qtnh_apply_gate_runs applies runs of gates separated by
+permutations, so the fused passes on both sides of a permutation form one fixed-point
+chain. Only a diagonal layer ends such a call.
 A phase layer directly after a layer's gates is folded into those gates: the diagonal
 on the qubits (a, b) of gate U follows it, so (D_a (x) D_b) U replaces U (elementwise,
 exact up to one rounding of each product); qubits that no gate of the layer covers keep
@@ -51,29 +52,37 @@ class DeviceCircuit:
         base = self.gates.data_ptr()
         self.steps = []
         gi = 0
-        pending = []  # (pair, gate index) of consecutive gate-only layers
+        runs = []  # the open qtnh_apply_gate_runs call: [targets, gate indices, ptup] per run
 
-        def flush():
-            if pending:
-                ng = len(pending)
-                ks = (ctypes.c_int32 * ng)(*([2] * ng))
-                tg = _u16([x for p, _ in pending for x in p])
-                ptrs = (ctypes.c_void_p * ng)(*[base + 16 * 16 * j for _, j in pending])
-                self.steps.append(("gates", (ctypes.c_int32(ng), ks, tg, ptrs)))
-                pending.clear()
+        def close():
+            if len(runs) > 1 or (runs and runs[0][1]):
+                ks = [2] * sum(len(ix) for _, ix, _ in runs)
+                ptrs = [base + 16 * 16 * j for _, ix, _ in runs for j in ix]
+                pts = [x for _, _, pt in runs[:-1] for x in pt]
+                self.steps.append(("runs", (ctypes.c_int32(len(runs)),
+                                            (ctypes.c_int32 * len(runs))(*[len(ix) for _, ix, _ in runs]),
+                                            (ctypes.c_int32 * max(1, len(ks)))(*ks),
+                                            _u16([x for tg, _, _ in runs for x in tg]),
+                                            (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs), _u16(pts), len(runs) - 1)))
+            runs.clear()
 
         for layer, rest in zip(circuit.layers, residual):
+            if not runs:
+                runs.append([[], [], None])
             for j, pr in enumerate(layer.pairs):
-                pending.append((pr, gi + j))
+                runs[-1][0].extend(pr)
+                runs[-1][1].append(gi + j)
             gi += len(layer.gates)
-            if rest or layer.ptup is not None:
-                flush()
             if rest:
+                close()
                 f = torch.from_numpy(phase_factors(np.asarray(layer.phases)[rest])).to(device)
                 self.steps.append(("diag", (ctypes.c_int32(len(rest)), _u16(rest), f)))
             if layer.ptup is not None:
-                self.steps.append(("perm", _u16(layer.ptup)))
-        flush()
+                if not runs:
+                    runs.append([[], [], None])
+                runs[-1][2] = list(layer.ptup)
+                runs.append([[], [], None])
+        close()
         self.layers = len(circuit.layers)
         self.gate_count = gi
 
@@ -91,17 +100,16 @@ class DeviceCircuit:
                 import torch
                 ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                 ev[0].record(stream)
-            if kind == "gates":
-                ng, ks, tg, ptrs = args
-                check(L.qtnh_apply_gate_layer(ctypes.c_void_p(cur.data_ptr()), self.rank, self.dims, ng, ks, tg, ptrs, st))
-            elif kind == "diag":
+            if kind == "runs":
+                nr, counts, ks, tg, ptrs, pts, nperm = args
+                check(L.qtnh_apply_gate_runs(ctypes.c_void_p(cur.data_ptr()), ctypes.c_void_p(other.data_ptr()),
+                                             self.rank, self.dims, nr, counts, ks, tg, ptrs, pts, st))
+                if nperm % 2:
+                    cur, other = other, cur
+            else:
                 nf, axes, f = args
                 check(L.qtnh_apply_diag_layer(ctypes.c_void_p(cur.data_ptr()), self.rank, self.dims, nf, axes,
                                               ctypes.c_void_p(f.data_ptr()), st))
-            else:
-                check(L.qtnh_permute(ctypes.c_void_p(cur.data_ptr()), ctypes.c_void_p(other.data_ptr()), self.rank,
-                                     self.dims, args, st))
-                cur, other = other, cur
             if ev is not None:
                 ev[1].record(stream)
                 events.setdefault(kind, []).append(ev)

@@ -76,6 +76,52 @@ __global__ void __launch_bounds__(256) gate_kernel(c128* __restrict__ psi, const
   }
 }
 
+// Target decode of the general kernel: the D = prod(tdim) amplitudes of a group, row-major
+// over the targets (the last target fastest), at state strides tstr.
+struct GateAnyParams {
+  uint64_t D;
+  int k;
+  uint64_t tdim[QTNH_MAX_RANK];
+  int64_t tstr[QTNH_MAX_RANK];
+};
+
+// Any gate size: one thread per (group, output), reading the inputs from a copy of the
+// state (`in`) and writing psi, in FP64 fused multiply-adds.
+__global__ void __launch_bounds__(256) gate_kernel_any(c128* __restrict__ psi, const c128* __restrict__ in,
+                                                       const c128* __restrict__ gate,
+                                                       const __grid_constant__ GateParams p,
+                                                       const __grid_constant__ GateAnyParams a) {
+  const uint64_t total = p.other.total * a.D;
+  for (uint64_t it = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; it < total;
+       it += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t grp = it / a.D, o = it % a.D;
+    const uint64_t base = group_base(grp, p);
+    int64_t off_o = 0;
+    uint64_t rem = o;
+    for (int j = a.k - 1; j >= 0; --j) {
+      off_o += (int64_t)(rem % a.tdim[j]) * a.tstr[j];
+      rem /= a.tdim[j];
+    }
+    // inputs in row-major order: an odometer over the target digits
+    uint64_t digit[QTNH_MAX_RANK];
+    for (int j = 0; j < a.k; ++j) digit[j] = 0;
+    int64_t off_i = 0;
+    c128 acc = make_double2(0.0, 0.0);
+    for (uint64_t i = 0; i < a.D; ++i) {
+      acc = cfma(gate[i * a.D + o], in[base + off_i], acc);  // SymmTensor layout [in, out]
+      for (int j = a.k - 1; j >= 0; --j) {
+        if (++digit[j] < a.tdim[j]) {
+          off_i += a.tstr[j];
+          break;
+        }
+        digit[j] = 0;
+        off_i -= (int64_t)(a.tdim[j] - 1) * a.tstr[j];
+      }
+    }
+    psi[base + off_o] = acc;
+  }
+}
+
 // FP64 fallback for one group (kept out of line so the float-float path is never
 // predicated over it; it re-reads the group, which has not been written yet).
 template <int D>
@@ -464,7 +510,26 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
     QTNH_GATE_CASE(8)
     QTNH_GATE_CASE(9)
     QTNH_GATE_CASE(16)
-    default: throw Error(QTNH_ERR_UNSUPPORTED, "gate size outside the register-blocked kernel");
+    default: {
+      // other sizes: the general kernel out of a copy of the state
+      GateAnyParams a;
+      a.D = D;
+      a.k = (int)targets.size();
+      for (size_t j = 0; j < targets.size(); ++j) {
+        a.tdim[j] = dims[targets[j]];
+        a.tstr[j] = (int64_t)st[targets[j]];
+      }
+      const uint64_t n = product(dims);
+      c128* copy = static_cast<c128*>(workspace_alloc(n * sizeof(c128), stream));
+      cudaError_t e = cudaMemcpyAsync(copy, psi, n * sizeof(c128), cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess) {
+        gate_kernel_any<<<grid_for((p.other.total * D + 255) / 256, 8), 256, 0, s>>>(psi, copy, g, p, a);
+        e = cudaGetLastError();
+      }
+      workspace_free(copy, stream);
+      check_cuda(e, "gate_kernel_any launch");
+      break;
+    }
   }
 #undef QTNH_GATE_CASE
   count_launch();
@@ -623,6 +688,73 @@ int qtnh_apply_gate_layer(void* state, int32_t rank, const uint64_t* dims, int32
     } else {
       for (int32_t g = 0; g < ngates; ++g) apply_gate_device(state, d, tl[g], gates[g], stream);
     }
+    return QTNH_OK;
+  });
+}
+
+int qtnh_apply_gate_runs(void* state, void* scratch, int32_t rank, const uint64_t* dims, int32_t nruns,
+                         const int32_t* run_ngates, const int32_t* gate_k, const uint16_t* targets,
+                         const void* const* gates, const uint16_t* ptups, void* stream) {
+  return QTNH_API([&]() -> int {
+    if (rank < 0 || rank > QTNH_MAX_RANK || nruns < 1) throw Error(QTNH_ERR_INVALID_ARGUMENT, "rank out of range");
+    if (nruns > 1 && (!scratch || scratch == state)) throw Error(QTNH_ERR_INVALID_ARGUMENT, "no separate scratch buffer");
+    // everything is checked before the first launch
+    dims_t d(dims, dims + rank);
+    dims_t dr = d;  // the dims when run r starts
+    std::vector<GateRun> runs((size_t)nruns);
+    size_t o = 0, gi = 0;
+    for (int32_t r = 0; r < nruns; ++r) {
+      if (run_ngates[r] < 0) throw Error(QTNH_ERR_INVALID_ARGUMENT, "negative gate count");
+      for (int32_t g = 0; g < run_ngates[r]; ++g, ++gi) {
+        const int32_t k = gate_k[gi];
+        if (k < 0 || k > rank) throw Error(QTNH_ERR_INVALID_ARGUMENT, "gate arity out of range");
+        std::vector<uint16_t> t(targets + o, targets + o + k);
+        check_targets(dr, t);
+        runs[r].targets.push_back(std::move(t));
+        runs[r].gates.push_back(gates[gi]);
+        o += (size_t)k;
+      }
+      if (r + 1 < nruns) {
+        const uint16_t* pt = ptups + (size_t)r * (size_t)rank;
+        std::vector<uint8_t> seen((size_t)rank, 0);
+        for (int32_t i = 0; i < rank; ++i) {
+          if (pt[i] >= rank || seen[pt[i]]) throw Error(QTNH_ERR_INVALID_ARGUMENT, "permutation tuple is not a permutation");
+          seen[pt[i]] = 1;
+        }
+        runs[r].ptup.assign(pt, pt + rank);
+        dims_t nd(dr.size());
+        for (size_t i = 0; i < dr.size(); ++i) nd[pt[i]] = dr[i];
+        dr = nd;
+      }
+    }
+    if (arithmetic_mode() == QTNH_ARITH_BF16X6) {
+      apply_gate_runs_tc(state, scratch, d, runs, stream);
+    } else {
+      void* cur = state;
+      void* oth = scratch;
+      for (const GateRun& run : runs) {
+        for (size_t g = 0; g < run.gates.size(); ++g) apply_gate_device(cur, d, run.targets[g], run.gates[g], stream);
+        if (!run.ptup.empty()) {
+          permute_device(cur, oth, d, run.ptup, stream);
+          dims_t nd(d.size());
+          for (size_t i = 0; i < d.size(); ++i) nd[run.ptup[i]] = d[i];
+          d = nd;
+          std::swap(cur, oth);
+        }
+      }
+    }
+    return QTNH_OK;
+  });
+}
+
+int qtnh_gate_timing(int enable, double* ms, uint64_t* launches) {
+  return QTNH_API([&]() -> int {
+    double t = 0;
+    uint64_t n = 0;
+    take_pass_times(t, n);
+    if (ms) *ms = t;
+    if (launches) *launches = n;
+    set_pass_timing(enable != 0);
     return QTNH_OK;
   });
 }

@@ -26,6 +26,8 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "gate_pair.cuh"
@@ -321,7 +323,33 @@ struct LayerStep {
   size_t g;        // first gate
   bool pair;       // gates g and g + 1 fused, else gate g alone
   PairParams p;    // pair parameters
+  int perm;        // >= 0: not a gate but the permutation after run `perm`
+  dims_t dims;     // the state's dims at this step (before the permutation)
 };
+
+// Optional CUDA-event timing of the tensor-core gate-pass launches (qtnh_gate_timing).
+std::mutex g_pass_mu;
+bool g_pass_timing = false;
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_pass_events;
+
+template <typename F>
+void timed_pass(cudaStream_t s, F&& launch) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    if (g_pass_timing) {
+      check_cuda(cudaEventCreate(&e0), "event");
+      check_cuda(cudaEventCreate(&e1), "event");
+    }
+  }
+  if (e0) check_cuda(cudaEventRecord(e0, s), "event record");
+  launch();
+  if (e1) {
+    check_cuda(cudaEventRecord(e1, s), "event record");
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    g_pass_events.emplace_back(e0, e1);
+  }
+}
 
 }  // namespace
 
@@ -331,57 +359,94 @@ struct LayerStep {
 // more fused pairs on the tcgen05 tile shape is a chain: the first pass reads and writes
 // doubles and records their largest exponent, the next ones cut the state at that one
 // scale and pass it on as 64-bit fixed point, the last writes doubles (ozaki.cuh,
-// gate_umma.cu). Returns after issuing all launches.
-void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
-                         const std::vector<const void*>& gates, void* stream) {
-  const size_t r = dims.size();
-  bool pow2 = true;
-  for (auto d : dims) pow2 = pow2 && log2_or_none(d) != 0xFFFFFFFFu;
-  const uint64_t n = product(dims);
+// gate_umma.cu). A permutation between two runs of gates (runs[r].ptup) moves the
+// elements from one buffer to the other; inside a chain it moves the fixed-point form
+// (16-byte elements, values unchanged, so the chain's record still holds). Returns whether
+// the result is in `scratch` (an odd number of permutations); all launches are issued.
+bool apply_gate_runs_tc(void* state, void* scratch, dims_t dims, const std::vector<GateRun>& runs, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   std::vector<LayerStep> steps;
-  size_t g = 0;
-  while (g < gates.size()) {
-    bool fused = false;
-    if (pow2 && n >= 128 && g + 1 < gates.size() && targets[g].size() == 2 && targets[g + 1].size() == 2) {
-      const auto& ta = targets[g];
-      const auto& tb = targets[g + 1];
-      std::vector<uint16_t> all = {ta[0], ta[1], tb[0], tb[1]};
-      bool ok = true;
-      for (auto a : all) ok = ok && a < r && dims[a] == 2;
-      std::vector<uint16_t> srt(all);
-      std::sort(srt.begin(), srt.end());
-      ok = ok && std::adjacent_find(srt.begin(), srt.end()) == srt.end();
-      if (ok) {
-        const uint16_t tg[4] = {ta[0], ta[1], tb[0], tb[1]};
-        steps.push_back({g, true, make_pair_params(dims, tg)});
-        g += 2;
-        fused = true;
+  std::vector<const void*> gates;
+  std::vector<std::vector<uint16_t>> targets;
+  for (size_t r = 0; r < runs.size(); ++r) {
+    const size_t rk = dims.size();
+    bool pow2 = true;
+    for (auto d : dims) pow2 = pow2 && log2_or_none(d) != 0xFFFFFFFFu;
+    const uint64_t n = product(dims);
+    const size_t base = gates.size();
+    gates.insert(gates.end(), runs[r].gates.begin(), runs[r].gates.end());
+    targets.insert(targets.end(), runs[r].targets.begin(), runs[r].targets.end());
+    size_t g = base;
+    while (g < gates.size()) {
+      bool fused = false;
+      if (pow2 && n >= 128 && g + 1 < gates.size() && targets[g].size() == 2 && targets[g + 1].size() == 2) {
+        const auto& ta = targets[g];
+        const auto& tb = targets[g + 1];
+        std::vector<uint16_t> all = {ta[0], ta[1], tb[0], tb[1]};
+        bool ok = true;
+        for (auto a : all) ok = ok && a < rk && dims[a] == 2;
+        std::vector<uint16_t> srt(all);
+        std::sort(srt.begin(), srt.end());
+        ok = ok && std::adjacent_find(srt.begin(), srt.end()) == srt.end();
+        if (ok) {
+          const uint16_t tg[4] = {ta[0], ta[1], tb[0], tb[1]};
+          steps.push_back({g, true, make_pair_params(dims, tg), -1, dims});
+          g += 2;
+          fused = true;
+        }
+      }
+      if (!fused) {
+        steps.push_back({g, false, PairParams{}, -1, dims});
+        g += 1;
       }
     }
-    if (!fused) {
-      steps.push_back({g, false, PairParams{}});
-      g += 1;
+    if (!runs[r].ptup.empty()) {
+      steps.push_back({0, false, PairParams{}, (int)r, dims});
+      dims_t nd(dims.size());
+      for (size_t i = 0; i < dims.size(); ++i) nd[runs[r].ptup[i]] = dims[i];
+      dims = nd;
     }
   }
-  double2* psi = static_cast<double2*>(state);
+  void* cur = state;
+  void* oth = scratch;
   auto gate_ptr = [&](size_t i) { return static_cast<const double2*>(gates[i]); };
+  auto permute = [&](const LayerStep& st) {
+    permute_device(cur, oth, st.dims, runs[(size_t)st.perm].ptup, stream);
+    std::swap(cur, oth);
+  };
   size_t i = 0;
   while (i < steps.size()) {
-    size_t j = i;
-    while (j < steps.size() && steps[j].pair && chain_applies(steps[j].p)) ++j;
-    const size_t R = j - i;
+    if (steps[i].perm >= 0) {
+      permute(steps[i]);
+      ++i;
+      continue;
+    }
+    // a chain: fused pairs on the tile shape, with permutations between them
+    size_t j = i, last = i, R = 0;
+    while (j < steps.size() && (steps[j].perm >= 0 || (steps[j].pair && chain_applies(steps[j].p)))) {
+      if (steps[j].perm < 0) ++R, last = j;
+      ++j;
+    }
     if (R >= 2 && chain_enabled()) {
       ChainRec* recs = static_cast<ChainRec*>(workspace_alloc(R * sizeof(ChainRec), stream));
       try {
         check_cuda(cudaMemsetAsync(recs, 0, R * sizeof(ChainRec), s), "clear chain records");
-        const LayerStep& s0 = steps[i];
-        launch_pair_umma(psi, gate_ptr(s0.g), gate_ptr(s0.g + 1), s0.p, s, PAIR_KRON, &recs[0]);
-        count_launch();
-        for (size_t k = 1; k < R; ++k) {
-          const LayerStep& sk = steps[i + k];
-          launch_pair_chain(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, &recs[k - 1], &recs[k], k + 1 < R);
+        size_t k = 0;
+        for (size_t t = i; t <= last; ++t) {
+          const LayerStep& sk = steps[t];
+          if (sk.perm >= 0) {
+            permute(sk);
+            continue;
+          }
+          double2* psi = static_cast<double2*>(cur);
+          if (k == 0)
+            timed_pass(s, [&] { launch_pair_umma(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, PAIR_KRON, &recs[0]); });
+          else
+            timed_pass(s, [&] {
+              launch_pair_chain(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, &recs[k - 1], &recs[k], k + 1 < R);
+            });
           count_launch();
+          ++k;
         }
         check_cuda(cudaGetLastError(), "gate chain launch");
       } catch (...) {
@@ -389,16 +454,49 @@ void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std:
         throw;
       }
       workspace_free(recs, stream);
-      i = j;
+      i = last + 1;
       continue;
     }
     const LayerStep& st = steps[i];
     if (st.pair)
-      launch_fused_pair(psi, gate_ptr(st.g), gate_ptr(st.g + 1), st.p, n, s);
+      timed_pass(s, [&] { launch_fused_pair(static_cast<double2*>(cur), gate_ptr(st.g), gate_ptr(st.g + 1), st.p,
+                                            product(st.dims), s); });
     else
-      apply_gate_device(state, dims, targets[st.g], gates[st.g], stream);
+      apply_gate_device(cur, st.dims, targets[st.g], gates[st.g], stream);
     ++i;
   }
+  return cur != state;
+}
+
+void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
+                         const std::vector<const void*>& gates, void* stream) {
+  std::vector<GateRun> runs(1);
+  runs[0].targets = targets;
+  runs[0].gates = gates;
+  apply_gate_runs_tc(state, nullptr, dims, runs, stream);
+}
+
+void take_pass_times(double& ms, uint64_t& launches) {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+  {
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    ev.swap(g_pass_events);
+  }
+  ms = 0;
+  launches = ev.size();
+  for (auto& e : ev) {
+    float t = 0;
+    check_cuda(cudaEventSynchronize(e.second), "event synchronize");
+    check_cuda(cudaEventElapsedTime(&t, e.first, e.second), "event elapsed");
+    ms += t;
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+}
+
+void set_pass_timing(bool on) {
+  std::lock_guard<std::mutex> lk(g_pass_mu);
+  g_pass_timing = on;
 }
 
 }  // namespace qtnh_impl

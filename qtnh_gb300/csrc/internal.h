@@ -121,6 +121,19 @@ bool apply_gate_tc_single(void* state, const dims_t& dims, const std::vector<uin
 // Gate list in order; consecutive disjoint two-qubit pairs fused onto the tensor cores.
 void apply_gate_layer_tc(void* state, const dims_t& dims, const std::vector<std::vector<uint16_t>>& targets,
                          const std::vector<const void*>& gates, void* stream);
+// One run of gates of apply_gate_runs_tc, followed by the permutation ptup (none if empty).
+struct GateRun {
+  std::vector<std::vector<uint16_t>> targets;
+  std::vector<const void*> gates;
+  std::vector<uint16_t> ptup;
+};
+// Runs of gates with permutations between them (out of place, state <-> scratch); the
+// fixed-point chain of fused pairs continues across the permutations. Returns whether
+// the result is in scratch.
+bool apply_gate_runs_tc(void* state, void* scratch, dims_t dims, const std::vector<GateRun>& runs, void* stream);
+// CUDA-event timing of the fused gate-pair passes (qtnh_gate_timing).
+void set_pass_timing(bool on);
+void take_pass_times(double& ms, uint64_t& launches);
 // C (M x N) = A (M x K) B (K x N), complex128 row-major, BF16x3 pieces on tcgen05.
 void gemm_bf16x3(const void* A, const void* B, void* C, uint64_t M, uint64_t N, uint64_t K, void* stream);
 // The same with the operand permutes fused into the piece splits (gemm_umma.cu).

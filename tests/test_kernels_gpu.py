@@ -640,3 +640,109 @@ def test_gate_layer_chain_zero_state_and_nonfinite_gate(bf16x6):
     st = dev(psi)
     q.apply_gate_layer(st, [2] * n, [(t, dev(g)) for t, g in big])
     assert rel_l2(host(st), _oracle_layer(psi, n, big)) < REL_TOL
+
+
+# ---- runs of gates separated by permutations (qtnh_apply_gate_runs) -----------------
+
+
+def _oracle_runs(psi, dims, runs):
+    """runs: list of (gates, ptup); the oracle's contractions, then Tensor::permute."""
+    cur = np.asarray(psi, dtype=np.complex128).reshape(-1)
+    dims = list(dims)
+    for gates, pt in runs:
+        t = orc.Tensor(orc.DENSE, [], dims, cur)
+        for targets, els in gates:
+            tdims = [dims[x] for x in targets]
+            t, _, _ = orc.contract(t, orc.Tensor(orc.SYMM, [], tdims * 2, els), [(x, j) for j, x in enumerate(targets)])
+        cur = t.els
+        if pt is not None:
+            cur = orc.permute(cur.reshape(dims), pt).reshape(-1)
+            nd = [0] * len(dims)
+            for i, p in enumerate(pt):
+                nd[p] = dims[i]
+            dims = nd
+    return cur
+
+
+@pytest.mark.parametrize("counts", [[2, 4, 4], [6, 4], [3, 4], [4, 0, 6]], ids=["first", "fixed", "lone", "empty"])
+def test_gate_runs_chain_across_permutations(counts, bf16x6):
+    # the fixed-point chain continues across the permutations: after the first pass (a
+    # permutation of doubles), after a later pass (of 64-bit fixed point), around a lone
+    # gate that ends a run, and across an empty run (two permutations in a row)
+    nrng = np.random.default_rng(50 + len(counts) + counts[0])
+    n = 16
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    psi /= np.linalg.norm(psi)
+    runs = []
+    for j, c in enumerate(counts):
+        gates = _disjoint_pairs(nrng, n, (c + 1) // 2)[:c]
+        pt = [int(x) for x in nrng.permutation(n)] if j + 1 < len(counts) else None
+        runs.append((gates, pt))
+    st, sc = dev(psi), dev(np.zeros_like(psi))
+    res = q.apply_gate_runs(st, sc, [2] * n, [([(t, dev(g)) for t, g in gl], pt) for gl, pt in runs])
+    assert res is (sc if (len(counts) - 1) % 2 else st)
+    out, ref = host(res), _oracle_runs(psi, [2] * n, runs)
+    assert rel_l2(out, ref) < REL_TOL
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < REL_TOL
+    # the same sequence as separate calls (each layer its own chain) agrees to the same level
+    st2, sc2 = dev(psi), dev(np.zeros_like(psi))
+    cur, oth = st2, sc2
+    for gl, pt in runs:
+        if gl:
+            q.apply_gate_layer(cur, [2] * n, [(t, dev(g)) for t, g in gl])
+        if pt is not None:
+            q.permute(cur, [2] * n, pt, out=oth)
+            cur, oth = oth, cur
+    assert rel_l2(out, host(cur)) < REL_TOL
+
+
+def test_gate_runs_mixed_dims(arith):
+    # non-power-of-two dims (general gate kernels, permutations change the dims)
+    nrng = np.random.default_rng(60)
+    dims = [3, 2, 4, 2, 3, 2]
+    psi = crandn(nrng, dims).reshape(-1)
+    pt0 = [2, 0, 5, 1, 3, 4]
+    d1 = [0] * 6
+    for i, p in enumerate(pt0):
+        d1[p] = dims[i]
+    runs = [([([0, 1], haar(nrng, 6).T.reshape(-1)), ([2], haar(nrng, 4).T.reshape(-1))], pt0),
+            ([([d1.index(3), d1.index(4)], haar(nrng, 12).T.reshape(-1))], None)]
+    st, sc = dev(psi), dev(np.zeros_like(psi))
+    res = q.apply_gate_runs(st, sc, dims, [([(t, dev(g)) for t, g in gl], pt) for gl, pt in runs])
+    assert res is sc
+    assert rel_l2(host(res), _oracle_runs(psi, dims, runs)) < REL_TOL
+
+
+def test_gate_runs_checks_before_launch(bf16x6):
+    nrng = np.random.default_rng(61)
+    n = 12
+    psi = crandn(nrng, [2] * n).reshape(-1)
+    gates = [(t, dev(g)) for t, g in _disjoint_pairs(nrng, n, 2)]
+    st, sc = dev(psi), dev(np.zeros_like(psi))
+    bad_perm = list(range(n))
+    bad_perm[3] = 4  # not a permutation
+    with pytest.raises(q.InvalidArgument):
+        q.apply_gate_runs(st, sc, [2] * n, [(gates, bad_perm), (gates, None)])
+    with pytest.raises(q.OutOfRange):
+        q.apply_gate_runs(st, sc, [2] * n, [(gates, list(range(n))), ([([0, n], gates[0][1])], None)])
+    with pytest.raises(q.InvalidArgument):
+        q.apply_gate_runs(st, st, [2] * n, [(gates, list(range(n))), (gates, None)])
+    # nothing was launched: the state is unchanged
+    assert np.array_equal(host(st), psi)
+
+
+@pytest.mark.parametrize("dims,targets", [([3, 2, 3, 2, 2], [0, 1]), ([2, 3, 4, 2], [3, 1, 2]), ([2] * 9, [1, 3, 4, 6, 8]),
+                                          ([5, 3, 2], [0])],
+                         ids=["D6", "D24", "D32", "D5"])
+def test_symmetric_gate_general_sizes(dims, targets, arith):
+    # gate sizes outside the register-blocked kernels (D = 6, 24, 32, 5) take the general kernel
+    nrng = np.random.default_rng(70 + len(targets))
+    psi = crandn(nrng, dims).reshape(-1)
+    D = int(np.prod([dims[t] for t in targets]))
+    els = haar(nrng, D).T.reshape(-1)
+    st = dev(psi)
+    q.apply_gate(st, dims, targets, dev(els))
+    ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], dims, psi),
+                             orc.Tensor(orc.SYMM, [], [dims[t] for t in targets] * 2, els),
+                             [(t, j) for j, t in enumerate(targets)])
+    assert rel_l2(host(st), ref.els) < REL_TOL
