@@ -85,6 +85,15 @@ inline void fill_axis(Axis& a, uint64_t dim, uint64_t s_in, uint64_t s_out) {
   a.s_out = s_out;
 }
 
+// Asynchronous 16-byte copies global -> shared (bypassing L1), in commit groups.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 inline int grid_for(uint64_t work_items, int per_sm) {
   uint64_t cap = (uint64_t)sm_count() * per_sm;
   return (int)(work_items < 1 ? 1 : (work_items < cap ? work_items : cap));

@@ -37,14 +37,6 @@ __device__ __forceinline__ IT pair_base(IT grp, const PairParams& p) {
   return b;
 }
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 // A group's (or a gate row's) largest biased exponent must lie in [TC_EMIN, TC_EMAX]
 // (magnitudes 2^-200 .. 2^201) unless it is 0 (zeros and subnormals only); infinities
 // and NaNs (exponent 0x7FF) fail. Then the level sums, scaled by 2^(Esum - 2060) through

@@ -164,15 +164,19 @@ __global__ void __launch_bounds__(256) gather_permute_kernel(const c128* __restr
 
 // Fused permute and split (the split-precision GEMM's operands): the same transpose, but
 // each element is written as its bf16 pieces into the GEMM's operand planes at (row, k).
-__global__ void __launch_bounds__(TILE_THREADS, 3) tiled_split_kernel(const c128* __restrict__ in,
+// Software-pipelined over two tile buffers: the elements of step j + 1 travel global ->
+// shared by cp.async while the block converts and writes step j, so the loads stay in
+// flight through the piece arithmetic and the scattered plane stores. The bases of the
+// tiles of a step are decoded two steps ahead into one of three slots.
+__global__ void __launch_bounds__(TILE_THREADS, 2) tiled_split_kernel(const c128* __restrict__ in,
                                                                       const __grid_constant__ TileParams p,
                                                                       const bx3::Planes o) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int T = p.T, G = p.G, S = p.tile_slots;
-  c128* tile = reinterpret_cast<c128*>(smem_raw);
-  uint64_t* s_bin = reinterpret_cast<uint64_t*>(tile + (size_t)G * S);
-  uint64_t* s_bout = s_bin + G;
-  int64_t* s_rin = reinterpret_cast<int64_t*>(s_bout + G);
+  const int T = p.T, G = p.G, S = p.tile_slots, GS = G * S;
+  c128* tile = reinterpret_cast<c128*>(smem_raw);  // two buffers of G tiles of S slots
+  uint64_t* s_bin = reinterpret_cast<uint64_t*>(tile + 2 * (size_t)GS);  // [3][G]
+  uint64_t* s_bout = s_bin + 3 * G;                                      // [3][G]
+  int64_t* s_rin = reinterpret_cast<int64_t*>(s_bout + 3 * G);
   int64_t* s_wout = s_rin + T;
   int32_t* s_rslot = reinterpret_cast<int32_t*>(s_wout + T);
   int32_t* s_wslot = s_rslot + T;
@@ -183,50 +187,66 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) tiled_split_kernel(const c128
     s_wslot[t] = p.wslot[t];
   }
   const uint64_t total = p.rest.total;
-  for (uint64_t r0 = (uint64_t)blockIdx.x * G; r0 < total; r0 += (uint64_t)gridDim.x * G) {
+  const uint64_t first = (uint64_t)blockIdx.x * G, stride = (uint64_t)gridDim.x * G;
+  auto elems = [&](uint64_t r0) {  // elements of the step starting at tile r0 (<= STEP_ELEMS)
+    const uint64_t left = total - r0;
+    return (left < (uint64_t)G ? (int)left : G) * T;
+  };
+  auto decode_step = [&](uint64_t r0, int q) {
     for (int g = threadIdx.x; g < G && r0 + g < total; g += blockDim.x) {
       uint64_t bin, bout;
       decode(r0 + g, p.rest, bin, bout);
-      s_bin[g] = bin;
-      s_bout[g] = bout;
+      s_bin[q * G + g] = bin;
+      s_bout[q * G + g] = bout;
     }
-    __syncthreads();
-    const uint64_t left = total - r0;
-    const int n = (left < (uint64_t)G ? (int)left : G) * T;
-    c128 v[TILE_PER_THREAD];
-    int slot[TILE_PER_THREAD];
+  };
+  auto issue = [&](uint64_t r0, int q, c128* buf) {
+    if (r0 < total) {
+      const int n = elems(r0);
 #pragma unroll
-    for (int k = 0; k < TILE_PER_THREAD; ++k) {
-      const int e = threadIdx.x + k * TILE_THREADS;
-      if (e < n) {
-        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-        slot[k] = g * S + s_rslot[t];
-        v[k] = __ldg(in + s_bin[g] + s_rin[t]);
+      for (int k = 0; k < TILE_PER_THREAD; ++k) {
+        const int e = threadIdx.x + k * TILE_THREADS;
+        if (e < n) {
+          const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
+          cp_async16(&buf[g * S + s_rslot[t]], in + s_bin[q * G + g] + s_rin[t]);
+        }
       }
     }
-#pragma unroll
-    for (int k = 0; k < TILE_PER_THREAD; ++k)
-      if (threadIdx.x + k * TILE_THREADS < n) tile[slot[k]] = v[k];
-    __syncthreads();
+    cp_async_commit();  // one group per step (empty past the end), so wait_group 1 is exact
+  };
+  decode_step(first, 0);
+  decode_step(first + stride, 1);
+  __syncthreads();  // tables and the bases of the first two steps
+  issue(first, 0, tile);
+  int j = 0;
+  for (uint64_t r0 = first; r0 < total; r0 += stride, ++j) {
+    c128* cur = tile + (size_t)(j & 1) * GS;
+    const uint64_t* bout = s_bout + (j % 3) * G;
+    issue(r0 + stride, (j + 1) % 3, tile + (size_t)((j + 1) & 1) * GS);
+    cp_async_wait_one();  // this thread's copies of step j have landed
+    __syncthreads();      // and everyone's
+    decode_step(r0 + 2 * stride, (j + 2) % 3);
+    const int n = elems(r0);
     if (p.quad) {
       // four consecutive columns of one row per thread: whole 16-byte chunks
       for (int e = 4 * threadIdx.x; e < n; e += 4 * TILE_THREADS) {
         const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-        const uint64_t rk = s_bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k, k % 4 == 0
+        const uint64_t rk = bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k, k % 4 == 0
         double2 v[4];
 #pragma unroll
-        for (int x = 0; x < 4; ++x) v[x] = tile[g * S + s_wslot[t + x]];
+        for (int x = 0; x < 4; ++x) v[x] = cur[g * S + s_wslot[t + x]];
         bx3::write_pieces4(o, rk >> 32, rk & 0xFFFFFFFFull, v);
       }
     } else {
       for (int e = threadIdx.x; e < n; e += TILE_THREADS) {
         const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-        const uint64_t rk = s_bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k
-        bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, tile[g * S + s_wslot[t]]);
+        const uint64_t rk = bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k
+        bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, cur[g * S + s_wslot[t]]);
       }
     }
-    __syncthreads();
+    __syncthreads();  // buffer j & 1 and base slot j % 3 are free again
   }
+  cp_async_wait_all();
 }
 
 // Fused fallback: one thread per element in output order.
@@ -515,7 +535,9 @@ Plan plan_permute(const dims_t& dims, const std::vector<uint16_t>& ptup, int bou
       if (!inA[i] && !inB[i]) fill_axis(p.rest.ax[nr++], c.dims[i], in_stride[i], out_stride[i]);
     p.rest.n = nr;
     p.rest.total = N / (uint64_t)T;
-    plan.smem = (size_t)p.G * p.tile_slots * sizeof(c128) + 2 * (size_t)p.G * sizeof(uint64_t) +
+    // the fused split double-buffers its tiles and keeps three slots of tile bases
+    const size_t nbuf = boundary >= 0 ? 2 : 1, nbase = boundary >= 0 ? 3 : 1;
+    plan.smem = nbuf * (size_t)p.G * p.tile_slots * sizeof(c128) + 2 * nbase * (size_t)p.G * sizeof(uint64_t) +
                 (size_t)T * (2 * sizeof(int64_t) + 2 * sizeof(int32_t));
     // as many blocks per SM as shared memory and registers allow (at most 4)
     const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (plan.smem + 1024)));
