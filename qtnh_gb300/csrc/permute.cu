@@ -167,10 +167,15 @@ __global__ void __launch_bounds__(256) gather_permute_kernel(const c128* __restr
 // Software-pipelined over two tile buffers: the elements of step j + 1 travel global ->
 // shared by cp.async while the block converts and writes step j, so the loads stay in
 // flight through the piece arithmetic and the scattered plane stores. The bases of the
-// tiles of a step are decoded two steps ahead into one of three slots.
+// tiles of a step are decoded two steps ahead into one of three slots. A thread handles
+// the same positions of the step's tiles at every step, so it keeps their table entries
+// (slots and offsets) in registers. QUAD: write order in aligned quads of consecutive
+// columns (whole 16-byte chunks per piece and row).
+template <bool QUAD>
 __global__ void __launch_bounds__(TILE_THREADS, 2) tiled_split_kernel(const c128* __restrict__ in,
                                                                       const __grid_constant__ TileParams p,
                                                                       const bx3::Planes o) {
+  constexpr int WPT = QUAD ? STEP_ELEMS / (4 * TILE_THREADS) : TILE_PER_THREAD;  // writes per thread and step
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = p.T, G = p.G, S = p.tile_slots, GS = G * S;
   c128* tile = reinterpret_cast<c128*>(smem_raw);  // two buffers of G tiles of S slots
@@ -192,6 +197,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) tiled_split_kernel(const c128
     const uint64_t left = total - r0;
     return (left < (uint64_t)G ? (int)left : G) * T;
   };
+  auto tile_of = [&](int e) { return G > 1 ? e >> p.T_log2 : 0; };
+  auto pos_of = [&](int e) { return G > 1 ? (e & (T - 1)) : e; };
   auto decode_step = [&](uint64_t r0, int q) {
     for (int g = threadIdx.x; g < G && r0 + g < total; g += blockDim.x) {
       uint64_t bin, bout;
@@ -200,48 +207,64 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) tiled_split_kernel(const c128
       s_bout[q * G + g] = bout;
     }
   };
+  decode_step(first, 0);
+  decode_step(first + stride, 1);
+  __syncthreads();  // tables and the bases of the first two steps
+  // this thread's table entries (positions past a full step are never used)
+  const int full = G * T;
+  int32_t rslot[TILE_PER_THREAD];
+  int64_t rin[TILE_PER_THREAD];
+#pragma unroll
+  for (int k = 0; k < TILE_PER_THREAD; ++k) {
+    const int e = threadIdx.x + k * TILE_THREADS;
+    const int t = pos_of(e < full ? e : 0);
+    rslot[k] = tile_of(e) * S + s_rslot[t];
+    rin[k] = s_rin[t];
+  }
+  int32_t wslot[WPT][QUAD ? 4 : 1];
+  int64_t wout[WPT];
+#pragma unroll
+  for (int i = 0; i < WPT; ++i) {
+    const int e = QUAD ? 4 * threadIdx.x + i * 4 * TILE_THREADS : threadIdx.x + i * TILE_THREADS;
+    const int t = pos_of(e < full ? e : 0);
+#pragma unroll
+    for (int x = 0; x < (QUAD ? 4 : 1); ++x) wslot[i][x] = tile_of(e) * S + s_wslot[t + x];
+    wout[i] = s_wout[t];
+  }
   auto issue = [&](uint64_t r0, int q, c128* buf) {
     if (r0 < total) {
       const int n = elems(r0);
 #pragma unroll
       for (int k = 0; k < TILE_PER_THREAD; ++k) {
         const int e = threadIdx.x + k * TILE_THREADS;
-        if (e < n) {
-          const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-          cp_async16(&buf[g * S + s_rslot[t]], in + s_bin[q * G + g] + s_rin[t]);
-        }
+        if (e < n) cp_async16(&buf[rslot[k]], in + s_bin[q * G + tile_of(e)] + rin[k]);
       }
     }
     cp_async_commit();  // one group per step (empty past the end), so wait_group 1 is exact
   };
-  decode_step(first, 0);
-  decode_step(first + stride, 1);
-  __syncthreads();  // tables and the bases of the first two steps
   issue(first, 0, tile);
   int j = 0;
   for (uint64_t r0 = first; r0 < total; r0 += stride, ++j) {
-    c128* cur = tile + (size_t)(j & 1) * GS;
+    const c128* cur = tile + (size_t)(j & 1) * GS;
     const uint64_t* bout = s_bout + (j % 3) * G;
     issue(r0 + stride, (j + 1) % 3, tile + (size_t)((j + 1) & 1) * GS);
     cp_async_wait_one();  // this thread's copies of step j have landed
     __syncthreads();      // and everyone's
     decode_step(r0 + 2 * stride, (j + 2) % 3);
     const int n = elems(r0);
-    if (p.quad) {
-      // four consecutive columns of one row per thread: whole 16-byte chunks
-      for (int e = 4 * threadIdx.x; e < n; e += 4 * TILE_THREADS) {
-        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-        const uint64_t rk = bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k, k % 4 == 0
-        double2 v[4];
 #pragma unroll
-        for (int x = 0; x < 4; ++x) v[x] = cur[g * S + s_wslot[t + x]];
-        bx3::write_pieces4(o, rk >> 32, rk & 0xFFFFFFFFull, v);
-      }
-    } else {
-      for (int e = threadIdx.x; e < n; e += TILE_THREADS) {
-        const int g = G > 1 ? e >> p.T_log2 : 0, t = G > 1 ? e & (T - 1) : e;
-        const uint64_t rk = bout[g] + (uint64_t)s_wout[t];  // (row << 32) + k
-        bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, cur[g * S + s_wslot[t]]);
+    for (int i = 0; i < WPT; ++i) {
+      const int e = QUAD ? 4 * threadIdx.x + i * 4 * TILE_THREADS : threadIdx.x + i * TILE_THREADS;
+      if (e < n) {
+        const uint64_t rk = bout[tile_of(e)] + (uint64_t)wout[i];  // (row << 32) + k
+        if (QUAD) {
+          double2 v[4];
+#pragma unroll
+          for (int x = 0; x < 4; ++x) v[x] = cur[wslot[i][QUAD ? x : 0]];
+          bx3::write_pieces4(o, rk >> 32, rk & 0xFFFFFFFFull, v);
+        } else {
+          bx3::write_pieces(o, rk >> 32, rk & 0xFFFFFFFFull, cur[wslot[i][0]]);
+        }
       }
     }
     __syncthreads();  // buffer j & 1 and base slot j % 3 are free again
@@ -616,10 +639,18 @@ void permute_split_device(const void* in_v, const dims_t& dims, const std::vecto
   if (product(dims) == 0) return;
   Plan plan = plan_permute(dims, ptup, nrow_axes);
   if (plan.kind == Plan::TILED) {
-    if (plan.smem > 48 * 1024)
-      check_cuda(cudaFuncSetAttribute(tiled_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem),
+    if (plan.smem > 48 * 1024) {
+      check_cuda(cudaFuncSetAttribute(tiled_split_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)plan.smem),
                  "tiled_split_kernel shared memory");
-    tiled_split_kernel<<<plan.grid, TILE_THREADS, plan.smem, s>>>(in, *plan.tile, o);
+      check_cuda(cudaFuncSetAttribute(tiled_split_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)plan.smem),
+                 "tiled_split_kernel shared memory");
+    }
+    if (plan.tile->quad)
+      tiled_split_kernel<true><<<plan.grid, TILE_THREADS, plan.smem, s>>>(in, *plan.tile, o);
+    else
+      tiled_split_kernel<false><<<plan.grid, TILE_THREADS, plan.smem, s>>>(in, *plan.tile, o);
   } else {
     gather_split_kernel<<<plan.grid, 256, 0, s>>>(in, plan.gather, o);
   }
