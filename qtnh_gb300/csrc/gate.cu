@@ -194,6 +194,92 @@ __global__ void __launch_bounds__(256, (D <= 4 ? 3 : 1)) gate_kernel_f32x2(c128*
   }
 }
 
+// Gates of 8 or more amplitudes per group: the threads of a block share the groups'
+// amplitudes through shared memory, one thread per (output, group) and GB = 256 / D
+// groups per batch, instead of one thread holding a whole group in registers (which spills
+// in FP64 and leaves one 8-warp block per SM in float-float). Thread t takes group t % GB
+// and output t / GB, so loads and stores run over consecutive groups (coalesced), and the
+// amplitudes are kept transposed in shared memory ([input][group]): a warp reads one
+// input of consecutive groups (no bank conflict) while the gate element is broadcast.
+// FF: float-float arithmetic with the amplitudes split once each; a batch holding an
+// element outside the split range (or any gate element outside it) runs in FP64.
+template <int D, bool FF>
+__global__ void __launch_bounds__(256) gate_coop_kernel(c128* __restrict__ psi, const c128* __restrict__ gate,
+                                                        const __grid_constant__ GateParams p) {
+  constexpr int GB = 256 / D;
+  __shared__ c128 g[D * D];
+  __shared__ df::cf2 gs[FF ? D * D : 1];
+  __shared__ c128 xs[D][GB];
+  __shared__ df::cf2 xsp[FF ? D : 1][GB];
+  __shared__ int gate_ok;
+  if (threadIdx.x == 0) gate_ok = 1;
+  __syncthreads();
+  for (int t = threadIdx.x; t < D * D; t += blockDim.x) {
+    const c128 v = gate[t];
+    g[t] = v;
+    if (FF) {
+      const bool ok = df::in_range_gate(v.x) && df::in_range_gate(v.y);
+      if (!ok) gate_ok = 0;
+      gs[FF ? t : 0] = ok ? df::csplit(v.x, v.y) : df::cf2{{0.f, 0.f}, {0.f, 0.f}};
+    }
+  }
+  __syncthreads();
+  const bool gok = gate_ok != 0;
+  const int gl = threadIdx.x % GB, o = threadIdx.x / GB;
+  const bool active = o < D;  // D * GB <= 256 threads take part
+  const uint64_t ngroups = p.other.total, stride = (uint64_t)gridDim.x * GB;
+  // this thread's amplitude of the batch at g0 (loaded one batch ahead)
+  auto fetch = [&](uint64_t g0, bool& live, uint64_t& addr, c128& x) {
+    const uint64_t grp = g0 + gl;
+    live = active && grp < ngroups;
+    addr = live ? group_base(grp, p) + p.off[o] : 0;
+    x = live ? psi[addr] : make_double2(0.0, 0.0);
+  };
+  bool live;
+  uint64_t addr;
+  c128 x;
+  fetch(blockIdx.x * (uint64_t)GB, live, addr, x);
+  for (uint64_t g0 = blockIdx.x * (uint64_t)GB; g0 < ngroups; g0 += stride) {
+    bool ok = true;
+    if (active) {
+      xs[o][gl] = x;
+      if (FF) {
+        ok = gok && df::in_range_state(x.x) && df::in_range_state(x.y);
+        xsp[FF ? o : 0][gl] = ok ? df::csplit(x.x, x.y) : df::cf2{{0.f, 0.f}, {0.f, 0.f}};
+      }
+    }
+    const bool all_ok = __syncthreads_and(ok);  // the batch's amplitudes are in shared memory
+    bool live_n;
+    uint64_t addr_n;
+    c128 x_n;
+    fetch(g0 + stride, live_n, addr_n, x_n);  // other groups: in flight during the arithmetic
+    if (live) {
+      c128 y;
+      if (FF && all_ok) {
+        df::acc re, im;
+        df::cmul_acc(gs[o], xsp[0][gl], re, im);
+#pragma unroll
+        for (int i = 1; i < D; ++i) {
+          const df::cf2 gi = gs[FF ? i * D + o : 0];
+          const df::cf2 xi = xsp[FF ? i : 0][gl];
+          df::acc_mac(re, gi.re, xi.re);
+          df::acc_mac(re, df::neg(gi.im), xi.im);
+          df::acc_mac(im, gi.re, xi.im);
+          df::acc_mac(im, gi.im, xi.re);
+        }
+        y = make_double2(df::to_double(re), df::to_double(im));
+      } else {
+        y = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int i = 0; i < D; ++i) y = cfma(g[i * D + o], xs[i][gl], y);  // SymmTensor layout [in, out]
+      }
+      psi[addr] = y;
+    }
+    __syncthreads();  // shared copies free for the next batch
+    live = live_n, addr = addr_n, x = x_n;
+  }
+}
+
 struct DiagParams {
   uint64_t n;
   int k;
@@ -502,14 +588,21 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
     if (ff) gate_kernel_f32x2<DD><<<grid, 256, 0, s>>>(psi, g, p);          \
     else gate_kernel<DD><<<grid, 256, 0, s>>>(psi, g, p);                   \
     break;
+#define QTNH_GATE_COOP_CASE(DD)                                                            \
+  case DD: {                                                                               \
+    const int cg = grid_for((p.other.total + 256 / DD - 1) / (256 / DD), 8);               \
+    if (ff) gate_coop_kernel<DD, true><<<cg, 256, 0, s>>>(psi, g, p);                      \
+    else gate_coop_kernel<DD, false><<<cg, 256, 0, s>>>(psi, g, p);                        \
+    break;                                                                                 \
+  }
   switch (D) {
     QTNH_GATE_CASE(1)
     QTNH_GATE_CASE(2)
     QTNH_GATE_CASE(3)
     QTNH_GATE_CASE(4)
-    QTNH_GATE_CASE(8)
-    QTNH_GATE_CASE(9)
-    QTNH_GATE_CASE(16)
+    QTNH_GATE_COOP_CASE(8)
+    QTNH_GATE_COOP_CASE(9)
+    QTNH_GATE_COOP_CASE(16)
     default: {
       // other sizes: the general kernel out of a copy of the state
       GateAnyParams a;
@@ -532,6 +625,7 @@ void apply_gate_device(void* state, const dims_t& dims, const std::vector<uint16
     }
   }
 #undef QTNH_GATE_CASE
+#undef QTNH_GATE_COOP_CASE
   count_launch();
   check_cuda(cudaGetLastError(), "gate_kernel launch");
 }

@@ -16,7 +16,8 @@
 //     for the tile is split into (outer, inner) parts so the tile takes only the inner
 //     part it needs (e.g. an exchange of the top and bottom 3 axes of a 28-axis state:
 //     dims (8, 2^22, 8) become (8, 2^20, 4, 8) and the tile is 8 x 4 x 8). The tile is
-//     staged in shared memory with one padding slot per row; the per-element offsets of
+//     staged in shared memory in XOR-swizzled rows (one padding slot per row where the
+//     row length is not a multiple of 8); the per-element offsets of
 //     the tile come as tables in the kernel parameters (copied to shared memory), and
 //     small tiles are processed several per step so that enough loads are in flight;
 //   * a gather (coalesced stores, indexed loads) when no tile fits.
@@ -492,7 +493,17 @@ Plan plan_permute(const dims_t& dims, const std::vector<uint16_t>& ptup, int bou
     TileParams& p = *plan.tile;
     const int T = (int)(PA * PB);
     p.T = T;
-    p.tile_slots = (int)(PB * (PA + 1));
+    // Shared-memory slot of tile element (a, b), a over the input-contiguous axes. With PA
+    // a multiple of 8, rows are unpadded and the 16-byte slot within each aligned group of
+    // 8 is XOR-swizzled by b ^ (b >> 2): consecutive a (the loads), consecutive b (the
+    // single-element writes) and b = 4j + x over j (the quad writes: lane j reads column
+    // x of its quad) each hit the 8 bank groups once per 8 lanes. Else one padding slot
+    // per row.
+    const bool swz = PA % 8 == 0;
+    auto slot_of = [&](uint64_t a, uint64_t b) {
+      return swz ? (int32_t)(b * PA + (a ^ ((b ^ (b >> 2)) & 7))) : (int32_t)(b * (PA + 1) + a);
+    };
+    p.tile_slots = (int)(swz ? PB * PA : PB * (PA + 1));
     const uint32_t tl = log2_or_none((uint64_t)T);
     p.G = (tl != 0xFFFFFFFFu && T < STEP_ELEMS) ? std::min(STEP_ELEMS / T, 256) : 1;
     p.T_log2 = tl == 0xFFFFFFFFu ? 0 : tl;
@@ -533,7 +544,7 @@ Plan plan_permute(const dims_t& dims, const std::vector<uint16_t>& ptup, int bou
         }
         int t = (int)(b * PA + a);
         p.rin[t] = (int64_t)(offa + offb);
-        p.rslot[t] = (int32_t)(b * (PA + 1) + a);
+        p.rslot[t] = slot_of(a, b);
       }
     }
     // Write order: tile axes by output position, row-major.
@@ -551,7 +562,7 @@ Plan plan_permute(const dims_t& dims, const std::vector<uint16_t>& ptup, int bou
         else b += d * mB[std::find(B.begin(), B.end(), i) - B.begin()];
       }
       p.wout[w] = (int64_t)off;
-      p.wslot[w] = (int32_t)(b * (PA + 1) + a);
+      p.wslot[w] = slot_of(a, b);
     }
     int nr = 0;
     for (int i = 0; i < r; ++i)

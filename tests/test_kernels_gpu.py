@@ -341,9 +341,12 @@ def test_distributed_identity_moves_index():
     assert np.array_equal(out, ref)
 
 
-def test_f32x2_falls_back_to_fp64_out_of_range():
+@pytest.mark.parametrize("targets", [[2, 9], [2, 9, 4], [2, 9, 4, 6]], ids=["D4", "D8", "D16"])
+def test_f32x2_falls_back_to_fp64_out_of_range(targets):
     # tiny and huge magnitudes, zeros and subnormals in one state: groups outside the
     # split range take the FP64 path, the rest the float-float path; all within tolerance
+    # (D = 4: per warp in the register-blocked kernel; D = 8, 16: per batch of groups in
+    # the shared-memory kernel)
     old = q.get_arithmetic()
     q.set_arithmetic(q.ARITH_F32X2)
     try:
@@ -354,12 +357,13 @@ def test_f32x2_falls_back_to_fp64_out_of_range():
         psi[64:128] *= 1e200
         psi[128:160] = 0.0
         psi[160] = 5e-324
-        u = haar(nrng, 4)
+        k = len(targets)
+        u = haar(nrng, 2 ** k)
         els = u.T.reshape(-1)
         st = dev(psi)
-        q.apply_gate(st, [2] * n, [2, 9], dev(els))
-        ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], [2] * n, psi), orc.Tensor(orc.SYMM, [], [2] * 4, els),
-                                 [(2, 0), (9, 1)])
+        q.apply_gate(st, [2] * n, targets, dev(els))
+        ref, _, _ = orc.contract(orc.Tensor(orc.DENSE, [], [2] * n, psi), orc.Tensor(orc.SYMM, [], [2] * (2 * k), els),
+                                 [(t, j) for j, t in enumerate(targets)])
         out = host(st)
         for sl in (slice(0, 64), slice(64, 128), slice(128, 1024)):
             assert rel_l2(out[sl], ref.els[sl]) < REL_TOL
