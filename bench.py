@@ -395,7 +395,7 @@ CONTRACT_METRIC = "contraction TFLOP/s (BF16x3 split precision, FP32 accumulatio
 CPU_GEMM_SAMPLE = (128, 128, 128)
 
 
-def _contract_config(a, pairs):
+def _contract_config(a, pairs, slice_steps=None):
     mnk = [(M, N, K) for _, _, _, M, N, K in pairs]
     return {
         "workload": "%d seeded DenseTensor pairs: ranks 4-6, dims from {2,4,16,32,64}, 2-3 shared indices at random "
@@ -405,6 +405,7 @@ def _contract_config(a, pairs):
         "flop_per_step": float(sum(8.0 * M * N * K for M, N, K in mnk)),
         "max_mnk": [int(x) for x in max(mnk, key=lambda t: t[0] * t[1] * t[2])],
         "element": "complex128 in and out",
+        "split_k_slice_steps": slice_steps,
         "l2_flush": "not needed: the operands of a step (GBs) are far larger than the 129 MB L2",
         "parallelism": "replicas" if a.gpus > 1 else "single GPU",
     }
@@ -653,7 +654,7 @@ def main_contract(a):
             "metric": CONTRACT_METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128 (bf16x3 pieces, fp32 accumulation)",
-            "data": "synthetic (seeded dense pairs, complex Gaussian entries)", "config": _contract_config(a, pairs),
+            "data": "synthetic (seeded dense pairs, complex Gaussian entries)", "config": _contract_config(a, pairs, q.get_gemm_slice()),
             "plain_fp64": {"tflops": flops / (plain_ms * 1e-3) / 1e12, "ms_per_step": plain_ms,
                            "speedup_of_split": (flops / (ms / a.steps * 1e-3)) / (flops / (plain_ms * 1e-3))},
             "plain_oz6": {"tflops": flops / (oz_ms * 1e-3) / 1e12, "ms_per_step": oz_ms,

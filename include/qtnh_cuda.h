@@ -161,6 +161,19 @@ enum { QTNH_GEMM_FP64 = 0, QTNH_GEMM_BF16X3 = 1, QTNH_GEMM_OZ6 = 2 };
 int qtnh_set_gemm_precision(int mode);
 int qtnh_get_gemm_precision(void);
 
+/* K-steps (16 bf16 reals each) accumulated on their own in one split-K slice of the
+ * QTNH_GEMM_BF16X3 GEMM, 1..QTNH_GEMM_SLICE_MAX (default 32; the environment variable
+ * QTNH_GEMM_SLICE sets the initial value). The tensor core's FP32 accumulation loses up to
+ * an ulp per K-step, so the error grows in proportion to the slice length while the FP32
+ * partials written per slice (8 bytes per output element) shrink in inverse proportion:
+ * on the 64-pair precision study, relative L2 vs FP64 2.3e-7 / 4.7e-7 / 1.0e-6 / 2.1e-6
+ * at 16 / 32 / 64 / 128 K-steps, for 134 / 178 / 205 / 215 complex TFLOP/s.
+ * Process-wide. */
+#define QTNH_GEMM_SLICE_DEFAULT 32
+#define QTNH_GEMM_SLICE_MAX 4096
+int qtnh_set_gemm_slice(int k_steps);
+int qtnh_get_gemm_slice(void);
+
 /* CUDA-event timing of the tcgen05 GEMM kernel launches (measurement support): returns
  * the summed duration (ms) and count of the launches recorded since the previous call
  * (synchronizing on them), then enables (enable != 0) or disables recording. */

@@ -289,6 +289,16 @@ def get_gemm_precision():
     return int(lib().qtnh_get_gemm_precision())
 
 
+def set_gemm_slice(k_steps):
+    """K-steps per split-K slice of the BF16x3 GEMM (default 32): longer slices are faster
+    and less accurate (error in proportion to the length)."""
+    check(lib().qtnh_set_gemm_slice(ctypes.c_int(k_steps)))
+
+
+def get_gemm_slice():
+    return int(lib().qtnh_get_gemm_slice())
+
+
 def gemm_timing(enable):
     """(ms, launches) of the tcgen05 GEMM kernel since the last call; then (dis)arm recording."""
     ms, n = ctypes.c_double(), ctypes.c_uint64()

@@ -13,9 +13,11 @@
 // real; the tensor core's FP32 accumulation loses up to an ulp per accumulation step in
 // one direction, so (1) the dominant pair h*h accumulates in its own TMEM accumulator
 // and the five smaller pairs (<= 2^-8 of it) in a second one, and (2) K is split into
-// slices of at most 32 K-steps (512 reals), each accumulated on its own and written as
-// FP32 partials, which a reduction kernel sums with compensated FP32 additions (split-K;
-// it also spreads small GEMMs over all SMs).
+// slices of at most qtnh_get_gemm_slice() K-steps (default 32 = 512 reals), each
+// accumulated on its own and written as FP32 partials, which a reduction kernel sums with
+// compensated FP32 additions (split-K; it also spreads small GEMMs over all SMs). The
+// error grows in proportion to the slice length (relative L2 2.3e-7, 4.7e-7, 1.0e-6,
+// 2.1e-6 at 16, 32, 64, 128 K-steps), the partials' traffic in inverse proportion.
 //
 // Kernels: split_a / split_b write the pieces as bf16 planes in the UMMA K-major
 // core-matrix layout (8 rows x 16 bytes; per tile and K-step of 16 a contiguous block,
@@ -56,7 +58,6 @@ constexpr int GM_STAGE_BYTES = GM_P * (GM_A_BLOCK + GM_B_BLOCK);
 constexpr int GM_THREADS = 192;            // warp 0 producer, warp 1 MMA, warps 2-5 epilogue
 constexpr uint32_t GM_TMEM_COLS = 512;     // accumulators D1 (h*h) and D2 (other pairs), GM_N columns each
 constexpr long long GM_WAIT_CYCLES = 1ll << 32;  // ~2 s at 2 GHz
-constexpr uint32_t GM_SLICE_STEPS = 32;          // K-steps accumulated on their own
 
 // piece pairs (A piece, B piece) with i + j <= 2
 __constant__ uint8_t c_pairs[6][2] = {{0, 0}, {0, 1}, {1, 0}, {0, 2}, {1, 1}, {2, 0}};
@@ -477,8 +478,8 @@ static void gemm_core(const Prep& pa, const Prep& pb, void* Cv, uint64_t M, uint
   p.C = C;
   p.a_plane_bytes = (uint64_t)p.MT * KS * GM_A_BLOCK;
   p.b_plane_bytes = (uint64_t)p.NT * KS * GM_B_BLOCK;
-  p.SK = GM_SLICE_STEPS;
-  p.S = (KS + GM_SLICE_STEPS - 1) / GM_SLICE_STEPS;
+  p.SK = (uint32_t)gemm_slice_steps();
+  p.S = (KS + p.SK - 1) / p.SK;
   const uint64_t planes = GM_P * (p.a_plane_bytes + p.b_plane_bytes);
   const uint64_t part = p.S > 1 ? (uint64_t)p.S * p.MT * GM_M * p.NT * GM_N * sizeof(float) : 0;
   uint8_t* ws = static_cast<uint8_t*>(workspace_alloc(planes + part, stream));

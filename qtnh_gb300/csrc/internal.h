@@ -56,6 +56,7 @@ int guarded_api(const char* name, F&& f) {
 extern std::atomic<uint64_t> g_launches;
 int arithmetic_mode();  // QTNH_ARITH_*
 int gemm_mode();        // QTNH_GEMM_*
+int gemm_slice_steps(); // K-steps per split-K slice of the QTNH_GEMM_BF16X3 GEMM
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 inline uint64_t product(const dims_t& d) {

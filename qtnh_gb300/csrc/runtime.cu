@@ -52,6 +52,19 @@ int gemm_mode() {
   return m;
 }
 
+static std::atomic<int> g_gemm_slice{0};
+
+int gemm_slice_steps() {
+  int k = g_gemm_slice.load(std::memory_order_relaxed);
+  if (k <= 0) {
+    const char* e = std::getenv("QTNH_GEMM_SLICE");
+    k = e ? std::atoi(e) : 0;
+    if (k < 1 || k > QTNH_GEMM_SLICE_MAX) k = QTNH_GEMM_SLICE_DEFAULT;
+    g_gemm_slice.store(k);
+  }
+  return k;
+}
+
 int status_from_current_exception() {
   try {
     throw;
@@ -214,6 +227,16 @@ int qtnh_set_gemm_precision(int mode) {
 }
 
 int qtnh_get_gemm_precision(void) { return gemm_mode(); }
+
+int qtnh_set_gemm_slice(int k_steps) {
+  return QTNH_API([&]() -> int {
+    if (k_steps < 1 || k_steps > QTNH_GEMM_SLICE_MAX) throw Error(QTNH_ERR_INVALID_ARGUMENT, "slice length out of range");
+    g_gemm_slice.store(k_steps);
+    return QTNH_OK;
+  });
+}
+
+int qtnh_get_gemm_slice(void) { return gemm_slice_steps(); }
 
 int qtnh_device_count(int* count) {
   return QTNH_API([&]() -> int {

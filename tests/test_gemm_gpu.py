@@ -165,3 +165,31 @@ def test_split_fused_edge_shapes(d1, d2, wires, bf16x3):
     q.set_gemm_precision(q.GEMM_BF16X3)
     rel, mx = errors(host(split.data), host(plain.data))
     assert rel < 2e-6 and mx < 2e-5, (d1, d2, wires, rel, mx)
+
+
+SLICE_MAX = 4096  # QTNH_GEMM_SLICE_MAX
+
+
+@pytest.mark.parametrize("slice_steps,bound", [(1, 1.5e-7), (16, 5e-7), (64, 2e-6), (SLICE_MAX, 3e-5)])
+def test_split_gemm_slice_length(slice_steps, bound, bf16x3):
+    # K = 4096 complex = 512 K-steps: 512, 32, 8 and 1 slices; the error grows with the
+    # slice length (the tensor core's FP32 accumulation loses up to an ulp per K-step)
+    old = q.get_gemm_slice()
+    assert old == 32
+    q.set_gemm_slice(slice_steps)
+    try:
+        rng = np.random.default_rng(90)
+        M, N, K = 256, 512, 4096
+        a = crandn(rng, (M, K), 1 / np.sqrt(K))
+        b = crandn(rng, (K, N))
+        res, _, _, _ = q.contract(q.Tensor(q.DENSE, [], [M, K], dev(a)), q.Tensor(q.DENSE, [], [K, N], dev(b)),
+                                  [(1, 0)])
+        rel, _ = errors(host(res.data).reshape(M, N), a @ b)
+        assert rel < bound, (slice_steps, rel)
+    finally:
+        q.set_gemm_slice(old)
+    with pytest.raises(q.InvalidArgument):
+        q.set_gemm_slice(0)
+    with pytest.raises(q.InvalidArgument):
+        q.set_gemm_slice(SLICE_MAX + 1)
+    assert q.get_gemm_slice() == old
