@@ -56,6 +56,10 @@ namespace qtnh {
         /// elements are next read, written, copied or fetched.
         void defer(int kind, const std::vector<std::uint16_t>& targets, const std::vector<std::uint64_t>& dims,
                    DeviceArray&& op);
+        /// Queues the permutation ptup of these elements (dims: their current dims; old index
+        /// i moves to ptup[i]) behind the queued applications; it runs with them (moving the
+        /// elements into a new buffer that the array then owns).
+        void defer_permute(const std::vector<std::uint16_t>& ptup, const std::vector<std::uint64_t>& dims);
         /// Runs the queued applications now (on the environment's stream).
         void settle() const;
 
@@ -63,7 +67,7 @@ namespace qtnh {
         void flush() const;
         void pull() const;
         const QTNHEnv* env_ = nullptr;
-        void* dev_ = nullptr;
+        mutable void* dev_ = nullptr;  // settle() may move the elements to a new buffer
         std::size_t n_ = 0;
         mutable std::vector<qtnh::tel> host_;
         mutable bool host_valid_ = false;

@@ -36,21 +36,29 @@ static const std::size_t kKeepMirrorElems = (std::size_t)16 << 20;
 //
 // Tensor::contract(state, gate, wires) with a SymmTensor gate or DiagTensor applied in
 // place (the in-place rule, src/tensor/contract.cpp:250-289) is queued on the state's
-// device array instead of running at once. The queue is applied when the elements are
-// next needed: runs of gates through qtnh_apply_gate_layer (consecutive disjoint two-qubit
-// gates share one pass over the state), runs of one-index diagonals through
-// qtnh_apply_diag_layer (one pass), other diagonals one by one. The queue is keyed by the
-// device pointer, which moves with the array. QTNH_LAZY=0 turns queuing off.
+// device array instead of running at once, and so is Tensor::permute of a DenseTensor
+// (src/tensor/dense.cpp:152-169). The queue is applied when the elements are next needed:
+// runs of gates and permutations through qtnh_apply_gate_runs (consecutive disjoint
+// two-qubit gates share one pass over the state, and the fixed-point chain of the fused
+// passes continues across the permutations, which move the elements between the array
+// and a scratch buffer), runs of one-index diagonals through qtnh_apply_diag_layer (one
+// pass), other diagonals one by one. The queue is keyed by the device pointer, which
+// moves with the array; applying it may leave the elements in the scratch buffer, which
+// the array then owns. QTNH_LAZY=0 turns queuing off.
+
+// Kind of a queued permutation: targets hold the permutation tuple, no operand.
+constexpr int kDeferPermute = -1;
 
 struct DeferredOp {
   int kind;
-  std::vector<uint16_t> targets;
+  std::vector<uint16_t> targets;  // the wired indices, or the permutation tuple
+  std::vector<uint64_t> dims;     // the elements' dims when the operation applies
   DeviceArray op;
 };
 
 struct DeferredQueue {
   const QTNHEnv* env = nullptr;
-  std::vector<uint64_t> dims;
+  std::vector<uint64_t> dims;  // the dims after every queued operation
   std::vector<DeferredOp> ops;
 };
 
@@ -76,22 +84,27 @@ static void drop_queue(const void* dev) {
 // A one-index diagonal whose index was last touched, in queue order, by a gate is folded
 // into that gate (qtnh_symm_diag_product, in place on the queued gate, which the
 // contraction consumed): the diagonal commutes with everything between them, and the
-// gate runs on both sides of it join into one fused run. Diagonals on an index whose
-// last toucher is not a gate, or that no earlier queued operation touches, stay.
+// gate runs on both sides of it join into one fused run. A queued permutation between
+// them maps the index back to its position before the permutation. Diagonals on an index
+// whose last toucher is not a gate, or that no earlier queued operation touches, stay.
 static void fold_diagonals(DeferredQueue& q) {
   void* st = q.env->stream;
   std::vector<char> gone(q.ops.size(), 0);
   for (std::size_t i = 0; i < q.ops.size(); ++i) {
     if (q.ops[i].kind != QTNH_KIND_DIAG || q.ops[i].targets.size() != 1) continue;
-    const uint16_t x = q.ops[i].targets[0];
+    uint16_t x = q.ops[i].targets[0];
     for (std::size_t j = i; j-- > 0;) {
       if (gone[j]) continue;
       const auto& tg = q.ops[j].targets;
+      if (q.ops[j].kind == kDeferPermute) {  // old index k moved to tg[k]
+        x = (uint16_t)(std::find(tg.begin(), tg.end(), x) - tg.begin());
+        continue;
+      }
       const auto it = std::find(tg.begin(), tg.end(), x);
       if (it == tg.end()) continue;
       if (q.ops[j].kind == QTNH_KIND_SYMM) {
         std::vector<uint64_t> td;
-        for (uint16_t t : tg) td.push_back(q.dims[t]);
+        for (uint16_t t : tg) td.push_back(q.ops[j].dims[t]);
         check(qtnh_symm_diag_product(q.ops[j].op.read(), (int32_t)tg.size(), td.data(), (int32_t)(it - tg.begin()),
                                      q.ops[i].op.read(), q.ops[j].op.write(), st));
         gone[i] = 1;
@@ -108,46 +121,64 @@ static void fold_diagonals(DeferredQueue& q) {
   q.ops.resize(k);
 }
 
-static void apply_queue(void* dev, DeferredQueue& q) {
+// Applies the queue to the elements at `cur`; permutations move them between cur and
+// scratch (allocated on the first one), so cur ends where the result is.
+static void apply_queue(void*& cur, void*& scratch, std::size_t n, DeferredQueue& q) {
   fold_diagonals(q);
-  const int32_t rank = (int32_t)q.dims.size();
   void* st = q.env->stream;
   std::size_t i = 0;
   while (i < q.ops.size()) {
     std::size_t j = i;
-    if (q.ops[i].kind == QTNH_KIND_SYMM) {
-      while (j < q.ops.size() && q.ops[j].kind == QTNH_KIND_SYMM) ++j;
-      std::vector<int32_t> ks;
-      std::vector<uint16_t> tg;
+    const std::vector<uint64_t>& dims = q.ops[i].dims;
+    const int32_t rank = (int32_t)dims.size();
+    if (q.ops[i].kind == QTNH_KIND_SYMM || q.ops[i].kind == kDeferPermute) {
+      // gates in runs separated by permutations, one call
+      std::vector<int32_t> per_run(1, 0), ks;
+      std::vector<uint16_t> tg, ptups;
       std::vector<const void*> ptrs;
-      for (std::size_t g = i; g < j; ++g) {
-        ks.push_back((int32_t)q.ops[g].targets.size());
-        tg.insert(tg.end(), q.ops[g].targets.begin(), q.ops[g].targets.end());
-        ptrs.push_back(q.ops[g].op.read());
+      for (; j < q.ops.size() && (q.ops[j].kind == QTNH_KIND_SYMM || q.ops[j].kind == kDeferPermute); ++j) {
+        const DeferredOp& o = q.ops[j];
+        if (o.kind == kDeferPermute) {
+          ptups.insert(ptups.end(), o.targets.begin(), o.targets.end());
+          per_run.push_back(0);
+          continue;
+        }
+        ++per_run.back();
+        ks.push_back((int32_t)o.targets.size());
+        tg.insert(tg.end(), o.targets.begin(), o.targets.end());
+        ptrs.push_back(o.op.read());
       }
-      check(qtnh_apply_gate_layer(dev, rank, q.dims.data(), (int32_t)ks.size(), ks.data(), tg.data(), ptrs.data(), st));
+      const int32_t nruns = (int32_t)per_run.size();
+      if (nruns == 1) {
+        check(qtnh_apply_gate_layer(cur, rank, dims.data(), (int32_t)ks.size(), ks.data(), tg.data(), ptrs.data(), st));
+      } else {
+        if (!scratch) check(qtnh_malloc_async(&scratch, std::max<std::size_t>(n, 1) * sizeof(tel), st));
+        check(qtnh_apply_gate_runs(cur, scratch, rank, dims.data(), nruns, per_run.data(), ks.data(), tg.data(),
+                                   ptrs.data(), ptups.data(), st));
+        if ((nruns - 1) % 2) std::swap(cur, scratch);
+      }
     } else if (q.ops[i].targets.size() == 1) {
       while (j < q.ops.size() && q.ops[j].kind == QTNH_KIND_DIAG && q.ops[j].targets.size() == 1) ++j;
       if (j - i == 1) {
-        check(qtnh_apply_diag(dev, rank, q.dims.data(), 1, q.ops[i].targets.data(), q.ops[i].op.read(), st));
+        check(qtnh_apply_diag(cur, rank, dims.data(), 1, q.ops[i].targets.data(), q.ops[i].op.read(), st));
       } else {
         // the one-index diagonals of the run, concatenated for one streaming pass
         std::vector<uint16_t> axes;
         std::size_t total = 0;
-        for (std::size_t g = i; g < j; ++g) axes.push_back(q.ops[g].targets[0]), total += q.dims[q.ops[g].targets[0]];
+        for (std::size_t g = i; g < j; ++g) axes.push_back(q.ops[g].targets[0]), total += dims[q.ops[g].targets[0]];
         DeviceArray factors(*q.env, total);
         char* f = static_cast<char*>(factors.write());
         std::size_t off = 0;
         for (std::size_t g = i; g < j; ++g) {
-          const std::size_t n = q.dims[q.ops[g].targets[0]];
-          check(qtnh_memcpy_d2d(f + off * sizeof(tel), q.ops[g].op.read(), n * sizeof(tel), st));
-          off += n;
+          const std::size_t len = dims[q.ops[g].targets[0]];
+          check(qtnh_memcpy_d2d(f + off * sizeof(tel), q.ops[g].op.read(), len * sizeof(tel), st));
+          off += len;
         }
-        check(qtnh_apply_diag_layer(dev, rank, q.dims.data(), (int32_t)axes.size(), axes.data(), factors.read(), st));
+        check(qtnh_apply_diag_layer(cur, rank, dims.data(), (int32_t)axes.size(), axes.data(), factors.read(), st));
       }
     } else {
       ++j;
-      check(qtnh_apply_diag(dev, rank, q.dims.data(), (int32_t)q.ops[i].targets.size(), q.ops[i].targets.data(),
+      check(qtnh_apply_diag(cur, rank, dims.data(), (int32_t)q.ops[i].targets.size(), q.ops[i].targets.data(),
                             q.ops[i].op.read(), st));
     }
     i = j;
@@ -164,7 +195,18 @@ void DeviceArray::settle() const {
     q = std::move(it->second);
     deferred_queues().erase(it);
   }
-  apply_queue(dev_, q);  // the operands are freed (stream-ordered) after their kernels
+  // the operands are freed (stream-ordered) after their kernels
+  void* cur = dev_;
+  void* scratch = nullptr;
+  try {
+    apply_queue(cur, scratch, n_, q);
+  } catch (...) {
+    if (scratch && scratch != dev_) qtnh_free_async(scratch, env_->stream);
+    if (cur != dev_) qtnh_free_async(cur, env_->stream);  // (not reached: cur moves only after a call succeeded)
+    throw;
+  }
+  if (cur != dev_) dev_ = cur;  // the elements ended in the scratch buffer: scratch is the old array
+  if (scratch) qtnh_free_async(scratch, env_->stream);
 }
 
 static bool lazy_enabled() {
@@ -175,6 +217,21 @@ static bool lazy_enabled() {
   return on;
 }
 
+// Appends an operation on elements of dims `dims` (the tensor's current dims) that leaves
+// them with dims `after`; returns the queue length.
+static std::size_t enqueue(const void* dev, const QTNHEnv* env, DeferredOp&& op, const std::vector<uint64_t>& after) {
+  std::lock_guard<std::mutex> lk(g_deferred_mu);
+  DeferredQueue& q = deferred_queues()[dev];
+  if (q.ops.empty()) {
+    q.env = env;
+  } else if (q.dims != op.dims) {
+    throw std::logic_error("queued contractions on differently shaped elements");
+  }
+  q.dims = after;
+  q.ops.push_back(std::move(op));
+  return q.ops.size();
+}
+
 void DeviceArray::defer(int kind, const std::vector<uint16_t>& targets, const std::vector<uint64_t>& dims,
                         DeviceArray&& op) {
   if (!dev_) throw std::runtime_error("tensor has no storage");
@@ -183,19 +240,24 @@ void DeviceArray::defer(int kind, const std::vector<uint16_t>& targets, const st
   host_.clear();
   host_.shrink_to_fit();
   op.flush();
-  std::size_t queued = 0;
-  {
-    std::lock_guard<std::mutex> lk(g_deferred_mu);
-    DeferredQueue& q = deferred_queues()[dev_];
-    if (q.ops.empty()) {
-      q.env = env_;
-      q.dims = dims;
-    } else if (q.dims != dims) {
-      throw std::logic_error("queued contractions on differently shaped elements");
-    }
-    q.ops.push_back(DeferredOp{kind, targets, std::move(op)});
-    queued = q.ops.size();
+  const std::size_t queued = enqueue(dev_, env_, DeferredOp{kind, targets, dims, std::move(op)}, dims);
+  if (queued >= kMaxDeferred || !lazy_enabled()) settle();
+}
+
+void DeviceArray::defer_permute(const std::vector<uint16_t>& ptup, const std::vector<uint64_t>& dims) {
+  if (!dev_) throw std::runtime_error("tensor has no storage");
+  std::vector<uint64_t> after(dims.size());
+  std::vector<char> seen(dims.size(), 0);
+  if (ptup.size() != dims.size()) throw std::invalid_argument("permutation tuple size differs from tensor rank");
+  for (std::size_t i = 0; i < ptup.size(); ++i) {
+    if (ptup[i] >= dims.size() || seen[ptup[i]]++) throw std::invalid_argument("permutation tuple is not a permutation");
+    after[ptup[i]] = dims[i];
   }
+  flush();
+  host_valid_ = false;
+  host_.clear();
+  host_.shrink_to_fit();
+  const std::size_t queued = enqueue(dev_, env_, DeferredOp{kDeferPermute, ptup, dims, DeviceArray()}, after);
   if (queued >= kMaxDeferred || !lazy_enabled()) settle();
 }
 

@@ -210,10 +210,9 @@ DenseTensor* DenseTensor::permute(std::vector<tidx_tup_st> ptup) {
   if (ptup.size() != dims.size()) throw std::out_of_range("permutation tuple has the wrong length");
   tidx_tup nd(dims.size());
   for (std::size_t i = 0; i < dims.size(); ++i) nd.at(ptup[i]) = dims[i];
-  DeviceArray out(bc_.env, els_.size());
-  auto d = u64(dims);
-  check(qtnh_permute(els_.read(), out.write(), (int32_t)d.size(), d.data(), ptup.data(), bc_.env.stream));
-  els_ = std::move(out);
+  // queued behind any in-place contractions on the elements, so that gate runs on both
+  // sides of it are applied in one call (qtnh_apply_gate_runs)
+  els_.defer_permute(ptup, u64(dims));
   auto parts = utils::split_dims(nd, (tidx_tup_st)dis_dims_.size());
   dis_dims_ = parts.first;
   loc_dims_ = parts.second;

@@ -492,6 +492,75 @@ static void test_queued_contractions(QTNHEnv& env) {
     sw[x] = ref[utils::idxs_to_i(idx, tidx_tup(n, 2))];
   }
   REQUIRE(close(*st, sw));
+  // a permutation queued between gates (DeviceArray::defer_permute): the gate runs on both
+  // sides of it are applied in one call (at 12 qubits one fixed-point chain on the tensor
+  // cores), a one-index diagonal after it folds into a gate before it (on the index it
+  // came from), two permutations in a row, and a permutation with nothing else queued
+  {
+    const int m = 12;
+    const std::size_t M = (std::size_t)1 << m;
+    const tidx_tup dm(m, 2);
+    std::vector<tel> phi(M);
+    for (std::size_t i = 0; i < M; ++i) phi[i] = tel(std::cos(0.11 * i + 0.3), std::sin(0.7 * i));
+    auto permute_host = [&](const std::vector<tel>& v, const std::vector<tidx_tup_st>& pt) {
+      std::vector<tel> out(M);
+      for (std::size_t x = 0; x < M; ++x) {
+        const auto idx = utils::i_to_idxs(x, dm);
+        tidx_tup nidx(m);
+        for (int i = 0; i < m; ++i) nidx[pt[i]] = idx[i];
+        out[utils::idxs_to_i(nidx, dm)] = v[x];
+      }
+      return out;
+    };
+    auto close_m = [&](Tensor& t, const std::vector<tel>& r) {
+      double big = 0;
+      for (auto& v : r) big = std::max(big, std::abs(v));
+      bool ok = t.totDims() == dm;
+      for (std::size_t i = 0; ok && i < M; ++i) ok = std::abs(t.at(utils::i_to_idxs(i, dm)) - r[i]) <= 1e-12 * big;
+      return ok;
+    };
+    auto apply_gate = [&](tptr t, std::vector<tel>& r, int a, int b, int seed) {
+      r = apply_plain(r, m, {a, b}, gate(seed));
+      return Tensor::contract(std::move(t), SymmTensor::make(env, {}, {2, 2, 2, 2}, 0, gate(seed)),
+                              {{(tidx_tup_st)a, 0}, {(tidx_tup_st)b, 1}});
+    };
+    auto permute = [&](tptr t, std::vector<tel>& r, const std::vector<tidx_tup_st>& pt) {
+      r = permute_host(r, pt);
+      return Tensor::permute(std::move(t), pt);
+    };
+    std::vector<tidx_tup_st> rot(m), rev(m), sw05(m);
+    for (int i = 0; i < m; ++i) rot[i] = (tidx_tup_st)((i + 3) % m), rev[i] = (tidx_tup_st)(m - 1 - i), sw05[i] = i;
+    std::swap(sw05[0], sw05[5]);
+    tptr pt = DenseTensor::make(env, {}, dm, std::vector<tel>(phi));
+    std::vector<tel> pref = phi;
+    pt = apply_gate(std::move(pt), pref, 0, 5, 11);
+    pt = apply_gate(std::move(pt), pref, 2, 3, 12);
+    pt = apply_gate(std::move(pt), pref, 7, 9, 13);
+    pt = apply_gate(std::move(pt), pref, 10, 11, 14);
+    pt = permute(std::move(pt), pref, rot);  // old index i -> (i + 3) % 12
+    pt = apply_gate(std::move(pt), pref, 1, 4, 15);
+    pt = apply_gate(std::move(pt), pref, 6, 8, 16);
+    pt = apply_gate(std::move(pt), pref, 2, 11, 17);
+    pt = apply_gate(std::move(pt), pref, 0, 3, 18);
+    // index 10 came from index 7, last touched by the gate on (7, 9): folded into it
+    const std::vector<tel> d = {std::exp(0.45i), std::exp(-0.8i)};
+    pt = Tensor::contract(std::move(pt), DiagTensor::make(env, {}, {2, 2}, 0, false, std::vector<tel>(d)), {{10, 0}});
+    pref = apply_plain(pref, m, {10}, {d[0], 0.0, 0.0, d[1]});
+    pt = permute(std::move(pt), pref, rev);
+    pt = permute(std::move(pt), pref, sw05);
+    pt = apply_gate(std::move(pt), pref, 3, 7, 19);
+    REQUIRE(close_m(*pt, pref));
+    pt = permute(std::move(pt), pref, rot);
+    REQUIRE(close_m(*pt, pref));
+    std::vector<tidx_tup_st> bad(m, 0);
+    bool threw = false;
+    try {
+      pt = Tensor::permute(std::move(pt), bad);
+    } catch (const std::invalid_argument&) {
+      threw = true;
+    }
+    REQUIRE(threw);
+  }
   // a state dropped with gates still queued, then a fresh one: nothing leaks into it
   {
     tptr tmp = DenseTensor::make(env, {}, tidx_tup(n, 2), std::vector<tel>(psi));
