@@ -4,12 +4,14 @@
 // (src/tensor/contract.cpp:250-289), the result keeps the state's index order and each
 // gate output replaces the state index wired to the matching input. The reference still
 // runs the generic permute -> triple loop -> permute path (contract.cpp:12-201) through
-// per-element iterator objects. Here it is a register-blocked kernel: each thread owns
-// one group of D = prod(target dims) amplitudes (all other indices fixed), loads them
-// with 128-bit loads, applies the D x D gate from shared memory and stores them back.
-// Consecutive threads own consecutive groups, so loads and stores are coalesced unless a
-// target is the innermost index, in which case every thread touches D contiguous
-// elements.
+// per-element iterator objects. Here, for D = prod(target dims) <= 4, it is a
+// register-blocked kernel: each thread owns one group of D amplitudes (all other indices
+// fixed), loads them with 128-bit loads, applies the D x D gate from shared memory and
+// stores them back. Consecutive threads own consecutive groups, so loads and stores are
+// coalesced unless a target is the innermost index, in which case every thread touches D
+// contiguous elements. For D = 8, 9 and 16 the threads of a block share the groups
+// through shared memory, one thread per (output, group) (gate_coop_kernel); any other D
+// runs a general FP64 kernel out of a copy of the state (gate_kernel_any).
 //
 // DiagTensor contraction (the reference stubs DiagTensor: src/tensor/diag.cpp:65-117)
 // is defined as contraction with D[in, out] = d[in] * delta(in, out); with the in-place
