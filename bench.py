@@ -303,7 +303,7 @@ def _qft_oracle_seconds(n, dq, seed):
 
 
 def main_qft(a):
-    """configs[0]: the QFT network on n=16 through the C++ API; every run copies the state in
+    """The reference example's QFT network on n=16 through the C++ API; every run copies the state in
     (DenseTensor::make) and the result out, so value and e2e are the same measurement."""
     import numpy as np
     from qtnh_gb300 import build as bld
