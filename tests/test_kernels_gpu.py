@@ -750,3 +750,25 @@ def test_symmetric_gate_general_sizes(dims, targets, arith):
                              orc.Tensor(orc.SYMM, [], [dims[t] for t in targets] * 2, els),
                              [(t, j) for j, t in enumerate(targets)])
     assert rel_l2(host(st), ref.els) < REL_TOL
+
+
+def test_gate_timing_counts_fused_passes():
+    # qtnh_gate_timing: one timed launch per fused pair pass (the first pass of the chain
+    # and the chain passes), none for permutations; recording off afterwards
+    old = q.get_arithmetic()
+    q.set_arithmetic(q.ARITH_BF16X6)
+    try:
+        nrng = np.random.default_rng(62)
+        n = 14
+        psi = crandn(nrng, [2] * n).reshape(-1)
+        gates = [(t, dev(g)) for t, g in _disjoint_pairs(nrng, n, 5)]  # 10 gates: 5 pair passes
+        st, sc = dev(psi), dev(np.zeros_like(psi))
+        q.gate_timing(False)
+        q.gate_timing(True)
+        q.apply_gate_runs(st, sc, [2] * n, [(gates[:4], list(range(n))[::-1]), (gates[4:], None)])
+        ms, launches = q.gate_timing(False)
+        assert launches == 5 and ms > 0
+        q.apply_gate_layer(st, [2] * n, gates[:2])
+        assert q.gate_timing(False) == (0.0, 0)
+    finally:
+        q.set_arithmetic(old)
