@@ -123,12 +123,28 @@ struct ChainRec {
 constexpr int CHAIN_RANGE = 6;
 
 
+// A permutation of a power-of-two state as a permutation of the bits of the element index
+// (states of at most 2^32 elements): P(x) = the OR over the index's four bytes of
+// tab[k][byte k], and poff[c] = P(off[c]) for the pair's 16 amplitude offsets. P is
+// linear over disjoint bit sets, so P(base | off) = P(base) | P(off).
+struct BitPerm {
+  uint32_t tab[4][256];
+  uint32_t poff[16];
+};
+// The bit tables of the permutation ptup (Tensor::permute convention) of a state of dims
+// `dims` and the pair's permuted offsets; false if the dims are not all powers of two or the
+// state has more than 2^32 elements.
+bool make_bit_perm(const dims_t& dims, const std::vector<uint16_t>& ptup, const PairParams& p, BitPerm& bp);
+
 // Whether the chain kernel takes a pair of this shape (the tcgen05 tile shape).
 bool chain_applies(const PairParams& p);
 // A later pass of a chain (two disjoint two-qubit gates): reads what rin describes, writes
-// fixed point (want_fixed, when the scales allow) or doubles, and records it in rout.
+// fixed point (want_fixed, when the scales allow) or doubles, and records it in rout. With
+// `perm` (host memory) it writes out of place, to `out`, with every element at its index
+// under the permutation (the pass and the permutation after it in one pass over the state).
 void launch_pair_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
-                       const ChainRec* rin, ChainRec* rout, bool want_fixed);
+                       const ChainRec* rin, ChainRec* rout, bool want_fixed, void* out = nullptr,
+                       const BitPerm* perm = nullptr);
 
 // Reads and clears the tcgen05 kernel's device error flags (bounded waits that expired).
 uint32_t take_umma_error();

@@ -327,6 +327,15 @@ struct LayerStep {
   dims_t dims;     // the state's dims at this step (before the permutation)
 };
 
+// QTNH_FUSE_PERMUTE=0 keeps a permutation after a chain pass as a pass of its own.
+bool fuse_permutes() {
+  static const bool on = [] {
+    const char* e = std::getenv("QTNH_FUSE_PERMUTE");
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 // Optional CUDA-event timing of the tensor-core gate-pass launches (qtnh_gate_timing).
 std::mutex g_pass_mu;
 bool g_pass_timing = false;
@@ -431,30 +440,39 @@ bool apply_gate_runs_tc(void* state, void* scratch, dims_t dims, const std::vect
       ChainRec* recs = static_cast<ChainRec*>(workspace_alloc(R * sizeof(ChainRec), stream));
       try {
         check_cuda(cudaMemsetAsync(recs, 0, R * sizeof(ChainRec), s), "clear chain records");
-        size_t k = 0;
-        for (size_t t = i; t <= last; ++t) {
+        size_t k = 0, t = i;
+        for (; t <= last; ++t) {
           const LayerStep& sk = steps[t];
           if (sk.perm >= 0) {
             permute(sk);
             continue;
           }
           double2* psi = static_cast<double2*>(cur);
+          // a chain pass followed by a permutation writes its outputs permuted, out of place
+          BitPerm bp;
+          const bool fuse = k > 0 && t + 1 < steps.size() && steps[t + 1].perm >= 0 && fuse_permutes() &&
+                            make_bit_perm(steps[t + 1].dims, runs[(size_t)steps[t + 1].perm].ptup, sk.p, bp);
           if (k == 0)
             timed_pass(s, [&] { launch_pair_umma(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, PAIR_KRON, &recs[0]); });
           else
             timed_pass(s, [&] {
-              launch_pair_chain(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, &recs[k - 1], &recs[k], k + 1 < R);
+              launch_pair_chain(psi, gate_ptr(sk.g), gate_ptr(sk.g + 1), sk.p, s, &recs[k - 1], &recs[k], k + 1 < R,
+                                fuse ? oth : nullptr, fuse ? &bp : nullptr);
             });
           count_launch();
           ++k;
+          if (fuse) {
+            std::swap(cur, oth);
+            ++t;  // the permutation is done
+          }
         }
         check_cuda(cudaGetLastError(), "gate chain launch");
+        i = t;
       } catch (...) {
         workspace_free(recs, stream);
         throw;
       }
       workspace_free(recs, stream);
-      i = last + 1;
       continue;
     }
     const LayerStep& st = steps[i];

@@ -467,6 +467,8 @@ struct ChSmem {
   int gate_ok;
   int abort;
   int no_abort;                         // stays 0: the final wait for in-flight MMAs
+  uint32_t ptab[4][256];                // PO: the permutation's bit tables (BitPerm)
+  uint32_t poff[16];                    // PO: the permuted amplitude offsets
 };
 static_assert(CH_NLMAX * UM_N <= (int)CH_ACC, "chain level sums exceed an accumulator set");
 static_assert(2 * CH_ACC <= CH_TMEM_COLS, "two accumulator sets");
@@ -492,19 +494,37 @@ static_assert(sizeof(ChSmem) + 1024 <= 227 * 1024, "chain shared memory");
 // buffer m % 2 after the team waited (in iteration m - 1) for the MMAs of tile m - 2 that
 // read it; the MMAs of tile m overwrite set m % 2 after every thread arrived on full for
 // tile m, i.e. after its reads of tile m - 2's sums (tcgen05.fence before the arrive).
-template <typename IT, uint32_t MODE, int NL>
+//
+// PO (permuted output, IT = uint32_t): the outputs go out of place to outv, element x to
+// index P(x) of the permutation `perm` (bit tables in shared memory; P(tile part | row
+// part | offset) is the OR of the three parts' images, the row part's and the offsets'
+// computed once), so the pass and the permutation after it take one pass over the state.
+template <typename IT, uint32_t MODE, int NL, bool PO>
 __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __restrict__ psiv,
                                                                         const double2* __restrict__ ga,
                                                                         const double2* __restrict__ gb,
                                                                         const __grid_constant__ PairParams p,
                                                                         const ChainRec* __restrict__ rin,
-                                                                        ChainRec* __restrict__ rout, int want_fixed) {
+                                                                        ChainRec* __restrict__ rout, int want_fixed,
+                                                                        void* __restrict__ outv,
+                                                                        const BitPerm* __restrict__ perm) {
+  static_assert(!PO || sizeof(IT) == 4, "permuted output for states of at most 2^32 elements");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   ChSmem& sm = *reinterpret_cast<ChSmem*>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint64_t ntiles = p.ngroups / UM_M;
-  double2* psi = static_cast<double2*>(psiv);
-  int64_t* psy = static_cast<int64_t*>(psiv);
+  const double2* psi = static_cast<const double2*>(psiv);
+  const int64_t* psy = static_cast<const int64_t*>(psiv);
+  double2* pso = static_cast<double2*>(PO ? outv : psiv);  // where the outputs go
+  int64_t* pyo = static_cast<int64_t*>(PO ? outv : psiv);
+  if (PO) {
+    for (int t = tid; t < 4 * 256; t += CH_THREADS) (&sm.ptab[0][0])[t] = (&perm->tab[0][0])[t];
+    if (tid < 16) sm.poff[tid] = perm->poff[tid];
+  }
+  // the image of a (tile or row) part of an element index under the permutation
+  auto pimg = [&](uint32_t x) -> uint32_t {
+    return sm.ptab[0][x & 255u] | sm.ptab[1][(x >> 8) & 255u] | sm.ptab[2][(x >> 16) & 255u] | sm.ptab[3][x >> 24];
+  };
 
   // ---- setup as the pair kernel: barriers, tensor memory, the fused gate and its digits ----
   if (tid == 0) {
@@ -607,11 +627,15 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
                         : psi[ix];
       }
       uint32_t gkey = 0;
+      const uint32_t pbase = PO ? pimg((uint32_t)gbase) : 0u;
 #pragma unroll 1
       for (int o = 0; o < 16; ++o) {
         const double2 v = group_output_fp64(sm.U16, x, o);
         gkey = max(gkey, amp_key(v));
-        psi[gbase + (IT)p.off[o]] = v;
+        if (PO)
+          pso[pbase | sm.poff[o]] = v;
+        else
+          pso[gbase + (IT)p.off[o]] = v;
       }
       okey = max(okey, gkey);
       if (gkey) ominc = max(ominc, 2047u - oz::key_exponent(gkey));
@@ -636,6 +660,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     // group base of row r of tile T = pair_base(T * 128) | pair_base(r): zero bits are inserted
     // into the tile's bits and the row's bits of the group index independently
     const IT rbase = pair_base<IT>((IT)r, p);
+    const uint32_t prbase = PO ? pimg((uint32_t)rbase) : 0u;  // the row part's image
     auto tile_part = [&](uint64_t T) -> IT { return pair_base<IT>((IT)(T * UM_M), p); };
     // per output 4h + a: the row shift to the common output scale (fixed point), 8 bits
     // each, and the row's scale exponent (0 and max_erow when all rows share one scale)
@@ -656,6 +681,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
     // whose tile part is tb
     auto recombine = [&](IT tb, uint32_t b) {
       const IT gbase = tb | rbase;
+      const uint32_t obase = PO ? (pimg((uint32_t)tb) | prbase) : 0u;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * CH_ACC + (uint32_t)(8 * h);
       uint32_t v[NL][8];  // level l, output real 8h + 2a + part
 #pragma unroll
@@ -672,7 +698,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
         } else {
           Tr = oz::fixed_levels<NL>(cr), Ti = oz::fixed_levels<NL>(ci);
         }
-        const IT ix = gbase + (IT)p.off[4 * h + a];
+        const IT ix = PO ? (IT)(obase | sm.poff[4 * h + a]) : gbase + (IT)p.off[4 * h + a];
         if (out_fixed) {
           int64_t Yr = Tr, Yi = Ti;
           if (!common) {
@@ -681,12 +707,12 @@ __global__ void __launch_bounds__(CH_THREADS, 1) gate_pair_chain_kernel(void* __
             Yr = (Tr + rh) >> k, Yi = (Ti + rh) >> k;
           }
           ohi |= oz::fixed_hi_mag(Yr) | oz::fixed_hi_mag(Yi);  // its bit length is the largest's
-          *reinterpret_cast<longlong2*>(psy + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
+          *reinterpret_cast<longlong2*>(pyo + 2 * (uint64_t)ix) = make_longlong2(Yr, Yi);
         } else {
           const int e = (common ? max_erow : sm.erow[4 * h + a]) + Ein - 2060;
           const double2 vv = make_double2(oz::fixed_to_double(Tr, e), oz::fixed_to_double(Ti, e));
           okey = max(okey, amp_key(vv));
-          psi[ix] = vv;
+          pso[ix] = vv;
         }
       }
     };
@@ -829,17 +855,17 @@ void launch_umma(double2* psi, const double2* ga, const double2* gb, const PairP
   }
 }
 
-template <typename IT, int NL>
+template <typename IT, int NL, bool PO>
 void launch_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
-                  const ChainRec* rin, ChainRec* rout, bool want_fixed) {
+                  const ChainRec* rin, ChainRec* rout, bool want_fixed, void* out, const BitPerm* perm) {
   const size_t smem = sizeof(ChSmem);
-  check_cuda(cudaFuncSetAttribute(gate_pair_chain_kernel<IT, PAIR_KRON, NL>,
+  check_cuda(cudaFuncSetAttribute(gate_pair_chain_kernel<IT, PAIR_KRON, NL, PO>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
              "gate_pair_chain_kernel shared memory");
   const uint64_t ntiles = p.ngroups / UM_M;
   const int grid = (int)std::min<uint64_t>(ntiles, (uint64_t)sm_count());  // one CTA per SM (all its TMEM)
-  gate_pair_chain_kernel<IT, PAIR_KRON, NL>
-      <<<grid, CH_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0);
+  gate_pair_chain_kernel<IT, PAIR_KRON, NL, PO>
+      <<<grid, CH_THREADS, smem, s>>>(psi, ga, gb, p, rin, rout, want_fixed ? 1 : 0, out, perm);
 }
 
 int chain_levels() {
@@ -855,19 +881,73 @@ int chain_levels() {
 bool chain_applies(const PairParams& p) { return p.ngroups >= (uint64_t)UM_M && p.ngroups % UM_M == 0; }
 
 void launch_pair_chain(void* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
-                       const ChainRec* rin, ChainRec* rout, bool want_fixed) {
+                       const ChainRec* rin, ChainRec* rout, bool want_fixed, void* out, const BitPerm* perm) {
   const bool i32 = p.ngroups * 16 <= (1ull << 32);
+  if (perm) {
+    if (!i32 || !out || out == psi) throw Error(QTNH_ERR_UNSUPPORTED, "permuted chain output");
+    // the tables travel in stream-ordered workspace, freed after the launch
+    BitPerm* dperm = static_cast<BitPerm*>(workspace_alloc(sizeof(BitPerm), s));
+    cudaError_t e = cudaMemcpyAsync(dperm, perm, sizeof(BitPerm), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      if (chain_levels() == 6)
+        launch_chain<uint32_t, 6, true>(psi, ga, gb, p, s, rin, rout, want_fixed, out, dperm);
+      else
+        launch_chain<uint32_t, 7, true>(psi, ga, gb, p, s, rin, rout, want_fixed, out, dperm);
+      e = cudaGetLastError();
+    }
+    workspace_free(dperm, s);
+    check_cuda(e, "permuted chain launch");
+    return;
+  }
   if (chain_levels() == 6) {
     if (i32)
-      launch_chain<uint32_t, 6>(psi, ga, gb, p, s, rin, rout, want_fixed);
+      launch_chain<uint32_t, 6, false>(psi, ga, gb, p, s, rin, rout, want_fixed, nullptr, nullptr);
     else
-      launch_chain<uint64_t, 6>(psi, ga, gb, p, s, rin, rout, want_fixed);
+      launch_chain<uint64_t, 6, false>(psi, ga, gb, p, s, rin, rout, want_fixed, nullptr, nullptr);
   } else {
     if (i32)
-      launch_chain<uint32_t, 7>(psi, ga, gb, p, s, rin, rout, want_fixed);
+      launch_chain<uint32_t, 7, false>(psi, ga, gb, p, s, rin, rout, want_fixed, nullptr, nullptr);
     else
-      launch_chain<uint64_t, 7>(psi, ga, gb, p, s, rin, rout, want_fixed);
+      launch_chain<uint64_t, 7, false>(psi, ga, gb, p, s, rin, rout, want_fixed, nullptr, nullptr);
   }
+}
+
+bool make_bit_perm(const dims_t& dims, const std::vector<uint16_t>& ptup, const PairParams& p, BitPerm& bp) {
+  const size_t r = dims.size();
+  if (ptup.size() != r) return false;
+  uint32_t total = 0;
+  std::vector<uint32_t> w(r);
+  for (size_t i = 0; i < r; ++i) {
+    const uint32_t l = log2_or_none(dims[i]);
+    if (l == 0xFFFFFFFFu) return false;
+    w[i] = l;
+    total += l;
+  }
+  if (total > 32) return false;
+  dims_t nd(r);
+  for (size_t i = 0; i < r; ++i) nd[ptup[i]] = dims[i];
+  // bit position of the lowest bit of axis i in the input, and of position j in the output
+  std::vector<uint32_t> in_lo(r), out_lo(r);
+  uint32_t acc = 0;
+  for (size_t i = r; i-- > 0;) in_lo[i] = acc, acc += w[i];
+  acc = 0;
+  for (size_t j = r; j-- > 0;) out_lo[j] = acc, acc += log2_or_none(nd[j]);
+  uint32_t dst[32];
+  for (int b = 0; b < 32; ++b) dst[b] = 32;  // bits above the state: never set
+  for (size_t i = 0; i < r; ++i)
+    for (uint32_t k = 0; k < w[i]; ++k) dst[in_lo[i] + k] = out_lo[ptup[i]] + k;
+  for (int t = 0; t < 4; ++t)
+    for (int v = 0; v < 256; ++v) {
+      uint32_t x = 0;
+      for (int k = 0; k < 8; ++k)
+        if (((v >> k) & 1) && dst[8 * t + k] < 32) x |= 1u << dst[8 * t + k];
+      bp.tab[t][v] = x;
+    }
+  for (int c = 0; c < 16; ++c) {
+    const uint32_t o = (uint32_t)p.off[c];
+    bp.poff[c] = bp.tab[0][o & 255u] | bp.tab[1][(o >> 8) & 255u] | bp.tab[2][(o >> 16) & 255u] | bp.tab[3][o >> 24];
+  }
+  return true;
 }
 
 bool launch_pair_umma(double2* psi, const double2* ga, const double2* gb, const PairParams& p, cudaStream_t s,
