@@ -616,9 +616,8 @@ def main_contract(a):
     d2h = sum(16 * M * N for _, _, _, M, N, _ in pairs)
     # copies on two copy streams: the operands of the pairs LOOK ahead go in while this pair
     # contracts (the host link, not the contractions, is the bound of this arm), results come
-    # out of NOUT output buffers in rotation (one copy stream for both directions measured
-    # 33.7 against 65-70 TFLOP/s: each result copy waits for its contraction and holds up
-    # the input copies queued behind it)
+    # out of NOUT output buffers in rotation (one copy stream for both directions, as the
+    # circuit arm uses, measured 33.7 against 65-70 TFLOP/s here)
     LOOK, NOUT = 8, 4
     h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
     outs = [out] + [torch.empty_like(out) for _ in range(NOUT - 1)]
