@@ -135,3 +135,43 @@ def test_plan_rejects_like_reference():
         q.contract_plan(q.Tensor(q.DENSE, [], [2, 2]), q.Tensor(q.DENSE, [], [3]), [(0, 0)])
     with pytest.raises(ValueError):  # contract.cpp:212-214
         q.contract_plan(q.Tensor(q.DENSE, [2], [2]), q.Tensor(q.DENSE, [], [2]), [(0, 0)])
+
+
+def test_gate_runs_argument_checks_before_any_launch():
+    # qtnh_apply_gate_runs checks every argument on the host before the first launch, so
+    # these fail here without a GPU (the device pointers are never touched)
+    L = q.lib()
+    n = 6
+    dims = q._u64([2] * n)
+    state, scratch = ctypes.c_void_p(0x1000), ctypes.c_void_p(0x2000)
+    gates = (ctypes.c_void_p * 4)(0x3000, 0x3100, 0x3200, 0x3300)
+    ks = (ctypes.c_int32 * 4)(2, 2, 2, 2)
+
+    def call(nruns, per_run, targets, ptups, st=state, sc=scratch, rank=n):
+        return L.qtnh_apply_gate_runs(st, sc, ctypes.c_int32(rank), dims, ctypes.c_int32(nruns),
+                                      (ctypes.c_int32 * max(1, len(per_run)))(*per_run), ks, q._u16(targets), gates,
+                                      q._u16(ptups), None)
+
+    ident = list(range(n))
+    good_t = [0, 1, 2, 3, 4, 5, 0, 2]
+    assert call(0, [], good_t, []) == 1                                      # no run
+    assert call(2, [2, 2], good_t, ident, sc=None) == 1                       # no scratch
+    assert call(2, [2, 2], good_t, ident, sc=state) == 1                      # scratch is the state
+    assert call(2, [2, 2], good_t, [0, 1, 2, 3, 4, 4]) == 1                   # not a permutation
+    assert call(2, [2, 2], [0, 1, 2, 3, 4, 6, 0, 2], ident) == 3              # target out of range
+    assert call(2, [2, 2], [0, 1, 2, 3, 4, 5, 1, 1], ident) == 1              # target repeated
+    assert call(2, [2, -1], good_t, ident) == 1                               # negative gate count
+    assert call(1, [2], good_t, [], rank=65) == 1                             # rank beyond QTNH_MAX_RANK
+
+
+def test_gemm_slice_setting_and_gate_timing_on_the_host():
+    L = q.lib()
+    assert q.get_gemm_slice() == 32
+    for bad in (0, -3, 4097):
+        assert L.qtnh_set_gemm_slice(ctypes.c_int(bad)) == 1
+    assert q.get_gemm_slice() == 32
+    q.set_gemm_slice(64)
+    assert q.get_gemm_slice() == 64
+    q.set_gemm_slice(32)
+    # nothing recorded: zero time, zero launches (no device needed)
+    assert q.gate_timing(False) == (0.0, 0)
